@@ -1,0 +1,428 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 step loop: particle-steps/s of the mixed-precision
+form and of the plain FP64 drop-in on one workload, through libmavi_cuda.so.
+
+Default workload (one GPU): 262,144 harmonic-truncated soft disks, periodic
+box at area fraction 0.70, relaxed by 200 overdamped steps, overdamped
+dt = 1e-2 (see mavi.jl_gb300/workloads.py). A "step" is one whole step of the
+step loop (chunk rebuild -> pair forces -> integration -> walls).
+
+Timing: W untimed warm-up steps, then K steps; before every timed step a
+256 MiB buffer is written (L2 flush), then one step runs as a CUDA graph whose
+first and last launch carry CUDA events on the library's own stream; the value
+is N * K / (sum of those device times). Per-kernel device times come from the
+same replays. `e2e` is measured through the C ABI with pinned host buffers:
+upload state -> one step -> download state, host-timed.
+
+--impl reference: the reference's algorithm on the host cores (the CPU
+restatement in oracle/, OpenMP over chunk columns like the reference's
+Threaded mode), on the same workload, a bounded number of steps.
+
+Multi-GPU (torchrun): replicas only — every rank advances its own copy of the
+workload; value = all ranks' particle-steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as graft  # noqa: E402
+
+METRIC = "particle-steps/s on 1 GB300, mixed+batched vs plain FP64, at ≤1e-5 rel force err"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="harm_262144")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def rel_force_err(f, ref):
+    rms = math.sqrt(float(np.mean(np.sum(ref * ref, axis=1))))
+    return float(np.max(np.linalg.norm(f - ref, axis=1)) / max(rms, 1e-300))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[2 + k].lower() == "active"})
+        loaded = [r[0] for r in rows if r[0] > 0.5 * r[1]] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def launches_per_step(step_kind, abi):
+    rebin = 5   # scan reduce, scan tiles, scan apply, scatter, per-chunk order + permutation
+    body = {abi.MAVI_STEP_NEWTON: 2, abi.MAVI_STEP_OVERDAMPED: 1, abi.MAVI_STEP_SZABO: 1, abi.MAVI_STEP_RTP: 1,
+            abi.MAVI_STEP_RINGS: 3}[step_kind]
+    return rebin + body
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def time_form(mg, system, step_func, K, W, flush, torch):
+    """Device-timed steps of one system; returns a dict of measurements."""
+    abi = mg.abi
+    h = system.handle if step_func is None else system._ensure(step_func.kind)
+    lib, hd = h.lib, h.handle
+    h.check(lib.mavi_step(hd, W), "warm-up")
+    h.check(lib.mavi_profile_enable(hd, 1), "profile")
+    h.check(lib.mavi_step(hd, 1), "profiled warm-up")          # captures the profiled graph
+    h.check(lib.mavi_profile_enable(hd, 1), "profile reset")
+    torch.cuda.synchronize()
+    step_ms = []
+    for _ in range(K):
+        flush()
+        torch.cuda.synchronize()
+        h.check(lib.mavi_step(hd, 1), "timed step")
+        p = abi.MaviProfile()
+        lib.mavi_profile_read(hd, C.byref(p))
+        step_ms.append(p.last_step_ms)
+    torch.cuda.synchronize()
+    p = abi.MaviProfile()
+    lib.mavi_profile_read(hd, C.byref(p))
+    h.check(lib.mavi_profile_enable(hd, 0), "profile off")
+    kinds = {abi.MAVI_KERNEL_NAMES[k]: {"ms": p.ms[k], "launches": int(p.launches[k])}
+             for k in range(abi.MAVI_NUM_KERNEL_KINDS) if p.launches[k]}
+    return {"total_ms": float(sum(step_ms)), "step_ms": step_ms, "kinds": kinds,
+            "launches_per_step": launches_per_step(h.step_kind, abi)}
+
+
+def e2e_form(mg, system, step_func, K, torch):
+    """Through the C ABI with pinned host buffers: upload -> 1 step -> download."""
+    h = system._ensure(step_func.kind)
+    lib, hd = h.lib, h.handle
+    n = system.num_slots
+    pos_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    pos_h.copy_(torch.from_numpy(system.state.pos))
+    has_vel = system.state.kind == mg.abi.MAVI_STATE_SECOND_LAW
+    vel_h = None
+    if has_vel:
+        vel_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+        vel_h.copy_(torch.from_numpy(system.state.vel))
+    dp = C.POINTER(C.c_double)
+    pp = C.cast(pos_h.data_ptr(), dp)
+    vp = C.cast(vel_h.data_ptr(), dp) if vel_h is not None else None
+    bi = pos_h.numel() * 8 + (vel_h.numel() * 8 if vel_h is not None else 0)
+    bo = bi
+    for _ in range(3):
+        h.check(lib.mavi_upload_state(hd, pp, vp, None), "upload")
+        h.check(lib.mavi_step(hd, 1), "step")
+        h.check(lib.mavi_download_state(hd, pp, vp, None), "download")
+    t0 = time.perf_counter()
+    for _ in range(K):
+        h.check(lib.mavi_upload_state(hd, pp, vp, None), "upload")
+        h.check(lib.mavi_step(hd, 1), "step")
+        h.check(lib.mavi_download_state(hd, pp, vp, None), "download")
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "h2d": bi, "d2h": bo}
+
+
+def algorithmic_bytes(kind, precision, step_kind, abi):
+    """Algorithmic HBM bytes per particle of one launch of each kernel kind
+    (unique data each launch must move once)."""
+    mixed = precision == "mixed"
+    if kind == "force":
+        # own position (+FP32 offset), uid, replica, chunk, chunk starts (~1/particle);
+        # writes: position, uid, replica, new chunk, rank (+vel for Verlet pass 2)
+        own = 16 + (8 if mixed else 0) + 4 + 4 + 4 + 4
+        out = 16 + 4 + 4 + 4 + 4
+        if step_kind == abi.MAVI_STEP_NEWTON:
+            # pass 1: read x, v; write x', F(t); pass 2: read x', v, F(t); write x, v, ...
+            own += 16 + 16
+            out += 16 + (8 if mixed else 16)
+        return own + out
+    if kind == "bin_sort":
+        return (16 + 4 + 4 + 4) * 2 + 4 + (8 if mixed else 0) + 4
+    if kind == "bin_scatter":
+        return 4 + 4 + 4 + 4
+    if kind == "bin_scan":
+        return 4 * 3
+    return 0
+
+
+# Flops per pair evaluation (sqrt and division count 1 each): HarmTrunc 16,
+# LenJones 23, Szabo 14 (periodic minimum image included).
+FLOPS_PER_PAIR = {0: 16, 1: 23, 2: 14, 3: 23, 4: 16}
+
+
+def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind):
+    kinds = meas["kinds"]
+    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    avg_ms = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1)
+    bpp = algorithmic_bytes(dom, precision, step_kind, abi)
+    traffic_bytes = bpp * n
+    achieved = traffic_bytes / (avg_ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    rf = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+          "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": traffic_bytes,
+          "avg_launch_ms": avg_ms, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    if dom == "force" and candidate_pairs:
+        flops_pair = FLOPS_PER_PAIR[dyn_kind]
+        passes = 2 if step_kind == abi.MAVI_STEP_NEWTON else 1
+        fl = 2 * candidate_pairs * flops_pair * passes   # each unordered pair is evaluated from both sides
+        rf["fp_pipe"] = {"achieved_tflops": fl / (avg_ms * 1e-3) / 1e12,
+                         "peak_tflops": fma_peak / 1e12 if fma_peak else None,
+                         "frac": (fl / (avg_ms * 1e-3)) / fma_peak if fma_peak else None,
+                         "pair_evaluations_per_launch": 2 * candidate_pairs * passes,
+                         "flops_per_pair": flops_pair}
+    return rf
+
+
+def cpu_baseline(mg, orc, system, step_func, seconds, nthreads):
+    o = orc.from_system(system, nthreads=nthreads, step_kind=step_func.kind)
+    mode = orc.THREADED if nthreads > 1 else orc.SEQUENTIAL
+    t0 = time.perf_counter()
+    o.step(1, mode)
+    t1 = time.perf_counter() - t0
+    k = max(1, min(10000, int(seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(k, mode)
+    dt = time.perf_counter() - t0
+    o.close()
+    n = system.num_slots
+    return {"value": n * k / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{k} steps of the full workload (N={n}) after 1 warm-up step, "
+                      f"oracle/mavi_oracle.c, {'Threaded column split' if nthreads > 1 else 'Sequencial'}"}
+
+
+def build_workload(mg, name, precision):
+    W = __import__("mavi_gb300.workloads", fromlist=["WORKLOADS"]).WORKLOADS
+    if name == "harm_262144":
+        return W[name](precision=precision)
+    return W[name](precision=precision)
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    mg = graft.load_package()
+    orc = graft.load_oracle()
+    from mavi_gb300 import workloads
+    nthreads = os.cpu_count() or 1
+    if args.workload != "harm_262144":
+        print(json.dumps({"impl": "reference", "unavailable": f"reference arm runs the default workload only"}))
+        return 0
+    pos, L = workloads.harm_262144_initial()
+    # same relaxation as the GPU arm, on the oracle (the reference's algorithm)
+    sys_ = workloads.harm_system(pos, L, "fp64")
+    o = orc.from_system(sys_, nthreads=nthreads, step_kind=workloads.OVERDAMPED.kind)
+    o.step(200, orc.THREADED)
+    relaxed, _, _ = o.state()
+    o.close()
+    s2 = workloads.harm_system(relaxed, L, "fp64")
+    o = orc.from_system(s2, nthreads=nthreads, step_kind=workloads.OVERDAMPED.kind)
+    o.step(max(args.warmup, 1), orc.THREADED)
+    t1 = time.perf_counter()
+    o.step(1, orc.THREADED)
+    one = time.perf_counter() - t1
+    k = max(1, min(args.steps, int(60.0 / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(k, orc.THREADED)
+    dt = time.perf_counter() - t0
+    n = s2.num_slots
+    v = n * k / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": k,
+            "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "N": n, "box": L, "chunks": [int(L // 2.0)] * 2,
+                       "step": "overdamped", "dt": 1e-2},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{k} steps of the full workload; the reference is Julia, absent on this "
+                                       f"machine: its algorithm restated in C (oracle/), Threaded column split"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_info()
+    if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+        # one GPU per rank: make the rank's GPU device 0 of this process
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    local_dev = 0 if world > 1 else local
+    import torch
+    torch.cuda.set_device(local_dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    mg = graft.load_package()
+    abi = mg.abi
+    lib = mg.load_library()
+    peaks = measured_peaks()
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flush_buf.fill_(1.0)
+
+    results = {}
+    for precision in ("fp64", "mixed"):
+        system, step_func = build_workload(mg, args.workload, precision)
+        results[precision] = {"system": system, "step": step_func}
+
+    # force accuracy at the starting state (both forms and the oracle)
+    f64 = results["fp64"]["system"].calc_forces()
+    fmx = results["mixed"]["system"].calc_forces()
+    err = {"mixed_vs_fp64": rel_force_err(fmx, f64)}
+    stats = results["fp64"]["system"].stats()
+    orc = None
+    if rank == 0 and not args.no_cpu_baseline:
+        orc = graft.load_oracle()
+        o = orc.from_system(results["fp64"]["system"], nthreads=os.cpu_count() or 1,
+                            step_kind=results["fp64"]["step"].kind)
+        fo = o.forces(orc.THREADED)
+        o.close()
+        err["fp64_vs_oracle"] = rel_force_err(f64, fo)
+        err["mixed_vs_oracle"] = rel_force_err(fmx, fo)
+
+    fma = {}
+    for prec, code in (("fp64", abi.MAVI_PREC_FP64), ("mixed", abi.MAVI_PREC_MIXED)):
+        v = C.c_double()
+        fma[prec] = v.value if lib.mavi_fma_peak(code, local_dev, C.byref(v)) == 0 else None
+
+    clocks = Clocks(local)
+    meas = {}
+    for precision in ("fp64", "mixed"):
+        r = results[precision]
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if precision == "mixed":
+            clocks.start()
+        m = time_form(mg, r["system"], r["step"], args.steps, max(args.warmup, 3), flush, torch)
+        if precision == "mixed":
+            clk = clocks.stop()
+        torch.cuda.synchronize()
+        if world > 1:
+            t = torch.tensor([m["total_ms"]], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            m["total_ms"] = float(t.item())
+            dist.barrier()
+        meas[precision] = m
+
+    e2e = e2e_form(mg, results["mixed"]["system"], results["mixed"]["step"], min(args.steps, 300), torch)
+
+    n = results["mixed"]["system"].num_slots
+    K = args.steps
+    line_forms = {}
+    for precision in ("fp64", "mixed"):
+        m = meas[precision]
+        v = world * n * K / (m["total_ms"] * 1e-3)
+        dyn_kind = abi.MaviReplicaParams()
+        results[precision]["system"].fill_params(dyn_kind, results[precision]["step"].kind)
+        rf = roofline(m, n, precision, results[precision]["step"].kind, abi, peaks, stats.candidate_pairs,
+                      fma[precision], dyn_kind.dyn.kind)
+        line_forms[precision] = {"value": v, "ms_per_step": m["total_ms"] / K, "roofline": rf,
+                                 "kernels_ms_per_step": {k: d["ms"] / K for k, d in m["kinds"].items()},
+                                 "gpu_launches": m["launches_per_step"] * K}
+    cpu = None
+    if rank == 0 and orc is not None:
+        cpu = cpu_baseline(mg, orc, results["fp64"]["system"], results["fp64"]["step"], args.cpu_seconds,
+                           os.cpu_count() or 1)
+    if rank == 0:
+        mx = line_forms["mixed"]
+        out = {
+            "metric": METRIC, "value": mx["value"], "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": max(args.warmup, 3), "ms_per_step": mx["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair loop + f64 update",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "N": n, "form": "mixed",
+                       "chunks": [int(stats.total_chunks ** 0.5)] * 2, "candidate_pairs": stats.candidate_pairs,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "roofline": mx["roofline"],
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * n * min(K, 300) / e2e["seconds"], "unit": UNIT,
+                    "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
+                    "path": "mavi_upload_state -> mavi_step(1) -> mavi_download_state, pinned host buffers"},
+            "gpu_launches": mx["gpu_launches"],
+            "clocks": clk,
+            "plain_fp64": {"value": line_forms["fp64"]["value"], "ms_per_step": line_forms["fp64"]["ms_per_step"],
+                           "roofline": line_forms["fp64"]["roofline"],
+                           "kernels_ms_per_step": line_forms["fp64"]["kernels_ms_per_step"],
+                           "gpu_launches": line_forms["fp64"]["gpu_launches"]},
+            "kernels_ms_per_step": mx["kernels_ms_per_step"],
+            "speedup_mixed_vs_fp64": mx["value"] / line_forms["fp64"]["value"],
+            "force_error": err,
+            "fma_peak_tflops": {k: (v / 1e12 if v else None) for k, v in fma.items()},
+        }
+        print(json.dumps(out))
+    for precision in ("fp64", "mixed"):
+        results[precision]["system"].close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

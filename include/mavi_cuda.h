@@ -1,0 +1,306 @@
+/*
+ * mavi_cuda.h — C ABI of libmavi_cuda.so, a GB300 (sm_103a) implementation of
+ * Mavi.jl's step loop: chunk (cell-list) rebuild -> pair forces -> integration
+ * -> wall handling.
+ *
+ * The ABI is plain C: opaque handles, plain pointers, sizes and POD parameter
+ * structs. Host arrays use the reference's memory layout, so a Julia caller can
+ * pass `pointer(state.pos)` of a `Vector{SVector{2,Float64}}` directly:
+ * positions/velocities are interleaved [x1,y1,x2,y2,...] doubles
+ * (reference: src/states.jl:75-79), rings positions are the column-major
+ * (nmax x num_rings) matrix of points (src/rings/states.jl:74-81, 101).
+ * Indices crossing the ABI are 0-based.
+ *
+ * Every entry point returns an int status (MAVI_OK == 0). Device-side failures
+ * (a particle leaving the chunk grid, a chunk over capacity, a non-finite
+ * position) are reported through a device error word that the library reads
+ * back; kernels never trap.
+ *
+ * Thread-safety: one handle must be used by one host thread at a time;
+ * different handles may be used concurrently (each owns its CUDA stream).
+ */
+#ifndef MAVI_CUDA_H
+#define MAVI_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MAVI_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define MAVI_OK                 0
+#define MAVI_ERR_INVALID_ARG    1  /* bad parameter / configuration                          */
+#define MAVI_ERR_CUDA           2  /* a CUDA runtime call failed (see mavi_last_error)       */
+#define MAVI_ERR_OUT_OF_GRID    3  /* particle outside the chunk grid
+                                      (reference raises BoundsError, src/chunks.jl:144-146) */
+#define MAVI_ERR_CHUNK_OVERFLOW 4  /* more particles in a chunk than its capacity
+                                      (reference raises BoundsError, src/chunks.jl:145)     */
+#define MAVI_ERR_NONFINITE      5  /* NaN/Inf position                                       */
+#define MAVI_ERR_OUTSIDE_SPACE  6  /* particles outside the space at construction
+                                      (reference throws, src/systems.jl:76-79)              */
+#define MAVI_ERR_UNSUPPORTED    7  /* combination the reference does not define             */
+#define MAVI_ERR_NO_DEVICE      8  /* no CUDA device available                              */
+#define MAVI_ERR_NOISE_MISSING  9  /* injected-noise mode but no noise supplied for a step  */
+
+/* ---- enums -------------------------------------------------------------- */
+/* State kinds: src/states.jl:75 (SecondLawState), :104 (SelfPropelledState),
+ * src/rings/states.jl:74 (RingsState). */
+#define MAVI_STATE_SECOND_LAW     0
+#define MAVI_STATE_SELF_PROPELLED 1
+#define MAVI_STATE_RINGS          2
+
+/* Dynamic configs: src/configs.jl:341 (HarmTruncCfg), :380 (LenJonesCfg),
+ * :399 (SzaboCfg), :410 (RunTumbleCfg), src/rings/configs.jl:326 (RingsCfg). */
+#define MAVI_DYN_HARM_TRUNC 0
+#define MAVI_DYN_LEN_JONES  1
+#define MAVI_DYN_SZABO      2
+#define MAVI_DYN_RUN_TUMBLE 3
+#define MAVI_DYN_RINGS      4
+
+/* Step functions: src/integration.jl:507 (newton_step!, velocity Verlet),
+ * :517 (szabo_step!), :527 (rtp_step!), src/rings/integration.jl:522 (step!).
+ * MAVI_STEP_OVERDAMPED composes reference pieces the way README.md:331-332 and
+ * examples/custom_step_function.jl:43-61 tell users to write a step:
+ * clean -> update_chunks! -> calc_forces! -> calc_walls_forces! ->
+ * x += mobility*F*dt -> walls! -> time. */
+#define MAVI_STEP_NEWTON     0
+#define MAVI_STEP_SZABO      1
+#define MAVI_STEP_RTP        2
+#define MAVI_STEP_RINGS      3
+#define MAVI_STEP_OVERDAMPED 4
+
+/* Geometries: src/configs.jl:34 (RectangleCfg), :145 (CircleCfg), :137 (LinesCfg). */
+#define MAVI_GEOM_RECTANGLE 0
+#define MAVI_GEOM_CIRCLE    1
+#define MAVI_GEOM_LINES     2
+
+/* Wall types: src/configs.jl:238-244 (Rigid, Periodic, Slippery), :263 (PotentialWalls).
+ * Several MaviSpace entries in one replica form ManyWalls (src/configs.jl:289-302). */
+#define MAVI_WALL_RIGID     0
+#define MAVI_WALL_PERIODIC  1
+#define MAVI_WALL_SLIPPERY  2
+#define MAVI_WALL_POTENTIAL 3
+
+/* PotentialWalls modes: src/configs.jl:255-261. */
+#define MAVI_POTMODE_OUTSIDE   0
+#define MAVI_POTMODE_INSIDE    1
+#define MAVI_POTMODE_REPULSION 2
+
+/* Arithmetic of the pair loop. FP64: every operation in double (the drop-in).
+ * MIXED: positions stay FP64 for update, wrap and binning; the pair loop runs in
+ * FP32 on chunk-centre-relative offsets with compensated FP32 accumulation. */
+#define MAVI_PREC_FP64  0
+#define MAVI_PREC_MIXED 1
+
+/* Noise source for Szabo / RTP / rings updates. INJECTED: the caller supplies
+ * the numbers of each step (mavi_set_noise) so that two implementations can
+ * consume identical noise. DEVICE: counter-based Philox4x32-10 on the GPU. */
+#define MAVI_NOISE_DEVICE   0
+#define MAVI_NOISE_INJECTED 1
+
+/* Potential-energy definitions (mavi_energies). */
+#define MAVI_PE_STENCIL   0  /* over the chunk-stencil pair set the forces use            */
+#define MAVI_PE_ALL_PAIRS 1  /* all pairs i<j, as src/quantities.jl:46-66 does for LJ      */
+
+#define MAVI_MAX_SPACES 4
+#define MAVI_MAX_LINES  16
+#define MAVI_MAX_TYPES  4
+
+/* ---- parameter structs -------------------------------------------------- */
+
+/* One (wall, geometry) entry of a SpaceCfg (src/configs.jl:285-288). */
+typedef struct MaviSpace {
+    int32_t wall;          /* MAVI_WALL_*                                        */
+    int32_t geometry;      /* MAVI_GEOM_*                                        */
+    /* RectangleCfg (src/configs.jl:34-39) */
+    double length, height, bl_x, bl_y;
+    /* CircleCfg (src/configs.jl:145-148) */
+    double radius, cx, cy;
+    /* LinesCfg (src/configs.jl:137-140): segments (x1,y1,x2,y2) and optional bbox */
+    int32_t num_lines;
+    int32_t has_bbox;
+    double lines[MAVI_MAX_LINES][4];
+    double bbox_length, bbox_height, bbox_bl_x, bbox_bl_y;
+    /* PotentialWalls (src/configs.jl:263-279): potential kind (MAVI_DYN_HARM_TRUNC
+     * or MAVI_DYN_LEN_JONES), mode (MAVI_POTMODE_*), parameters
+     * HarmTrunc: {k_rep, k_atr, dist_eq, dist_max}; LenJones: {sigma, epsilon, 0, 0} */
+    int32_t pot_kind;
+    int32_t pot_mode;
+    double pot_params[4];
+} MaviSpace;
+
+/* Per-type rings parameters (src/rings/configs.jl:326-338) and the
+ * InteractionMatrix of HarmTruncCfg (src/rings/configs.jl:257-262, 292-316).
+ * k_bend is an addition (bending term, zero reproduces the reference). */
+typedef struct MaviRingsCfg {
+    int32_t num_types;
+    int32_t num_rings;
+    int32_t nmax;                           /* rows of rings_pos (max particles per ring) */
+    int32_t _pad0;
+    int32_t num_particles[MAVI_MAX_TYPES];  /* particles per ring of each type          */
+    double p0[MAVI_MAX_TYPES];
+    double relax_time[MAVI_MAX_TYPES];
+    double vo[MAVI_MAX_TYPES];
+    double mobility[MAVI_MAX_TYPES];
+    double rot_diff[MAVI_MAX_TYPES];
+    double k_area[MAVI_MAX_TYPES];
+    double k_spring[MAVI_MAX_TYPES];
+    double l_spring[MAVI_MAX_TYPES];
+    double k_bend[MAVI_MAX_TYPES];
+    double inter_k_rep[MAVI_MAX_TYPES][MAVI_MAX_TYPES];
+    double inter_k_atr[MAVI_MAX_TYPES][MAVI_MAX_TYPES];
+    double inter_dist_eq[MAVI_MAX_TYPES][MAVI_MAX_TYPES];
+    double inter_dist_max[MAVI_MAX_TYPES][MAVI_MAX_TYPES];
+} MaviRingsCfg;
+
+/* Dynamic configuration (src/configs.jl:341-415). Fields not used by `kind`
+ * are ignored. */
+typedef struct MaviDynamicCfg {
+    int32_t kind;          /* MAVI_DYN_*                                         */
+    int32_t _pad0;
+    double k_rep, k_atr, dist_eq, dist_max;                 /* HarmTruncCfg        */
+    double sigma, epsilon;                                  /* LenJonesCfg / RTP   */
+    double vo, mobility, relax_time, k_adh, r_eq, r_max, rot_diff; /* SzaboCfg     */
+    double tumble_rate;                                     /* RunTumbleCfg        */
+} MaviDynamicCfg;
+
+/* One independent system (a Julia `System`, src/systems.jl:45-72). */
+typedef struct MaviReplicaParams {
+    int64_t num_particles;   /* slots: N, or nmax*num_rings for rings              */
+    int32_t state_kind;      /* MAVI_STATE_*                                       */
+    int32_t step_kind;       /* MAVI_STEP_*                                        */
+    int32_t num_spaces;      /* 1..MAVI_MAX_SPACES; >1 means ManyWalls             */
+    int32_t chunk_cols;      /* ChunksCfg.num_cols (src/configs.jl:477-480);      */
+    int32_t chunk_rows;      /*   0/0 = no chunks: all-pairs forces               */
+    int32_t _pad0;
+    double dt;               /* IntCfg.dt (src/configs.jl:482-487)                 */
+    MaviSpace spaces[MAVI_MAX_SPACES];
+    MaviDynamicCfg dyn;
+    MaviRingsCfg rings;
+} MaviReplicaParams;
+
+/* Options shared by all replicas of a handle. */
+typedef struct MaviOptions {
+    int32_t precision;       /* MAVI_PREC_*                                        */
+    int32_t noise_mode;      /* MAVI_NOISE_*                                       */
+    uint64_t seed;           /* Philox key for MAVI_NOISE_DEVICE                    */
+    int32_t device;          /* CUDA device ordinal                                */
+    int32_t use_graph;       /* capture the step in a CUDA graph when nonzero      */
+    int32_t block_size;      /* threads per block for particle kernels (0 = tuned) */
+    int32_t _pad0;
+} MaviOptions;
+
+/* Work counters of the last force pass (for roofline accounting). */
+typedef struct MaviStats {
+    int64_t candidate_pairs;  /* chunk-stencil pairs, each unordered pair once     */
+    int64_t total_particles;
+    int64_t total_chunks;
+    int32_t max_chunk_count;  /* largest chunk occupancy at the last rebuild        */
+    int32_t _pad0;
+} MaviStats;
+
+/* Per-kernel device time accumulated while profiling is on (milliseconds). */
+#define MAVI_KERNEL_BIN_COUNT   0  /* chunk index + histogram (fused into update)   */
+#define MAVI_KERNEL_BIN_SCAN    1
+#define MAVI_KERNEL_BIN_SCATTER 2
+#define MAVI_KERNEL_BIN_SORT    3  /* per-chunk order + state permutation           */
+#define MAVI_KERNEL_FORCE       4  /* pair-force passes (all of them)               */
+#define MAVI_KERNEL_UPDATE      5  /* integration + walls (+ rings terms)           */
+#define MAVI_KERNEL_OTHER       6
+#define MAVI_NUM_KERNEL_KINDS   7
+
+typedef struct MaviProfile {
+    double ms[MAVI_NUM_KERNEL_KINDS];
+    int64_t launches[MAVI_NUM_KERNEL_KINDS];
+    int64_t steps;
+    double step_ms;      /* device time from the first to the last launch of each step */
+    double last_step_ms; /* the same for the most recent step                          */
+} MaviProfile;
+
+typedef struct MaviSystem MaviSystem;
+
+/* ---- entry points ------------------------------------------------------- */
+
+int         mavi_abi_version(void);
+const char* mavi_status_string(int status);
+
+/* Build a handle for `num_replicas` independent systems and upload their state.
+ * Mirrors `System(...)` (src/systems.jl:73-114): validates that particles are
+ * inside the space (check_inside, src/space_checks.jl:53-60), sizes the chunk
+ * grid on the geometry's bounding box (get_chunks, src/systems.jl:14-28,
+ * capacity src/chunks.jl:26-40) and runs the first update_chunks!. Rings
+ * systems also run the first force evaluation (src/rings/rings.jl:280-290).
+ * Host arrays are concatenated over replicas in replica order:
+ *   pos, vel : 2*num_particles doubles per replica (vel NULL unless SecondLaw)
+ *   pol      : num_particles (SelfPropelled) or num_rings (Rings) doubles, else NULL
+ *   ring_types: num_rings int32 (1-based type ids as in the reference) or NULL */
+int mavi_create(const MaviOptions* opt, int32_t num_replicas,
+                const MaviReplicaParams* replicas,
+                const double* pos, const double* vel, const double* pol,
+                const int32_t* ring_types, MaviSystem** out);
+int mavi_destroy(MaviSystem* sys);
+
+/* Advance every replica `num_steps` steps with the replica's step function
+ * (get_step_function, src/integration.jl:537-548; rings src/rings/integration.jl:545),
+ * replacing `run_system(system; num_steps)` (src/run_system.jl:7-23). */
+int mavi_step(MaviSystem* sys, int64_t num_steps);
+
+/* update_chunks! for every replica (src/chunks.jl:150-161). */
+int mavi_update_chunks(MaviSystem* sys);
+
+/* Chunk contents of one replica in the reference layout
+ * chunk_particles[cap, rows, cols] / num_particles_in_chunk[rows, cols]
+ * (column-major, src/chunks.jl:23-24, 35-36); particle ids are 0-based and
+ * ascending inside a chunk, as update_chunks! leaves them. `cap` is the
+ * capacity returned by mavi_chunk_geometry. */
+int mavi_chunk_geometry(MaviSystem* sys, int32_t replica, int32_t* rows,
+                        int32_t* cols, int32_t* cap);
+int mavi_get_chunks(MaviSystem* sys, int32_t replica, int32_t* num_in_chunk,
+                    int32_t* chunk_particles);
+
+/* One force evaluation on the current state: clean_forces! + update_chunks! +
+ * calc_forces! (src/integration.jl:112-224, rings src/rings/integration.jl:197-226)
+ * and, when include_walls != 0, calc_walls_forces! (src/integration.jl:228-266).
+ * Writes forces of all replicas (2*N doubles, user particle order). */
+int mavi_calc_forces(MaviSystem* sys, int32_t include_walls, double* forces_out);
+
+/* Copy host state in / out (user particle order, same layout as mavi_create). */
+int mavi_upload_state(MaviSystem* sys, const double* pos, const double* vel,
+                      const double* pol);
+int mavi_download_state(MaviSystem* sys, double* pos, double* vel, double* pol);
+
+/* Noise for the next step in MAVI_NOISE_INJECTED mode: per replica, Szabo uses
+ * one standard normal per particle (src/integration.jl:460), RTP two uniforms
+ * per particle (src/integration.jl:493-495), rings one standard normal per ring
+ * (src/rings/integration.jl:348). `count` must equal mavi_noise_count(). */
+int64_t mavi_noise_count(MaviSystem* sys);
+int mavi_set_noise(MaviSystem* sys, const double* noise, int64_t count);
+int mavi_set_seed(MaviSystem* sys, uint64_t seed);
+
+/* Kinetic energy (src/quantities.jl:12-18) and potential energy per replica.
+ * pe_mode: MAVI_PE_STENCIL or MAVI_PE_ALL_PAIRS. Outputs num_replicas doubles. */
+int mavi_energies(MaviSystem* sys, int32_t pe_mode, double* ke, double* pe);
+
+/* time_info (src/systems.jl:30-33, src/integration.jl:500-503). */
+int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
+
+int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
+int mavi_profile_enable(MaviSystem* sys, int32_t on);
+int mavi_profile_read(MaviSystem* sys, MaviProfile* prof);
+
+/* Message of the last failure on this handle (NUL-terminated, truncated). */
+int mavi_last_error(MaviSystem* sys, char* buf, int32_t len);
+
+/* Measured FMA throughput of one GPU (FLOP/s, 2 per FMA) for
+ * MAVI_PREC_FP64 (double) or MAVI_PREC_MIXED (float): the denominators of the
+ * pair-force roofline. A measurement utility; the reference has no
+ * counterpart. */
+int mavi_fma_peak(int32_t precision, int32_t device, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAVI_CUDA_H */

@@ -1,0 +1,810 @@
+// mavi_api.cu — host runtime and C ABI of libmavi_cuda.so (declared in
+// include/mavi_cuda.h). One handle = a batch of independent replicas on one
+// GPU, one CUDA stream, all device buffers preallocated at creation.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "mavi_system.cuh"
+
+using namespace mavi;
+
+// ---------------------------------------------------------------------------
+// launch sequences shared by both precisions
+// ---------------------------------------------------------------------------
+static void launch_count(MaviSystem* s) {
+    record_begin(s, MAVI_KERNEL_BIN_COUNT);
+    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
+    k_count<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+    record_end(s, MAVI_KERNEL_BIN_COUNT);
+}
+
+// update_chunks! (src/chunks.jl:150-161): chunk lists from the histogram of the
+// *_out state: scan -> scatter -> per-chunk order + permutation into *_cur.
+static void launch_rebin(MaviSystem* s, bool advance) {
+    if (!s->counts_valid) launch_count(s);
+    record_begin(s, MAVI_KERNEL_BIN_SCAN);
+    k_scan_reduce<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->tile_sum);
+    k_scan_tiles<<<1, 1024, 0, s->stream>>>(s->tile_sum, s->ntiles, s->C.start, s->Ctot, s->C.d_step, advance ? 1 : 0);
+    k_scan_apply<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->tile_sum, s->C.start);
+    record_end(s, MAVI_KERNEL_BIN_SCAN);
+    record_begin(s, MAVI_KERNEL_BIN_SCATTER);
+    k_scatter<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+    record_end(s, MAVI_KERNEL_BIN_SCATTER);
+    record_begin(s, MAVI_KERNEL_BIN_SORT);
+    if (s->prec == MAVI_PREC_FP64) sort_permute_fp64(s);
+    else sort_permute_mixed(s);
+    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
+    record_end(s, MAVI_KERNEL_BIN_SORT);
+    s->counts_valid = false;
+}
+
+// One whole step; its last kernel leaves the histogram for the next step.
+static void launch_step(MaviSystem* s) {
+    if (s->profiling) {
+        cudaEventRecord(s->ev.step_a, s->stream);
+        s->ev.step_used = 1;
+    }
+    launch_rebin(s, true);
+    if (s->prec == MAVI_PREC_FP64) step_body_fp64(s);
+    else step_body_mixed(s);
+    if (s->profiling) cudaEventRecord(s->ev.step_b, s->stream);
+    s->counts_valid = true;
+}
+
+// ---------------------------------------------------------------------------
+// host-side configuration helpers
+// ---------------------------------------------------------------------------
+// particle_radius (src/configs.jl:418-421); rings: minimum over types, as
+// get_chunks uses (src/systems.jl:26, src/rings/configs.jl:438-443).
+static double particle_radius_of(const MaviReplicaParams& p) {
+    const MaviDynamicCfg& d = p.dyn;
+    switch (d.kind) {
+    case MAVI_DYN_LEN_JONES: return d.sigma * std::pow(2.0, 1.0 / 6.0) / 2;
+    case MAVI_DYN_SZABO: return d.r_eq / 2;
+    case MAVI_DYN_RUN_TUMBLE: return d.sigma * std::pow(2.0, 1.0 / 6.0) / 2;
+    case MAVI_DYN_HARM_TRUNC: return d.dist_eq / 2.0;
+    case MAVI_DYN_RINGS: {
+        double m = INFINITY;
+        for (int t = 0; t < p.rings.num_types; t++) m = std::min(m, p.rings.inter_dist_eq[t][t] / 2.0);
+        return m;
+    }
+    }
+    return NAN;
+}
+
+static void bbox_of_space(const MaviSpace& sp, double& len, double& h, double& blx, double& bly) {
+    if (sp.geometry == MAVI_GEOM_RECTANGLE) {
+        len = sp.length; h = sp.height; blx = sp.bl_x; bly = sp.bl_y;
+    } else if (sp.geometry == MAVI_GEOM_CIRCLE) {
+        double r = sp.radius;
+        len = 2 * r; h = 2 * r; blx = sp.cx - r; bly = sp.cy - r;
+    } else if (sp.has_bbox) {
+        len = sp.bbox_length; h = sp.bbox_height; blx = sp.bbox_bl_x; bly = sp.bbox_bl_y;
+    } else {
+        double mxx = -INFINITY, mnx = INFINITY, mxy = -INFINITY, mny = INFINITY;
+        for (int l = 0; l < sp.num_lines; l++)
+            for (int e = 0; e < 2; e++) {
+                double x = sp.lines[l][2 * e], y = sp.lines[l][2 * e + 1];
+                mxx = std::max(mxx, x); mnx = std::min(mnx, x);
+                mxy = std::max(mxy, y); mny = std::min(mny, y);
+            }
+        len = mxx - mnx; h = mxy - mny; blx = mnx; bly = mny;
+    }
+}
+
+// get_bounding_box incl. the ManyGeometries fold (src/configs.jl:68-77, 188-229)
+static void bbox_of(const MaviReplicaParams& p, double& len, double& h, double& blx, double& bly) {
+    bbox_of_space(p.spaces[0], len, h, blx, bly);
+    for (int k = 1; k < p.num_spaces; k++) {
+        double l2, h2, x2, y2;
+        bbox_of_space(p.spaces[k], l2, h2, x2, y2);
+        double max_x = std::max(blx + len, x2 + l2), max_y = std::max(bly + h, y2 + h2);
+        double min_x = std::min(blx, x2), min_y = std::min(bly, y2);
+        h = max_y - min_y; len = max_x - min_x; blx = min_x; bly = min_y;
+    }
+}
+
+// Real particles of a replica (rings: FixRingsIds p_ids, src/rings/states.jl:46-62).
+static int64_t active_count(const MaviReplicaParams& p, const int32_t* types) {
+    if (p.state_kind != MAVI_STATE_RINGS) return p.num_particles;
+    int64_t a = 0;
+    for (int r = 0; r < p.rings.num_rings; r++) {
+        int t = types ? types[r] - 1 : 0;
+        a += p.rings.num_particles[t];
+    }
+    return a;
+}
+
+static int validate(MaviSystem* s, const MaviReplicaParams& p, int idx, const int32_t* types) {
+    if (p.num_particles < 1) return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: num_particles must be >= 1", idx);
+    if (p.num_spaces < 1 || p.num_spaces > MAVI_MAX_SPACES)
+        return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: num_spaces must be in 1..%d", idx, MAVI_MAX_SPACES);
+    if (!(p.dt > 0)) return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: dt must be > 0", idx);
+    bool sl = p.state_kind == MAVI_STATE_SECOND_LAW, sp_ = p.state_kind == MAVI_STATE_SELF_PROPELLED,
+         rg = p.state_kind == MAVI_STATE_RINGS;
+    switch (p.step_kind) {
+    case MAVI_STEP_NEWTON:
+        if (!sl) return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: newton_step! needs a SecondLawState", idx);
+        if (p.dyn.kind == MAVI_DYN_RINGS) return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: rings need the rings step", idx);
+        break;
+    case MAVI_STEP_OVERDAMPED:
+        if (!(sl || sp_))
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: overdamped step needs a SecondLaw or SelfPropelled state", idx);
+        if (p.dyn.kind == MAVI_DYN_RINGS) return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: rings need the rings step", idx);
+        break;
+    case MAVI_STEP_SZABO:
+        if (!sp_ || p.dyn.kind != MAVI_DYN_SZABO)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: szabo_step! needs SelfPropelledState + SzaboCfg", idx);
+        break;
+    case MAVI_STEP_RTP:
+        if (!sp_ || p.dyn.kind != MAVI_DYN_RUN_TUMBLE)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: rtp_step! needs SelfPropelledState + RunTumbleCfg", idx);
+        break;
+    case MAVI_STEP_RINGS:
+        if (!rg || p.dyn.kind != MAVI_DYN_RINGS)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: rings step needs RingsState + RingsCfg", idx);
+        break;
+    default:
+        return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: unknown step kind %d", idx, p.step_kind);
+    }
+    if (rg) {
+        const MaviRingsCfg& rc = p.rings;
+        if (rc.num_types < 1 || rc.num_types > MAVI_MAX_TYPES)
+            return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: num_types must be in 1..%d", idx, MAVI_MAX_TYPES);
+        if (rc.num_rings < 1 || rc.nmax < 3 || (int64_t)rc.num_rings * rc.nmax != p.num_particles)
+            return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: num_particles must equal nmax*num_rings", idx);
+        if (rc.nmax > kRingMax)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: rings with more than %d particles", idx, kRingMax);
+        for (int t = 0; t < rc.num_types; t++)
+            if (rc.num_particles[t] < 3 || rc.num_particles[t] > rc.nmax)
+                return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: ring type %d size out of range", idx, t + 1);
+        if (types)
+            for (int r = 0; r < rc.num_rings; r++)
+                if (types[r] < 1 || types[r] > rc.num_types)
+                    return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: ring %d has type %d", idx, r, types[r]);
+    }
+    for (int k = 0; k < p.num_spaces; k++) {
+        const MaviSpace& sp = p.spaces[k];
+        if (sp.geometry == MAVI_GEOM_LINES && (sp.num_lines < 1 || sp.num_lines > MAVI_MAX_LINES))
+            return fail(s, MAVI_ERR_INVALID_ARG, "replica %d: num_lines must be in 1..%d", idx, MAVI_MAX_LINES);
+        if (sp.wall == MAVI_WALL_RIGID && !sl)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: RigidWalls reflect velocities; the state has none", idx);
+        if (sp.wall == MAVI_WALL_RIGID && sp.geometry == MAVI_GEOM_LINES)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: RigidWalls on LinesCfg is not defined", idx);
+        if (sp.wall == MAVI_WALL_PERIODIC && sp.geometry == MAVI_GEOM_LINES)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: PeriodicWalls on LinesCfg is not defined", idx);
+        if (sp.wall == MAVI_WALL_POTENTIAL && sp.geometry == MAVI_GEOM_RECTANGLE)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: PotentialWalls need a CircleCfg or LinesCfg", idx);
+        if (sp.wall == MAVI_WALL_SLIPPERY && sp.geometry == MAVI_GEOM_RECTANGLE)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: SlipperyWalls need a CircleCfg or LinesCfg", idx);
+    }
+    bool chunks = p.chunk_cols > 0 && p.chunk_rows > 0;
+    if (chunks) {
+        if (p.spaces[0].wall == MAVI_WALL_PERIODIC && (p.chunk_cols < 3 || p.chunk_rows < 3))
+            return fail(s, MAVI_ERR_UNSUPPORTED,
+                        "replica %d: periodic chunk grid needs >= 3 rows and cols (the reference's stencil "
+                        "repeats chunks below that)", idx);
+        if (p.spaces[0].wall != MAVI_WALL_PERIODIC && p.chunk_cols < 2)
+            return fail(s, MAVI_ERR_UNSUPPORTED, "replica %d: open chunk grid needs >= 2 columns", idx);
+    }
+    return MAVI_OK;
+}
+
+// check_inside (src/space_checks.jl:9-37, 53-60): the circle test ignores
+// the centre, as the reference does.
+static bool outside_space(const MaviReplicaParams& p, const double* pos, const int32_t* types) {
+    if (p.num_spaces != 1) return false;
+    const MaviSpace& sp = p.spaces[0];
+    for (int64_t i = 0; i < p.num_particles; i++) {
+        if (p.state_kind == MAVI_STATE_RINGS) {
+            int64_t ring = i / p.rings.nmax, k = i % p.rings.nmax;
+            int t = types ? types[ring] - 1 : 0;
+            if (k >= p.rings.num_particles[t]) continue;
+        }
+        double x = pos[2 * i], y = pos[2 * i + 1];
+        if (sp.geometry == MAVI_GEOM_RECTANGLE) {
+            if (x < sp.bl_x || y < sp.bl_y || x > sp.bl_x + sp.length || y > sp.bl_y + sp.height) return true;
+        } else if (sp.geometry == MAVI_GEOM_CIRCLE) {
+            if (x * x + y * y > sp.radius * sp.radius) return true;
+        }
+    }
+    return false;
+}
+
+// Pair-law constants in the packing the kernels expect (mavi_device.cuh).
+static void pack_pair_params(const MaviDynamicCfg& d, DevRep& R) {
+    for (int k = 0; k < 8; k++) R.pd[k] = 0;
+    switch (d.kind) {
+    case MAVI_DYN_HARM_TRUNC:
+        R.pd[0] = d.k_rep; R.pd[1] = d.k_atr; R.pd[2] = 1.0 / d.dist_eq; R.pd[3] = d.dist_eq * d.dist_eq;
+        R.pd[4] = d.dist_max * d.dist_max; R.pd[5] = d.dist_eq; R.pd[6] = d.dist_max;
+        break;
+    case MAVI_DYN_LEN_JONES:
+    case MAVI_DYN_RUN_TUMBLE: {
+        double s6 = std::pow(d.sigma, 6.0), s12 = std::pow(d.sigma, 12.0);
+        R.pd[0] = 48 * d.epsilon * s12; R.pd[1] = 24 * d.epsilon * s6;
+        double cut = std::pow(2.0, 1.0 / 6.0) * d.sigma;
+        R.pd[2] = cut * cut;
+        R.pd[4] = 4 * d.epsilon; R.pd[5] = s12; R.pd[6] = s6; R.pd[7] = cut * cut;
+        break;
+    }
+    case MAVI_DYN_SZABO:
+        R.pd[0] = d.k_rep / (d.r_max - d.r_eq); R.pd[1] = d.k_adh / d.r_eq; R.pd[2] = d.r_eq; R.pd[3] = d.r_max;
+        R.pd[4] = d.r_max * d.r_max;
+        break;
+    }
+    for (int k = 0; k < 8; k++) R.pf[k] = (float)R.pd[k];
+}
+
+static int check_device_error(MaviSystem* s) {
+    DevError e{};
+    CUDA_TRY(s, cudaMemcpyAsync(&e, s->C.err, sizeof(DevError), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    if (e.code == 0) return MAVI_OK;
+    int32_t uid = -1;
+    if (e.slot >= 0 && e.slot < s->M) cudaMemcpy(&uid, s->C.uid_out + e.slot, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    DevError z{};
+    cudaMemcpy(s->C.err, &z, sizeof(DevError), cudaMemcpyHostToDevice);
+    switch (e.code) {
+    case MAVI_ERR_OUT_OF_GRID:
+        return fail(s, e.code, "particle %d left the chunk grid (row*1000003+col = %lld)", uid, (long long)e.aux);
+    case MAVI_ERR_CHUNK_OVERFLOW:
+        return fail(s, e.code, "chunk %lld holds more particles than its capacity (particle %d)", (long long)e.aux, uid);
+    case MAVI_ERR_NONFINITE:
+        return fail(s, e.code, "particle %d has a non-finite position", uid);
+    }
+    return fail(s, e.code, "device error %d", e.code);
+}
+
+static void drop_graph(MaviSystem* s) {
+    if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+    if (s->graph) { cudaGraphDestroy(s->graph); s->graph = nullptr; }
+}
+
+// Captures one whole step (assuming a valid histogram, which every step
+// leaves behind). With profiling on, the event records are captured too and
+// replayed with the graph.
+static int ensure_graph(MaviSystem* s) {
+    if (s->graph_exec && s->graph_profiled == s->profiling) return MAVI_OK;
+    drop_graph(s);
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
+    CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    s->counts_valid = true;
+    launch_step(s);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &s->graph);
+    if (e != cudaSuccess) return fail(s, MAVI_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    CUDA_TRY(s, cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) {
+        s->graph_ev_used[k] = s->ev.used[k];
+        s->ev.used[k] = 0;
+    }
+    s->graph_step_used = s->ev.step_used;
+    s->ev.step_used = 0;
+    s->graph_profiled = s->profiling;
+    return MAVI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int mavi_abi_version(void) { return MAVI_ABI_VERSION; }
+
+const char* mavi_status_string(int st) {
+    switch (st) {
+    case MAVI_OK: return "ok";
+    case MAVI_ERR_INVALID_ARG: return "invalid argument";
+    case MAVI_ERR_CUDA: return "CUDA error";
+    case MAVI_ERR_OUT_OF_GRID: return "particle outside the chunk grid";
+    case MAVI_ERR_CHUNK_OVERFLOW: return "chunk over capacity";
+    case MAVI_ERR_NONFINITE: return "non-finite position";
+    case MAVI_ERR_OUTSIDE_SPACE: return "particles outside the space";
+    case MAVI_ERR_UNSUPPORTED: return "unsupported configuration";
+    case MAVI_ERR_NO_DEVICE: return "no CUDA device";
+    case MAVI_ERR_NOISE_MISSING: return "noise not supplied";
+    }
+    return "unknown status";
+}
+
+int mavi_destroy(MaviSystem* s) {
+    if (!s) return MAVI_OK;
+    drop_graph(s);
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++)
+        for (int u = 0; u < 4; u++) {
+            if (s->ev.a[k][u]) cudaEventDestroy(s->ev.a[k][u]);
+            if (s->ev.b[k][u]) cudaEventDestroy(s->ev.b[k][u]);
+        }
+    if (s->ev.step_a) cudaEventDestroy(s->ev.step_a);
+    if (s->ev.step_b) cudaEventDestroy(s->ev.step_b);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return MAVI_OK;
+}
+
+int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaParams* replicas,
+                const double* pos, const double* vel, const double* pol, const int32_t* ring_types,
+                MaviSystem** out) {
+    if (!out) return MAVI_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (!opt || !replicas || num_replicas < 1 || !pos) return MAVI_ERR_INVALID_ARG;
+    MaviSystem* s = new MaviSystem();
+    s->opt = *opt;
+    s->R = num_replicas;
+    s->params.assign(replicas, replicas + num_replicas);
+    s->prec = opt->precision;
+    if (s->prec != MAVI_PREC_FP64 && s->prec != MAVI_PREC_MIXED) {
+        delete s;
+        return MAVI_ERR_INVALID_ARG;
+    }
+    const MaviReplicaParams& p0 = replicas[0];
+    s->dyn = p0.dyn.kind;
+    s->step_kind = p0.step_kind;
+    s->state_kind = p0.state_kind;
+    s->has_vel = s->state_kind == MAVI_STATE_SECOND_LAW;
+    s->has_pol = s->state_kind == MAVI_STATE_SELF_PROPELLED;
+    s->is_rings = s->state_kind == MAVI_STATE_RINGS;
+    if (s->has_vel && !vel) { delete s; return MAVI_ERR_INVALID_ARG; }
+    if ((s->has_pol || s->is_rings) && !pol) { delete s; return MAVI_ERR_INVALID_ARG; }
+
+    // per-replica layout
+    int64_t slot0 = 0, a0 = 0, c0 = 0, ring0 = 0, noise0 = 0;
+    const int32_t* types_cursor = ring_types;
+    int st = MAVI_OK;
+    for (int r = 0; r < num_replicas; r++) {
+        const MaviReplicaParams& p = replicas[r];
+        if (p.dyn.kind != s->dyn || p.step_kind != s->step_kind || p.state_kind != s->state_kind) {
+            st = fail(s, MAVI_ERR_UNSUPPORTED, "all replicas of a handle must share state, dynamics and step kinds");
+            break;
+        }
+        const int32_t* types = s->is_rings ? types_cursor : nullptr;
+        if ((st = validate(s, p, r, types))) break;
+        if (outside_space(p, pos + 2 * slot0, types)) {
+            st = fail(s, MAVI_ERR_OUTSIDE_SPACE, "replica %d: particles outside the space", r);
+            break;
+        }
+        DevRep R{};
+        R.slot0 = slot0;
+        R.nslots = p.num_particles;
+        R.a0 = a0;
+        R.na = active_count(p, types);
+        R.c0 = c0;
+        R.ring0 = ring0;
+        R.noise0 = noise0;
+        R.dt = p.dt;
+        R.num_spaces = p.num_spaces;
+        R.radius = particle_radius_of(p);
+        bbox_of(p, R.bb_len, R.bb_h, R.bb_blx, R.bb_bly);
+        R.has_chunks = p.chunk_cols > 0 && p.chunk_rows > 0;
+        if (R.has_chunks) {
+            R.rows = p.chunk_rows;
+            R.cols = p.chunk_cols;
+            R.chunk_l = R.bb_len / R.cols;
+            R.chunk_h = R.bb_h / R.rows;
+            // capacity (src/chunks.jl:32-34)
+            double nc = (std::ceil(0.5 * R.chunk_l / R.radius) + 1) * (std::ceil(0.5 * R.chunk_h / R.radius) + 1);
+            R.cap = (int32_t)std::ceil(nc * 2);
+        } else {
+            R.rows = 1; R.cols = 1;
+            R.chunk_l = R.bb_len; R.chunk_h = R.bb_h;
+            R.cap = 1 << 30;
+        }
+        R.periodic = p.spaces[0].wall == MAVI_WALL_PERIODIC;
+        R.min_image = p.spaces[0].wall == MAVI_WALL_PERIODIC && p.spaces[0].geometry == MAVI_GEOM_RECTANGLE;
+        R.box_x = p.spaces[0].length;
+        R.box_y = p.spaces[0].height;
+        R.half_box_x = R.box_x / 2;
+        R.half_box_y = R.box_y / 2;
+        R.chunk_lf = (float)R.chunk_l; R.chunk_hf = (float)R.chunk_h;
+        R.box_xf = (float)R.box_x; R.box_yf = (float)R.box_y;
+        R.half_box_xf = (float)R.half_box_x; R.half_box_yf = (float)R.half_box_y;
+        for (int k = 0; k < p.num_spaces; k++) {
+            if (p.spaces[k].wall == MAVI_WALL_POTENTIAL) R.has_wall_forces = 1;
+            else R.has_walls = 1;
+        }
+        pack_pair_params(p.dyn, R);
+        R.mobility = p.dyn.mobility;
+        R.vo = p.dyn.vo;
+        R.relax_time = p.dyn.relax_time;
+        R.rot_diff = p.dyn.rot_diff;
+        R.tumble_rate = p.dyn.tumble_rate;
+        if (s->is_rings) {
+            R.num_rings = p.rings.num_rings;
+            R.nmax = p.rings.nmax;
+        }
+        s->reps_h.push_back(R);
+        s->rep_active.push_back(R.na);
+        slot0 += p.num_particles;
+        a0 += R.na;
+        c0 += (int64_t)R.rows * R.cols;
+        if (s->is_rings) {
+            ring0 += p.rings.num_rings;
+            if (types_cursor) types_cursor += p.rings.num_rings;
+        }
+        int64_t nz = 0;
+        if (s->step_kind == MAVI_STEP_SZABO) nz = p.num_particles;
+        else if (s->step_kind == MAVI_STEP_RTP) nz = 2 * p.num_particles;
+        else if (s->step_kind == MAVI_STEP_RINGS) nz = p.rings.num_rings;
+        noise0 += nz;
+    }
+    if (st) {
+        std::string msg = s->last_error;
+        delete s;
+        fprintf(stderr, "mavi_create: %s\n", msg.c_str());
+        return st;
+    }
+    s->Nslots = slot0;
+    s->M = a0;
+    s->Ctot = c0;
+    s->total_rings = ring0;
+    s->noise_count = noise0;
+    s->ntiles = (s->Ctot + kScanTile - 1) / kScanTile;
+    if (s->Nslots >= (1ll << 31) || s->M >= (1ll << 31) || s->Ctot >= (1ll << 31) - 1) {
+        delete s;
+        return MAVI_ERR_UNSUPPORTED;
+    }
+    s->num_steps.assign(num_replicas, 0);
+    s->time.assign(num_replicas, 0.0);
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        delete s;
+        return MAVI_ERR_NO_DEVICE;
+    }
+    if (cudaSetDevice(opt->device) != cudaSuccess) {
+        delete s;
+        return MAVI_ERR_NO_DEVICE;
+    }
+    auto bail = [&](int code) {
+        fprintf(stderr, "mavi_create: %s\n", s->last_error.c_str());
+        mavi_destroy(s);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(s, MAVI_ERR_CUDA, "stream creation failed"));
+
+    Ctx& C = s->C;
+    const int64_t M = s->M, N = s->Nslots;
+#define ALLOC(ptr, n) \
+    if (dalloc(s, &(ptr), (n)) != cudaSuccess) return bail(fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for %s", #ptr))
+    ALLOC(C.pos_cur, M); ALLOC(C.pos_mid, M); ALLOC(C.pos_out, M);
+    if (s->has_vel) { ALLOC(C.vel_cur, M); ALLOC(C.vel_out, M); }
+    if (s->has_pol) { ALLOC(C.pol_cur, M); ALLOC(C.pol_out, M); }
+    if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.off_cur, M); ALLOC(C.off_mid, M); ALLOC(C.ff, M); }
+    else { ALLOC(C.fd, M); }
+    if (s->step_kind == MAVI_STEP_NEWTON) {
+        if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.fold_f, M); } else { ALLOC(C.fold_d, M); }
+    }
+    ALLOC(C.uid_cur, M); ALLOC(C.uid_out, M); ALLOC(C.rep_cur, M); ALLOC(C.rep_out, M);
+    ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.rank, M); ALLOC(C.src_of, M);
+    ALLOC(C.slot_of, N);
+    ALLOC(C.count, s->Ctot); ALLOC(C.start, s->Ctot + 1);
+    ALLOC(s->tile_sum, s->ntiles);
+    int32_t* ring_types_d = nullptr;
+    if (s->is_rings) { ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings); }
+    DevRep* reps_d = nullptr;
+    MaviSpace* spaces_d = nullptr;
+    MaviRingsCfg* rcfg_d = nullptr;
+    ALLOC(reps_d, s->R); ALLOC(spaces_d, (int64_t)s->R * MAVI_MAX_SPACES); ALLOC(rcfg_d, s->R);
+    ALLOC(C.err, 1); ALLOC(C.d_step, 1);
+    ALLOC(s->pos_user, N); ALLOC(s->f_user, N);
+    if (s->has_vel) { ALLOC(s->vel_user, N); }
+    if (s->has_pol) { ALLOC(s->pol_user, N); }
+    ALLOC(s->ke_t, M); ALLOC(s->pe_t, M); ALLOC(s->ke_r, s->R); ALLOC(s->pe_r, s->R);
+    ALLOC(s->d_pairs, 1);
+    if (s->noise_count > 0) { ALLOC(s->noise_cur, s->noise_count); }
+#undef ALLOC
+    C.ring_types = ring_types_d;
+    C.reps = reps_d;
+    C.spaces = spaces_d;
+    C.rcfg = rcfg_d;
+    C.M = M;
+    C.Ctot = s->Ctot;
+    C.noise = s->noise_cur;
+    C.noise_mode = opt->noise_mode;
+    C.num_reps = s->R;
+    C.seed = opt->seed;
+
+    // descriptors
+    std::vector<MaviSpace> spaces_h((size_t)s->R * MAVI_MAX_SPACES);
+    std::vector<MaviRingsCfg> rcfg_h(s->R);
+    for (int r = 0; r < s->R; r++) {
+        for (int k = 0; k < MAVI_MAX_SPACES; k++) spaces_h[(size_t)r * MAVI_MAX_SPACES + k] = replicas[r].spaces[k];
+        rcfg_h[r] = replicas[r].rings;
+    }
+    // identity user order over active slots
+    std::vector<int32_t> uid_h(M), rep_h(M);
+    std::vector<int32_t> types_all;
+    {
+        int64_t k = 0;
+        const int32_t* tc = ring_types;
+        for (int r = 0; r < s->R; r++) {
+            const MaviReplicaParams& p = replicas[r];
+            const DevRep& R = s->reps_h[r];
+            if (s->is_rings) {
+                for (int q = 0; q < p.rings.num_rings; q++) {
+                    int t = tc ? tc[q] : 1;
+                    types_all.push_back(t);
+                    for (int i = 0; i < p.rings.num_particles[t - 1]; i++) {
+                        uid_h[k] = (int32_t)(R.slot0 + (int64_t)q * p.rings.nmax + i);
+                        rep_h[k] = r;
+                        k++;
+                    }
+                }
+                if (tc) tc += p.rings.num_rings;
+            } else {
+                for (int64_t i = 0; i < p.num_particles; i++) {
+                    uid_h[k] = (int32_t)(R.slot0 + i);
+                    rep_h[k] = r;
+                    k++;
+                }
+            }
+        }
+    }
+    CUDA_TRY(s, cudaMemcpyAsync(reps_d, s->reps_h.data(), sizeof(DevRep) * s->R, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(spaces_d, spaces_h.data(), sizeof(MaviSpace) * spaces_h.size(), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(rcfg_d, rcfg_h.data(), sizeof(MaviRingsCfg) * s->R, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(C.uid_out, uid_h.data(), sizeof(int32_t) * M, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(C.rep_out, rep_h.data(), sizeof(int32_t) * M, cudaMemcpyHostToDevice, s->stream));
+    if (s->is_rings) {
+        CUDA_TRY(s, cudaMemcpyAsync(ring_types_d, types_all.data(), sizeof(int32_t) * s->total_rings,
+                                    cudaMemcpyHostToDevice, s->stream));
+    }
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++)
+        for (int u = 0; u < 4; u++) {
+            cudaEventCreate(&s->ev.a[k][u]);
+            cudaEventCreate(&s->ev.b[k][u]);
+        }
+    cudaEventCreate(&s->ev.step_a);
+    cudaEventCreate(&s->ev.step_b);
+    int rc = mavi_upload_state(s, pos, vel, pol);
+    if (rc) return bail(rc);
+    // System() runs the first update_chunks! (src/systems.jl:103-105)
+    launch_rebin(s, false);
+    rc = check_device_error(s);
+    if (rc) return bail(rc);
+    *out = s;
+    return MAVI_OK;
+}
+
+int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const double* pol) {
+    if (!s || !pos) return MAVI_ERR_INVALID_ARG;
+    CUDA_TRY(s, cudaMemcpyAsync(s->pos_user, pos, sizeof(double2) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
+    if (s->has_vel && vel)
+        CUDA_TRY(s, cudaMemcpyAsync(s->vel_user, vel, sizeof(double2) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
+    if (s->has_pol && pol)
+        CUDA_TRY(s, cudaMemcpyAsync(s->pol_user, pol, sizeof(double) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
+    if (s->is_rings && pol)
+        CUDA_TRY(s, cudaMemcpyAsync(s->C.ring_pol, pol, sizeof(double) * s->total_rings, cudaMemcpyHostToDevice, s->stream));
+    k_gather_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, (s->has_vel && vel) ? s->vel_user : nullptr,
+                                                           (s->has_pol && pol) ? s->pol_user : nullptr);
+    s->counts_valid = false;
+    launch_count(s);
+    s->counts_valid = true;
+    CUDA_TRY(s, cudaGetLastError());
+    return check_device_error(s);
+}
+
+int mavi_download_state(MaviSystem* s, double* pos, double* vel, double* pol) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    k_scatter_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, s->has_vel ? s->vel_user : nullptr,
+                                                            s->has_pol ? s->pol_user : nullptr);
+    CUDA_TRY(s, cudaGetLastError());
+    if (pos) CUDA_TRY(s, cudaMemcpyAsync(pos, s->pos_user, sizeof(double2) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
+    if (vel && s->has_vel)
+        CUDA_TRY(s, cudaMemcpyAsync(vel, s->vel_user, sizeof(double2) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
+    if (pol && s->has_pol)
+        CUDA_TRY(s, cudaMemcpyAsync(pol, s->pol_user, sizeof(double) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
+    if (pol && s->is_rings)
+        CUDA_TRY(s, cudaMemcpyAsync(pol, s->C.ring_pol, sizeof(double) * s->total_rings, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    return MAVI_OK;
+}
+
+int64_t mavi_noise_count(MaviSystem* s) { return s ? s->noise_count : -1; }
+
+int mavi_set_noise(MaviSystem* s, const double* noise, int64_t count) {
+    if (!s || !noise || s->noise_count == 0 || count <= 0 || count % s->noise_count != 0)
+        return fail(s, MAVI_ERR_INVALID_ARG, "noise count must be a positive multiple of %lld",
+                    (long long)(s ? s->noise_count : 0));
+    if (count > s->noise_queue_cap) {
+        if (s->noise_queue) {
+            cudaStreamSynchronize(s->stream);
+            cudaFree(s->noise_queue);
+            s->allocs.erase(std::remove(s->allocs.begin(), s->allocs.end(), (void*)s->noise_queue), s->allocs.end());
+        }
+        if (dalloc(s, &s->noise_queue, count) != cudaSuccess) return fail(s, MAVI_ERR_CUDA, "noise buffer allocation failed");
+        s->noise_queue_cap = count;
+    }
+    CUDA_TRY(s, cudaMemcpyAsync(s->noise_queue, noise, sizeof(double) * count, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    s->noise_queue_len = count / s->noise_count;
+    s->noise_queue_pos = 0;
+    return MAVI_OK;
+}
+
+int mavi_set_seed(MaviSystem* s, uint64_t seed) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    s->opt.seed = seed;
+    s->C.seed = seed;
+    drop_graph(s);
+    return MAVI_OK;
+}
+
+int mavi_step(MaviSystem* s, int64_t nsteps) {
+    if (!s || nsteps < 0) return MAVI_ERR_INVALID_ARG;
+    bool injected = s->noise_count > 0 && s->opt.noise_mode == MAVI_NOISE_INJECTED;
+    if (injected && s->noise_queue_len - s->noise_queue_pos < nsteps)
+        return fail(s, MAVI_ERR_NOISE_MISSING, "%lld steps need noise; %lld steps of noise supplied",
+                    (long long)nsteps, (long long)(s->noise_queue_len - s->noise_queue_pos));
+    if (nsteps == 0) return MAVI_OK;
+    if (!s->counts_valid) {     // after calc_forces/energies/update_chunks
+        launch_count(s);
+        for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
+        s->counts_valid = true;
+    }
+    if (s->opt.use_graph) {
+        int rc = ensure_graph(s);
+        if (rc) return rc;
+    }
+    for (int64_t k = 0; k < nsteps; k++) {
+        if (injected) {
+            CUDA_TRY(s, cudaMemcpyAsync(s->noise_cur, s->noise_queue + s->noise_queue_pos * s->noise_count,
+                                        sizeof(double) * s->noise_count, cudaMemcpyDeviceToDevice, s->stream));
+            s->noise_queue_pos++;
+        }
+        if (s->graph_exec) {
+            CUDA_TRY(s, cudaGraphLaunch(s->graph_exec, s->stream));
+            s->counts_valid = true;
+            collect_profile(s, s->graph_ev_used);
+            collect_step_time(s, s->graph_step_used);
+        } else {
+            launch_step(s);
+            CUDA_TRY(s, cudaGetLastError());
+            collect_profile(s, s->ev.used);
+            collect_step_time(s, s->ev.step_used);
+            for (int q = 0; q < MAVI_NUM_KERNEL_KINDS; q++) s->ev.used[q] = 0;
+            s->ev.step_used = 0;
+        }
+        for (int r = 0; r < s->R; r++) {
+            s->num_steps[r] += 1;
+            s->time[r] += s->params[r].dt;
+        }
+        if (s->profiling) s->prof.steps += 1;
+    }
+    CUDA_TRY(s, cudaGetLastError());
+    return check_device_error(s);
+}
+
+int mavi_update_chunks(MaviSystem* s) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    s->counts_valid = false;
+    launch_rebin(s, false);
+    CUDA_TRY(s, cudaGetLastError());
+    return check_device_error(s);
+}
+
+int mavi_chunk_geometry(MaviSystem* s, int32_t replica, int32_t* rows, int32_t* cols, int32_t* cap) {
+    if (!s || replica < 0 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    const DevRep& R = s->reps_h[replica];
+    if (!R.has_chunks) return fail(s, MAVI_ERR_INVALID_ARG, "replica %d has no chunks", replica);
+    if (rows) *rows = R.rows;
+    if (cols) *cols = R.cols;
+    if (cap) *cap = R.cap;
+    return MAVI_OK;
+}
+
+int mavi_get_chunks(MaviSystem* s, int32_t replica, int32_t* num_in_chunk, int32_t* chunk_particles) {
+    if (!s || replica < 0 || replica >= s->R || !num_in_chunk || !chunk_particles) return MAVI_ERR_INVALID_ARG;
+    const DevRep& R = s->reps_h[replica];
+    if (!R.has_chunks) return fail(s, MAVI_ERR_INVALID_ARG, "replica %d has no chunks", replica);
+    int rc = mavi_update_chunks(s);
+    if (rc) return rc;
+    int64_t nch = (int64_t)R.rows * R.cols;
+    std::vector<int32_t> start(nch + 1), uid(R.na);
+    CUDA_TRY(s, cudaMemcpy(start.data(), s->C.start + R.c0, sizeof(int32_t) * (nch + 1), cudaMemcpyDeviceToHost));
+    CUDA_TRY(s, cudaMemcpy(uid.data(), s->C.uid_cur + R.a0, sizeof(int32_t) * R.na, cudaMemcpyDeviceToHost));
+    int32_t mx = 0;
+    for (int64_t c = 0; c < nch; c++) {
+        int32_t b = start[c] - (int32_t)R.a0, e = start[c + 1] - (int32_t)R.a0;
+        num_in_chunk[c] = e - b;
+        mx = std::max(mx, e - b);
+        for (int32_t k = 0; k < R.cap; k++)
+            chunk_particles[c * R.cap + k] = (k < e - b) ? uid[b + k] - (int32_t)R.slot0 : -1;
+    }
+    s->max_chunk_count = mx;
+    return MAVI_OK;
+}
+
+int mavi_calc_forces(MaviSystem* s, int32_t include_walls, double* forces_out) {
+    if (!s || !forces_out) return MAVI_ERR_INVALID_ARG;
+    s->counts_valid = false;
+    launch_rebin(s, false);
+    if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, include_walls);
+    else forces_only_mixed(s, include_walls);
+    if (s->is_rings) {
+        if (s->prec == MAVI_PREC_FP64) rings_terms_fp64(s, 0);
+        else rings_terms_mixed(s, 0);
+    }
+    CUDA_TRY(s, cudaMemsetAsync(s->f_user, 0, sizeof(double2) * s->Nslots, s->stream));
+    if (s->prec == MAVI_PREC_FP64) forces_to_user_fp64(s);
+    else forces_to_user_mixed(s);
+    CUDA_TRY(s, cudaGetLastError());
+    CUDA_TRY(s, cudaMemcpyAsync(forces_out, s->f_user, sizeof(double2) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
+    return check_device_error(s);
+}
+
+int mavi_energies(MaviSystem* s, int32_t pe_mode, double* ke, double* pe) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    s->counts_valid = false;
+    launch_rebin(s, false);
+    k_energy_terms<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->dyn, pe_mode == MAVI_PE_ALL_PAIRS, s->ke_t, s->pe_t,
+                                                            s->has_vel ? 1 : 0);
+    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->ke_t, s->ke_r, 0.5);
+    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->pe_t, s->pe_r, 1.0);
+    CUDA_TRY(s, cudaGetLastError());
+    if (ke) CUDA_TRY(s, cudaMemcpyAsync(ke, s->ke_r, sizeof(double) * s->R, cudaMemcpyDeviceToHost, s->stream));
+    if (pe) CUDA_TRY(s, cudaMemcpyAsync(pe, s->pe_r, sizeof(double) * s->R, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    bool pe_defined = s->dyn == MAVI_DYN_LEN_JONES || s->dyn == MAVI_DYN_HARM_TRUNC || s->dyn == MAVI_DYN_RUN_TUMBLE;
+    if (pe && !pe_defined)
+        for (int r = 0; r < s->R; r++) pe[r] = NAN;
+    return check_device_error(s);
+}
+
+int mavi_get_time(MaviSystem* s, int64_t* num_steps, double* time) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    if (num_steps) *num_steps = s->num_steps[0];
+    if (time) *time = s->time[0];
+    return MAVI_OK;
+}
+
+int mavi_get_stats(MaviSystem* s, MaviStats* st) {
+    if (!s || !st) return MAVI_ERR_INVALID_ARG;
+    int rc = mavi_update_chunks(s);
+    if (rc) return rc;
+    CUDA_TRY(s, cudaMemsetAsync(s->d_pairs, 0, sizeof(unsigned long long), s->stream));
+    k_pair_count<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->d_pairs);
+    unsigned long long pairs = 0;
+    CUDA_TRY(s, cudaMemcpyAsync(&pairs, s->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost, s->stream));
+    std::vector<int32_t> start(s->Ctot + 1);
+    CUDA_TRY(s, cudaMemcpyAsync(start.data(), s->C.start, sizeof(int32_t) * (s->Ctot + 1), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    int32_t mx = 0;
+    for (int64_t c = 0; c < s->Ctot; c++) mx = std::max(mx, start[c + 1] - start[c]);
+    st->candidate_pairs = (int64_t)(pairs / 2);
+    st->total_particles = s->M;
+    st->total_chunks = s->Ctot;
+    st->max_chunk_count = mx;
+    return MAVI_OK;
+}
+
+int mavi_profile_enable(MaviSystem* s, int32_t on) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    s->profiling = on != 0;
+    s->prof = MaviProfile{};
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
+    return MAVI_OK;
+}
+
+int mavi_profile_read(MaviSystem* s, MaviProfile* p) {
+    if (!s || !p) return MAVI_ERR_INVALID_ARG;
+    *p = s->prof;
+    return MAVI_OK;
+}
+
+int mavi_last_error(MaviSystem* s, char* buf, int32_t len) {
+    if (!s || !buf || len <= 0) return MAVI_ERR_INVALID_ARG;
+    snprintf(buf, (size_t)len, "%s", s->last_error.c_str());
+    return MAVI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,221 @@
+// mavi_device.cuh — device-side definitions shared by the kernels of
+// libmavi_cuda.so: the per-replica descriptor, Julia-exact chunk arithmetic,
+// the pair force laws, wall handling and the counter-based RNG.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/mavi_cuda.h"
+
+namespace mavi {
+
+constexpr int kPrecFP64 = MAVI_PREC_FP64;
+constexpr int kPrecMixed = MAVI_PREC_MIXED;
+
+// Device error word: the first error code wins; `err_info` keeps the sorted
+// slot that raised it. Kernels record and continue with clamped indices so
+// that every access stays in bounds; the host reads the word after a step.
+struct DevError {
+    int32_t code;
+    int32_t slot;
+    int64_t aux;
+};
+
+__device__ __forceinline__ void raise_error(DevError* e, int32_t code, int64_t slot, int64_t aux) {
+    if (atomicCAS(&e->code, 0, code) == 0) {
+        e->slot = (int32_t)slot;
+        e->aux = aux;
+    }
+}
+
+// Per-replica descriptor, built on the host from MaviReplicaParams.
+struct DevRep {
+    int64_t a0, na;        // range of this replica's particles in sorted order
+    int64_t slot0, nslots; // range of this replica's user slots
+    int64_t c0;            // first global chunk of this replica
+    int64_t ring0;         // first global ring of this replica
+    int64_t noise0;        // first noise number of this replica in a step
+    int32_t rows, cols, cap, periodic; // chunk grid; periodic stencil
+    int32_t has_chunks;
+    int32_t num_rings, nmax;
+    int32_t min_image;     // first space is PeriodicWalls on a RectangleCfg
+    int32_t num_spaces;
+    int32_t has_wall_forces;
+    int32_t has_walls;     // any space that acts in walls!
+    int32_t _pad;
+    double chunk_l, chunk_h, bb_blx, bb_bly, bb_h, bb_len;
+    double box_x, box_y;
+    float chunk_lf, chunk_hf, box_xf, box_yf;
+    float half_box_xf, half_box_yf;
+    double half_box_x, half_box_y;
+    double radius;         // particle_radius (walls)
+    double dt;
+    double pd[8];          // pair-law parameters (double)
+    float pf[8];           // same in float
+    double mobility, vo, relax_time, rot_diff, tumble_rate;
+};
+
+// ---------------------------------------------------------------------------
+// Julia-exact chunk index (src/chunks.jl:120-147). Julia's float div(x, y)
+// rounds-to-nearest the exact quotient (x - rem(x, y)) / y, rem == fmod.
+// Explicit _rn intrinsics keep the compiler from contracting anything.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double julia_div(double x, double y) {
+    double r = fmod(x, y);
+    return rint(__ddiv_rn(__dsub_rn(x, r), y));
+}
+
+// Returns the 0-based (row, col) before bounds checks, following
+// `row = trunc(Int, div(-y + bl_y + H, chunk_h)) + 1` and the one-chunk clamp
+// of index n+1. `ok` is false for a non-finite quotient.
+__device__ __forceinline__ void chunk_row_col(const DevRep& R, double x, double y,
+                                              int64_t& row, int64_t& col, bool& finite) {
+    double qr = julia_div(__dadd_rn(__dadd_rn(-y, R.bb_bly), R.bb_h), R.chunk_h);
+    double qc = julia_div(__dsub_rn(x, R.bb_blx), R.chunk_l);
+    finite = isfinite(qr) && isfinite(qc) && fabs(qr) < 4e18 && fabs(qc) < 4e18;
+    int64_t r = finite ? (int64_t)qr + 1 : 1;
+    int64_t c = finite ? (int64_t)qc + 1 : 1;
+    r -= (r == (int64_t)R.rows + 1) ? 1 : 0;
+    c -= (c == (int64_t)R.cols + 1) ? 1 : 0;
+    row = r - 1;
+    col = c - 1;
+}
+
+// Centre of chunk (row, col): the FP32 offsets of the mixed form are taken
+// relative to it, so |offset| stays within half a chunk.
+__device__ __forceinline__ double chunk_cx(const DevRep& R, int64_t col) {
+    return R.bb_blx + ((double)col + 0.5) * R.chunk_l;
+}
+__device__ __forceinline__ double chunk_cy(const DevRep& R, int64_t row) {
+    return R.bb_bly + R.bb_h - ((double)row + 0.5) * R.chunk_h;
+}
+
+// ---------------------------------------------------------------------------
+// Minimum image (src/integration.jl:43-48):
+//   dr - (abs.(dr) .> size/2) .* copysign.(size, dr)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double min_image1(double d, double box, double half) {
+    return fabs(d) > half ? d - copysign(box, d) : d;
+}
+__device__ __forceinline__ float min_image1f(float d, float box, float half) {
+    return fabsf(d) > half ? d - copysignf(box, d) : d;
+}
+
+// ---------------------------------------------------------------------------
+// Pair laws: force on i from j as a scalar s with f = s * dr.
+// ---------------------------------------------------------------------------
+// Parameter packing (DevRep::pd / pf), set by the host:
+//  HarmTrunc: {k_rep, k_atr, 1/dist_eq, dist_eq^2, dist_max^2}
+//     fmod/dist = -k (dist/dist_eq - 1)/dist = k (1/dist - 1/dist_eq)
+//  LenJones:  {48 eps sigma^12, 24 eps sigma^6}
+//     fmod/dist = 4 eps (12 sigma^12/d^14 - 6 sigma^6/d^8) = ir8 (A ir6 - B)
+//  Szabo:     {k_rep/(r_max-r_eq), k_adh/r_eq, r_eq, r_max, r_max^2}
+//     f = -f_mod (dist - r_eq) dr
+//  RunTumble: {48 eps sigma^12, 24 eps sigma^6, cutoff^2}
+
+template <typename T> __device__ __forceinline__ T rcp_(T x);
+template <> __device__ __forceinline__ double rcp_<double>(double x) { return 1.0 / x; }
+template <> __device__ __forceinline__ float rcp_<float>(float x) { return __frcp_rn(x); }
+template <typename T> __device__ __forceinline__ T rsqrt_(T x);
+template <> __device__ __forceinline__ double rsqrt_<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return rsqrtf(x); }
+template <typename T> __device__ __forceinline__ T sqrt_(T x);
+template <> __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrtf(x); }
+
+template <int DYN, typename T>
+__device__ __forceinline__ T pair_scalar(const T* prm, T d2) {
+    if constexpr (DYN == MAVI_DYN_LEN_JONES) {
+        T ir2 = rcp_<T>(d2);
+        T ir6 = ir2 * ir2 * ir2;
+        return ir6 * ir2 * (prm[0] * ir6 - prm[1]);
+    } else if constexpr (DYN == MAVI_DYN_HARM_TRUNC) {
+        if (d2 > prm[4]) return T(0);
+        T k = d2 < prm[3] ? prm[0] : prm[1];
+        return k * (rsqrt_<T>(d2) - prm[2]);
+    } else if constexpr (DYN == MAVI_DYN_SZABO) {
+        if (d2 > prm[4]) return T(0);
+        T dist = sqrt_<T>(d2);
+        T f_mod = dist > prm[2] ? prm[1] : prm[0];
+        return -f_mod * (dist - prm[2]);
+    } else if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
+        if (d2 > prm[2]) return T(0);
+        T ir2 = rcp_<T>(d2);
+        T ir6 = ir2 * ir2 * ir2;
+        return ir6 * ir2 * (prm[0] * ir6 - prm[1]);
+    } else {
+        return T(0);
+    }
+}
+
+// Pair energy consistent with the force law:
+// LenJones 4 eps[(s/d)^12-(s/d)^6] (src/quantities.jl:46-66); HarmTrunc
+// k/(2 dist_eq) (d - dist_eq)^2 below dist_max; RunTumble unshifted WCA.
+__device__ __forceinline__ double pair_energy(int dyn, const double* e, double d2) {
+    if (dyn == MAVI_DYN_LEN_JONES) {
+        double ir2 = 1.0 / d2;
+        double ir6 = ir2 * ir2 * ir2;
+        return e[0] * (e[1] * ir6 * ir6 - e[2] * ir6);
+    } else if (dyn == MAVI_DYN_HARM_TRUNC) {
+        if (d2 > e[3] * e[3]) return 0.0;
+        double d = sqrt(d2);
+        double k = d < e[2] ? e[0] : e[1];
+        double x = d - e[2];
+        return k / (2 * e[2]) * x * x;
+    } else if (dyn == MAVI_DYN_RUN_TUMBLE) {
+        if (d2 > e[3]) return 0.0;
+        double ir2 = 1.0 / d2;
+        double ir6 = ir2 * ir2 * ir2;
+        return e[0] * (e[1] * ir6 * ir6 - e[2] * ir6);
+    }
+    return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Counter-based RNG: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel
+// random numbers: as easy as 1, 2, 3", SC 2011), counter = (a, b, c, d),
+// key = 64-bit seed. Uniforms in (0, 1], normals by Box-Muller.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32_10(U4 ctr, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        U4 n;
+        n.x = hi1 ^ ctr.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ ctr.w ^ k1;
+        n.w = lo0;
+        ctr = n;
+        k0 += W0;
+        k1 += W1;
+    }
+    return ctr;
+}
+
+__device__ __forceinline__ double u32_to_unit(uint32_t a, uint32_t b) {
+    // 53-bit uniform in (0, 1]
+    uint64_t m = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);
+    m &= ((1ull << 53) - 1);
+    return ((double)m + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+struct Rand2 { double a, b; };
+
+// Two uniforms and a standard normal for (stream id, step).
+__device__ __forceinline__ Rand2 philox_uniform2(uint64_t seed, uint64_t id, uint64_t step) {
+    U4 c{(uint32_t)id, (uint32_t)(id >> 32), (uint32_t)step, (uint32_t)(step >> 32)};
+    U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    return Rand2{u32_to_unit(r.x, r.y), u32_to_unit(r.z, r.w)};
+}
+
+__device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t id, uint64_t step) {
+    Rand2 u = philox_uniform2(seed, id, step);
+    return sqrt(-2.0 * log(u.a)) * cospi(2.0 * u.b);
+}
+
+}  // namespace mavi

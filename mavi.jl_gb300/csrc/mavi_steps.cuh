@@ -1,0 +1,119 @@
+// mavi_steps.cuh — per-precision launch sequences. Included once by
+// mavi_steps_fp64.cu (PREC = FP64) and once by mavi_steps_mixed.cu
+// (PREC = mixed) so the two sets of kernel instantiations compile in parallel.
+#pragma once
+
+#include "mavi_system.cuh"
+
+namespace mavi {
+namespace steps {
+
+template <int PREC>
+void sort_permute(MaviSystem* s) {
+    unsigned g = nblocks(s->Ctot);
+    if (s->has_vel) k_sort_permute<PREC, true, false><<<g, kBlock, 0, s->stream>>>(s->C);
+    else if (s->has_pol) k_sort_permute<PREC, false, true><<<g, kBlock, 0, s->stream>>>(s->C);
+    else k_sort_permute<PREC, false, false><<<g, kBlock, 0, s->stream>>>(s->C);
+}
+
+template <int PREC, int DYN, int PASS>
+void pass(MaviSystem* s, int with_walls) {
+    unsigned g = nblocks(s->M);
+    if (s->has_vel) k_pass<PREC, DYN, PASS, true, false><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
+    else if (s->has_pol) k_pass<PREC, DYN, PASS, false, true><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
+    else k_pass<PREC, DYN, PASS, false, false><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
+}
+
+template <int PREC>
+void rings_terms(MaviSystem* s, int do_update) {
+    unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
+    k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update);
+}
+
+// The passes of one step after the chunk rebuild.
+template <int PREC, int DYN>
+void step_body(MaviSystem* s) {
+    switch (s->step_kind) {
+    case MAVI_STEP_NEWTON:
+        if constexpr (DYN != MAVI_DYN_RINGS) {
+            record_begin(s, MAVI_KERNEL_FORCE);
+            pass<PREC, DYN, kPassVerlet1>(s, 1);   // F(t) with wall forces, x(t+dt)
+            pass<PREC, DYN, kPassVerlet2>(s, 0);   // F(t+dt) on stale chunks, v, walls!
+            record_end(s, MAVI_KERNEL_FORCE);
+        }
+        break;
+    case MAVI_STEP_OVERDAMPED:
+        if constexpr (DYN != MAVI_DYN_RINGS) {
+            record_begin(s, MAVI_KERNEL_FORCE);
+            pass<PREC, DYN, kPassOverdamped>(s, 1);
+            record_end(s, MAVI_KERNEL_FORCE);
+        }
+        break;
+    case MAVI_STEP_SZABO:
+        if constexpr (DYN == MAVI_DYN_SZABO) {
+            record_begin(s, MAVI_KERNEL_FORCE);
+            pass<PREC, DYN, kPassSzabo>(s, 1);
+            record_end(s, MAVI_KERNEL_FORCE);
+        }
+        break;
+    case MAVI_STEP_RTP:
+        if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
+            record_begin(s, MAVI_KERNEL_FORCE);
+            pass<PREC, DYN, kPassRTP>(s, 1);
+            record_end(s, MAVI_KERNEL_FORCE);
+        }
+        break;
+    case MAVI_STEP_RINGS:
+        if constexpr (DYN == MAVI_DYN_RINGS) {
+            record_begin(s, MAVI_KERNEL_FORCE);
+            pass<PREC, DYN, kPassForce>(s, 0);
+            record_end(s, MAVI_KERNEL_FORCE);
+            record_begin(s, MAVI_KERNEL_UPDATE);
+            rings_terms<PREC>(s, 1);
+            k_count<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+            record_end(s, MAVI_KERNEL_UPDATE);
+        }
+        break;
+    }
+}
+
+template <int PREC>
+void step_body_dispatch(MaviSystem* s) {
+    switch (s->dyn) {
+    case MAVI_DYN_HARM_TRUNC: step_body<PREC, MAVI_DYN_HARM_TRUNC>(s); break;
+    case MAVI_DYN_LEN_JONES: step_body<PREC, MAVI_DYN_LEN_JONES>(s); break;
+    case MAVI_DYN_SZABO: step_body<PREC, MAVI_DYN_SZABO>(s); break;
+    case MAVI_DYN_RUN_TUMBLE: step_body<PREC, MAVI_DYN_RUN_TUMBLE>(s); break;
+    case MAVI_DYN_RINGS: step_body<PREC, MAVI_DYN_RINGS>(s); break;
+    }
+}
+
+// calc_forces! (+ calc_walls_forces!) on the current chunks; rings add their
+// bonded terms in rings_terms(do_update = 0).
+template <int PREC>
+void forces_only(MaviSystem* s, int with_walls) {
+    switch (s->dyn) {
+    case MAVI_DYN_HARM_TRUNC: pass<PREC, MAVI_DYN_HARM_TRUNC, kPassForce>(s, with_walls); break;
+    case MAVI_DYN_LEN_JONES: pass<PREC, MAVI_DYN_LEN_JONES, kPassForce>(s, with_walls); break;
+    case MAVI_DYN_SZABO: pass<PREC, MAVI_DYN_SZABO, kPassForce>(s, with_walls); break;
+    case MAVI_DYN_RUN_TUMBLE: pass<PREC, MAVI_DYN_RUN_TUMBLE, kPassForce>(s, with_walls); break;
+    case MAVI_DYN_RINGS: pass<PREC, MAVI_DYN_RINGS, kPassForce>(s, 0); break;
+    }
+}
+
+template <int PREC>
+void forces_to_user(MaviSystem* s) {
+    k_forces_to_user<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->f_user);
+}
+
+}  // namespace steps
+}  // namespace mavi
+
+#define MAVI_DEFINE_STEPS(SUFFIX, PREC)                                                      \
+    namespace mavi {                                                                         \
+    void sort_permute_##SUFFIX(MaviSystem* s) { steps::sort_permute<PREC>(s); }              \
+    void step_body_##SUFFIX(MaviSystem* s) { steps::step_body_dispatch<PREC>(s); }           \
+    void forces_only_##SUFFIX(MaviSystem* s, int w) { steps::forces_only<PREC>(s, w); }      \
+    void rings_terms_##SUFFIX(MaviSystem* s, int u) { steps::rings_terms<PREC>(s, u); }      \
+    void forces_to_user_##SUFFIX(MaviSystem* s) { steps::forces_to_user<PREC>(s); }          \
+    }

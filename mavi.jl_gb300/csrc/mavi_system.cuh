@@ -1,0 +1,155 @@
+// mavi_system.cuh — the handle (MaviSystem) and the launch sequences shared by
+// the translation units of libmavi_cuda.so.
+#pragma once
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "mavi_kernels.cuh"
+
+namespace mavi {
+
+constexpr int kBlock = 256;
+
+struct ProfEvents {
+    cudaEvent_t a[MAVI_NUM_KERNEL_KINDS][4];
+    cudaEvent_t b[MAVI_NUM_KERNEL_KINDS][4];
+    int used[MAVI_NUM_KERNEL_KINDS];
+    cudaEvent_t step_a, step_b;
+    int step_used;
+};
+
+}  // namespace mavi
+
+// The opaque handle of the C ABI (include/mavi_cuda.h).
+struct MaviSystem {
+    using DevRep = mavi::DevRep;
+    using Ctx = mavi::Ctx;
+    using ProfEvents = mavi::ProfEvents;
+    MaviOptions opt{};
+    int32_t R = 0;
+    std::vector<MaviReplicaParams> params;
+    std::vector<DevRep> reps_h;
+    std::vector<int64_t> rep_active;   // active particles per replica
+    int32_t dyn = 0, step_kind = 0, state_kind = 0, prec = 0;
+    bool has_vel = false, has_pol = false, is_rings = false;
+    int64_t M = 0, Nslots = 0, Ctot = 0, total_rings = 0, noise_count = 0, ntiles = 0;
+    std::vector<int64_t> num_steps;
+    std::vector<double> time;
+    cudaStream_t stream = nullptr;
+    Ctx C{};
+    std::vector<void*> allocs;
+    double2 *pos_user = nullptr, *vel_user = nullptr, *f_user = nullptr;
+    double* pol_user = nullptr;
+    int32_t* tile_sum = nullptr;
+    double *ke_t = nullptr, *pe_t = nullptr, *ke_r = nullptr, *pe_r = nullptr;
+    unsigned long long* d_pairs = nullptr;
+    double* noise_cur = nullptr;
+    double* noise_queue = nullptr;
+    int64_t noise_queue_cap = 0, noise_queue_len = 0, noise_queue_pos = 0;
+    bool counts_valid = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool profiling = false;
+    bool graph_profiled = false;
+    int graph_ev_used[MAVI_NUM_KERNEL_KINDS] = {0};
+    int graph_step_used = 0;
+    ProfEvents ev{};
+    MaviProfile prof{};
+    int32_t max_chunk_count = 0;
+    int64_t last_pairs = -1;
+    std::string last_error;
+};
+
+namespace mavi {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+inline int fail(MaviSystem* s, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (s) s->last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(sys, expr)                                                                  \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return fail(sys, MAVI_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(_e)); \
+    } while (0)
+
+template <typename T>
+inline cudaError_t dalloc(MaviSystem* s, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e == cudaSuccess) {
+        s->allocs.push_back((void*)*p);
+        cudaMemsetAsync(*p, 0, sizeof(T) * count, s->stream);
+    }
+    return e;
+}
+
+inline unsigned nblocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
+
+inline void record_begin(MaviSystem* s, int kind) {
+    if (!s->profiling) return;
+    int u = s->ev.used[kind];
+    if (u < 4) cudaEventRecord(s->ev.a[kind][u], s->stream);
+}
+inline void record_end(MaviSystem* s, int kind) {
+    if (!s->profiling) return;
+    int u = s->ev.used[kind];
+    if (u < 4) {
+        cudaEventRecord(s->ev.b[kind][u], s->stream);
+        s->ev.used[kind] = u + 1;
+    }
+}
+// Adds the device time between each begin/end event pair of the last
+// launch sequence (eager or graph replay) to the profile.
+inline void collect_profile(MaviSystem* s, const int* used) {
+    if (!s->profiling) return;
+    cudaStreamSynchronize(s->stream);
+    for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) {
+        for (int u = 0; u < used[k]; u++) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, s->ev.a[k][u], s->ev.b[k][u]) == cudaSuccess) {
+                s->prof.ms[k] += ms;
+                s->prof.launches[k] += 1;
+            }
+        }
+        s->ev.used[k] = 0;
+    }
+}
+
+// Whole-step device time: an event before the first and after the last launch.
+inline void collect_step_time(MaviSystem* s, int used) {
+    if (!s->profiling || !used) return;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, s->ev.step_a, s->ev.step_b) == cudaSuccess) {
+        s->prof.step_ms += ms;
+        s->prof.last_step_ms = ms;
+    }
+}
+
+
+// Per-precision launch sequences (mavi_steps_fp64.cu / mavi_steps_mixed.cu).
+void sort_permute_fp64(MaviSystem* s);
+void sort_permute_mixed(MaviSystem* s);
+void step_body_fp64(MaviSystem* s);
+void step_body_mixed(MaviSystem* s);
+void forces_only_fp64(MaviSystem* s, int with_walls);
+void forces_only_mixed(MaviSystem* s, int with_walls);
+void rings_terms_fp64(MaviSystem* s, int do_update);
+void rings_terms_mixed(MaviSystem* s, int do_update);
+void forces_to_user_fp64(MaviSystem* s);
+void forces_to_user_mixed(MaviSystem* s);
+
+}  // namespace mavi

@@ -1,0 +1,238 @@
+"""The rings model mirroring Mavi.Rings (src/rings/*.jl): ring polymers of
+particles with pair excluded volume, springs, an area term, self-propulsion
+along a per-ring polarisation, plus an optional bending term (``k_bend``;
+zero reproduces the reference, which has none)."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import Any, Sequence
+
+import numpy as np
+
+from . import abi
+from .configs import HarmTruncCfg, IntCfg, ChunksCfg, CUDADevice, chunk_capacity
+from .system import System, TimeInfo
+
+
+# ---------------------------------------------------------------------------
+# configs (src/rings/configs.jl)
+# ---------------------------------------------------------------------------
+@dataclass
+class InteractionMatrix:
+    """InteractionMatrix (src/rings/configs.jl:292-316): HarmTruncCfg per pair of types."""
+    matrix: Sequence[Sequence[HarmTruncCfg]]
+
+    def get(self, t1: int, t2: int) -> HarmTruncCfg:     # 1-based types
+        return self.matrix[t1 - 1][t2 - 1]
+
+    @property
+    def num_types(self) -> int:
+        return len(self.matrix)
+
+
+def _per_type(v, n):
+    if isinstance(v, (list, tuple, np.ndarray)):
+        if len(v) != n:
+            raise ValueError("per-type parameter has the wrong length")
+        return [float(x) for x in v]
+    return [float(v)] * n
+
+
+@dataclass
+class RingsCfg:
+    """RingsCfg (src/rings/configs.jl:326-381). Scalars or one value per type."""
+    p0: Any
+    relax_time: Any
+    vo: Any
+    mobility: Any
+    rot_diff: Any
+    k_area: Any
+    k_spring: Any
+    l_spring: Any
+    interaction_finder: Any
+    num_particles: Any = -1
+    k_bend: Any = 0.0
+
+    @property
+    def num_types(self) -> int:
+        if isinstance(self.interaction_finder, InteractionMatrix):
+            return self.interaction_finder.num_types
+        lens = [len(v) for v in (self.p0, self.relax_time, self.vo, self.mobility, self.rot_diff, self.k_area,
+                                 self.k_spring, self.l_spring) if isinstance(v, (list, tuple, np.ndarray))]
+        return max(lens) if lens else 1
+
+    def interaction(self, t1: int, t2: int) -> HarmTruncCfg:
+        f = self.interaction_finder
+        return f.get(t1, t2) if isinstance(f, InteractionMatrix) else f
+
+    def type_value(self, name: str, t: int) -> float:     # 1-based
+        return _per_type(getattr(self, name), self.num_types)[t - 1]
+
+    def particle_radius(self):
+        """Minimum particle radius over types (src/rings/configs.jl:438-443)."""
+        return min(self.interaction(t, t).dist_eq / 2.0 for t in range(1, self.num_types + 1))
+
+    def ring_num_particles(self, t: int = 1) -> int:
+        n = self.num_particles
+        return int(n[t - 1]) if isinstance(n, (list, tuple, np.ndarray)) else int(n)
+
+    def fill(self, d: abi.MaviDynamicCfg):
+        d.kind = abi.MAVI_DYN_RINGS
+
+    def fill_rings(self, rc: abi.MaviRingsCfg, num_rings: int, nmax: int, num_particles):
+        nt = self.num_types
+        if nt > abi.MAVI_MAX_TYPES:
+            raise ValueError(f"at most {abi.MAVI_MAX_TYPES} ring types")
+        rc.num_types, rc.num_rings, rc.nmax = nt, num_rings, nmax
+        nps = num_particles if isinstance(num_particles, (list, tuple, np.ndarray)) else [num_particles] * nt
+        for t in range(nt):
+            rc.num_particles[t] = int(nps[t])
+            for name in ("p0", "relax_time", "vo", "mobility", "rot_diff", "k_area", "k_spring", "l_spring", "k_bend"):
+                getattr(rc, name)[t] = self.type_value(name, t + 1)
+            for u in range(nt):
+                it = self.interaction(t + 1, u + 1)
+                rc.inter_k_rep[t][u] = float(it.k_rep)
+                rc.inter_k_atr[t][u] = float(it.k_atr)
+                rc.inter_dist_eq[t][u] = float(it.dist_eq)
+                rc.inter_dist_max[t][u] = float(it.dist_max)
+
+
+def get_area0(cfg: RingsCfg, t: int = 1) -> float:
+    """get_area0 (src/rings/configs.jl:452-457)."""
+    n = cfg.ring_num_particles(t)
+    return (n * cfg.type_value("l_spring", t) / cfg.type_value("p0", t)) ** 2
+
+
+def get_equilibrium_p0(num_particles: int) -> float:
+    """get_equilibrium_p0 (src/rings/configs.jl:464-468)."""
+    theta = 2 * math.pi / num_particles
+    return 2 * (num_particles * (1 - math.cos(theta)) / math.sin(theta)) ** .5
+
+
+def get_ring_radius(p_radius: float, num_particles: int) -> float:
+    """get_ring_radius (src/rings/utils.jl:5-7): radius of the polygon whose
+    consecutive vertices are 2*p_radius apart."""
+    return (p_radius * 2) / (2 * (1 - math.cos(2 * math.pi / num_particles))) ** .5
+
+
+def RingsIntCfg(dt: float, p_chunks_cfg: ChunksCfg | None = None, device: CUDADevice | None = None) -> IntCfg:
+    """RingsIntCfg (src/rings/configs.jl:575-582)."""
+    return IntCfg(dt=dt, chunks_cfg=p_chunks_cfg, device=device or CUDADevice())
+
+
+# ---------------------------------------------------------------------------
+# state (src/rings/states.jl)
+# ---------------------------------------------------------------------------
+class RingsState:
+    """RingsState (src/rings/states.jl:74-124). ``rings_pos`` has shape
+    (num_rings, nmax, 2): the bytes of Julia's column-major
+    Matrix{SVector{2}}(nmax, num_rings); ``pos`` is the flat (num_rings*nmax, 2)
+    view sharing memory with it. ``types`` are 1-based per ring (or None)."""
+    kind = abi.MAVI_STATE_RINGS
+
+    def __init__(self, rings_pos, pol, num_particles=None, types=None):
+        rp = np.ascontiguousarray(np.asarray(rings_pos, dtype=np.float64))
+        if rp.ndim != 3 or rp.shape[2] != 2:
+            raise ValueError("rings_pos must have shape (num_rings, nmax, 2)")
+        self.rings_pos = rp
+        self.pos = rp.reshape(-1, 2)
+        self.pol = np.ascontiguousarray(np.asarray(pol, dtype=np.float64).reshape(-1))
+        self.num_rings, self.nmax = rp.shape[0], rp.shape[1]
+        if self.pol.shape[0] != self.num_rings:
+            raise ValueError("pol must have one entry per ring")
+        self.num_particles = self.nmax if num_particles is None else num_particles
+        self.types = None if types is None else np.ascontiguousarray(np.asarray(types, dtype=np.int32))
+        self.vel = None
+
+    def types_array(self):
+        return self.types if self.types is not None else np.ones(self.num_rings, dtype=np.int32)
+
+    def pol_array(self):
+        return self.pol
+
+    def ring_num_particles(self, ring: int) -> int:
+        n = self.num_particles
+        if isinstance(n, (list, tuple, np.ndarray)):
+            return int(n[self.types_array()[ring] - 1])
+        return int(n)
+
+
+class RingsSystem(System):
+    """RingsSystem (src/rings/rings.jl:231-291) on the GPU."""
+    is_rings = True
+
+    def __init__(self, state: RingsState, space_cfg, dynamic_cfg: RingsCfg, int_cfg: IntCfg,
+                 time_info: TimeInfo | None = None):
+        super().__init__(state, space_cfg, dynamic_cfg, int_cfg, time_info)
+        if dynamic_cfg.num_types > 1 and state.types is None:
+            raise ValueError("DynamicCfg has multiple types, but state.types is nothing!")
+
+    @property
+    def num_slots(self) -> int:
+        return self.state.num_rings * self.state.nmax
+
+    @property
+    def num_pol(self) -> int:
+        return self.state.num_rings
+
+    def fill_params(self, p: abi.MaviReplicaParams, step_kind: int):
+        super().fill_params(p, step_kind)
+        nps = self.state.num_particles
+        if isinstance(self.dynamic_cfg.num_particles, (list, tuple, np.ndarray)) or self.dynamic_cfg.num_particles != -1:
+            nps = self.dynamic_cfg.num_particles
+        self.dynamic_cfg.fill_rings(p.rings, self.state.num_rings, self.state.nmax, nps)
+
+    def chunk_capacity(self) -> int:
+        bb = self.space_cfg.bounding_box()
+        cc = self.int_cfg.chunks_cfg
+        return chunk_capacity(bb.length / cc.num_cols, bb.height / cc.num_rows, self.dynamic_cfg.particle_radius())
+
+
+# ---------------------------------------------------------------------------
+# initial states (src/rings/init_states.jl)
+# ---------------------------------------------------------------------------
+def create_circle(center, radius: float, num_p: int) -> np.ndarray:
+    """create_circle (src/rings/init_states.jl:10-25): (num_p, 2) points."""
+    theta = 2 * math.pi / num_p
+    out = np.empty((num_p, 2))
+    for i in range(num_p):
+        out[i, 0] = radius * math.cos(i * theta) + center[0]
+        out[i, 1] = radius * math.sin(i * theta) + center[1]
+    return out
+
+
+def rectangular_grid(num_cols: int, num_rows: int, num_particles, p_radius, types=None,
+                     pad_x: float = 0.0, pad_y: float = 0.0, radius_k: float = 1.0):
+    """Rings on a rectangular grid (src/rings/init_states.jl:27-72).
+    Returns (rings_pos (num_rings, nmax, 2), RectangleCfg)."""
+    from .configs import RectangleCfg
+    if types is None:
+        num_particles = [num_particles]
+        p_radius = [p_radius]
+        types = [1] * (num_cols * num_rows)
+    ring_r = [get_ring_radius(pr, n) for pr, n in zip(p_radius, num_particles)]
+    ring_length = [2 * (r + pr) for r, pr in zip(ring_r, p_radius)]
+    max_ring_r, max_ring_length, nmax = max(ring_r), max(ring_length), max(num_particles)
+    pad_x = pad_x * max_ring_r
+    pad_y = pad_y * max_ring_r
+    rp = np.zeros((num_cols * num_rows, nmax, 2))
+    idx = 0
+    for col in range(num_cols):
+        for row in range(num_rows):
+            cx = pad_x / 2 + col * (max_ring_length + pad_x) + max_ring_length / 2
+            # the reference spaces rows with pad_x as well
+            cy = pad_y / 2 + row * (max_ring_length + pad_x) + max_ring_length / 2
+            t = types[idx]
+            n = num_particles[t - 1]
+            rp[idx, :n] = create_circle((cx, cy), ring_r[t - 1] * radius_k, n)
+            idx += 1
+    geom = RectangleCfg(length=num_cols * (pad_x + max_ring_length), height=num_rows * (pad_y + max_ring_length))
+    return rp, geom
+
+
+def random_pol(num_rings: int, rng=None) -> np.ndarray:
+    """random_pol (src/rings/init_states.jl:74-80)."""
+    rng = rng or np.random.default_rng()
+    return rng.random(num_rings) * 2 * math.pi

@@ -1,0 +1,1085 @@
+/*
+ * mavi_oracle.c — TEST INFRASTRUCTURE ONLY (see mavi_oracle.h).
+ *
+ * A CPU FP64 restatement of Mavi.jl v1.0.1's step loop. Every function below
+ * follows the reference function it names, keeping its loop order (which fixes
+ * the FP64 summation order) and its evaluation order of each expression. It is
+ * compiled with -ffp-contract=off so that no multiply-add is fused, matching
+ * Julia's IEEE semantics without @fastmath.
+ *
+ * Indices are 0-based here; the reference is 1-based and column-major. A chunk
+ * (row, col) has linear index col*rows + row, matching Julia's
+ * num_particles_in_chunk[row, col] memory order.
+ */
+#include "mavi_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { double x, y; } V2;
+
+static inline V2 v2(double x, double y) { V2 r = {x, y}; return r; }
+static inline V2 vsub(V2 a, V2 b) { return v2(a.x - b.x, a.y - b.y); }
+static inline V2 vadd(V2 a, V2 b) { return v2(a.x + b.x, a.y + b.y); }
+static inline V2 vscale(double s, V2 a) { return v2(s * a.x, s * a.y); }
+static inline double sum_sq(V2 a) { return a.x * a.x + a.y * a.y; }
+
+struct OracleSys {
+    MaviReplicaParams p;
+    int64_t n;              /* slots */
+    double *pos, *vel, *pol;
+    int32_t *types;         /* rings: 1-based type per ring */
+    double *forces;         /* 2n, get_forces(system) == slice 0 */
+    int32_t nthreads;
+    double *slices;         /* (nthreads-1) extra slices of 2n for Threaded */
+    int64_t *pids; int64_t npids;
+    /* chunks (src/chunks.jl:10-25) */
+    int has_chunks;
+    int32_t rows, cols, cap;
+    double chunk_l, chunk_h, bb_len, bb_h, bb_blx, bb_bly;
+    int32_t *chunk_particles;   /* [chunk][cap] */
+    int32_t *num_in_chunk;      /* [chunk] */
+    int32_t *nbr;               /* [chunk][4] */
+    int32_t *nbr_cnt;           /* [chunk] */
+    /* rings */
+    int64_t num_rings; int32_t nmax;
+    double *cont_pos;           /* 2*n */
+    double *areas;              /* num_rings */
+    /* time_info */
+    int64_t num_steps; double time;
+    int32_t err;
+};
+
+/* ------------------------------------------------------------------------ */
+/* Julia Base helpers                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Julia's float `div(x, y)` (RoundToZero): round((x - rem(x, y)) / y) with
+ * rem == C fmod and round == round-half-even (Julia Base, base/div.jl; used at
+ * src/chunks.jl:129-130). */
+double oracle_julia_div(double x, double y) {
+    double r = fmod(x, y);
+    return nearbyint((x - r) / y);
+}
+
+static inline double jsign(double x) { return (x > 0) ? 1.0 : ((x < 0) ? -1.0 : x); }
+
+/* particle_radius (src/configs.jl:418-421; rings src/rings/configs.jl:438-443:
+ * the minimum over types is what get_chunks uses, src/systems.jl:26). */
+static double particle_radius_of(const MaviReplicaParams* p) {
+    const MaviDynamicCfg* d = &p->dyn;
+    switch (d->kind) {
+    case MAVI_DYN_LEN_JONES: return d->sigma * pow(2.0, 1.0 / 6.0) / 2;
+    case MAVI_DYN_SZABO: return d->r_eq / 2;
+    case MAVI_DYN_RUN_TUMBLE: return d->sigma * pow(2.0, 1.0 / 6.0) / 2;
+    case MAVI_DYN_HARM_TRUNC: return d->dist_eq / 2.0;
+    case MAVI_DYN_RINGS: {
+        double m = INFINITY;
+        for (int t = 0; t < p->rings.num_types; t++) {
+            double r = p->rings.inter_dist_eq[t][t] / 2.0;
+            if (r < m) m = r;
+        }
+        return m;
+    }
+    }
+    return NAN;
+}
+
+/* Bounding box of a geometry (src/configs.jl:188-229). */
+static void bbox_of_space(const MaviSpace* sp, double* len, double* h, double* blx, double* bly) {
+    if (sp->geometry == MAVI_GEOM_RECTANGLE) {
+        *len = sp->length; *h = sp->height; *blx = sp->bl_x; *bly = sp->bl_y;
+    } else if (sp->geometry == MAVI_GEOM_CIRCLE) {
+        double r = sp->radius;
+        *len = 2 * r; *h = 2 * r; *blx = sp->cx - r; *bly = sp->cy - r;
+    } else {
+        if (sp->has_bbox) {
+            *len = sp->bbox_length; *h = sp->bbox_height; *blx = sp->bbox_bl_x; *bly = sp->bbox_bl_y;
+            return;
+        }
+        double mxx = -INFINITY, mnx = INFINITY, mxy = -INFINITY, mny = INFINITY;
+        for (int l = 0; l < sp->num_lines; l++) {
+            for (int e = 0; e < 2; e++) {
+                double x = sp->lines[l][2 * e], y = sp->lines[l][2 * e + 1];
+                if (x > mxx) mxx = x; if (x < mnx) mnx = x;
+                if (y > mxy) mxy = y; if (y < mny) mny = y;
+            }
+        }
+        *len = mxx - mnx; *h = mxy - mny; *blx = mnx; *bly = mny;
+    }
+}
+
+/* ManyGeometries bounding box: fold with `+` (src/configs.jl:68-77, 223-229). */
+static void bbox_of(const MaviReplicaParams* p, double* len, double* h, double* blx, double* bly) {
+    bbox_of_space(&p->spaces[0], len, h, blx, bly);
+    for (int k = 1; k < p->num_spaces; k++) {
+        double l2, h2, x2, y2;
+        bbox_of_space(&p->spaces[k], &l2, &h2, &x2, &y2);
+        double max_x = fmax(*blx + *len, x2 + l2);
+        double max_y = fmax(*bly + *h, y2 + h2);
+        double min_x = fmin(*blx, x2);
+        double min_y = fmin(*bly, y2);
+        *h = max_y - min_y; *len = max_x - min_x; *blx = min_x; *bly = min_y;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* calc_diff (src/integration.jl:38-52): the first (wall, geometry) entry     */
+/* decides; minimum image only for PeriodicWalls on a RectangleCfg.          */
+/* ------------------------------------------------------------------------ */
+static inline V2 calc_diff(const OracleSys* s, V2 r1, V2 r2) {
+    V2 dr = vsub(r1, r2);
+    const MaviSpace* sp = &s->p.spaces[0];
+    if (sp->wall == MAVI_WALL_PERIODIC && sp->geometry == MAVI_GEOM_RECTANGLE) {
+        double sx = sp->length, sy = sp->height;
+        /* dr - (abs.(dr) .> size/2) .* copysign.(size, dr) */
+        double mx = (fabs(dr.x) > sx / 2) ? copysign(sx, dr.x) : copysign(0.0, copysign(sx, dr.x));
+        double my = (fabs(dr.y) > sy / 2) ? copysign(sy, dr.y) : copysign(0.0, copysign(sy, dr.y));
+        dr = v2(dr.x - mx, dr.y - my);
+    }
+    return dr;
+}
+
+static inline V2 P(const OracleSys* s, int64_t i) { return v2(s->pos[2 * i], s->pos[2 * i + 1]); }
+
+/* ------------------------------------------------------------------------ */
+/* pair interactions                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* potential_force(dr, dist, ::HarmTruncCfg) (src/configs.jl:354-368). */
+static inline V2 harm_trunc_force(V2 dr, double dist, double k_rep, double k_atr,
+                                  double dist_eq, double dist_max) {
+    if (dist > dist_max) return v2(0, 0);
+    double fmod_;
+    if (dist < dist_eq) fmod_ = -k_rep * (dist / dist_eq - 1);
+    else fmod_ = -k_atr * (dist / dist_eq - 1);
+    return vscale(fmod_ / dist, dr);
+}
+
+/* potential_force(dr, dist, ::LenJonesCfg) (src/configs.jl:389-397): no cutoff. */
+static inline V2 len_jones_force(V2 dr, double dist, double sigma, double epsilon) {
+    double fmod_ = 4 * epsilon * (12 * pow(sigma, 12) / pow(dist, 13) - 6 * pow(sigma, 6) / pow(dist, 7));
+    return vscale(fmod_ / dist, dr);
+}
+
+/* Rings pair force: calc_interaction + calc_interaction_force
+ * (src/rings/integration.jl:32-77) with InteractionMatrix lookup
+ * (src/rings/configs.jl:310-318) and bonded-neighbour exclusion. */
+static inline V2 rings_pair_force(const OracleSys* s, int64_t i, int64_t j) {
+    const MaviRingsCfg* rc = &s->p.rings;
+    int64_t ri = i / s->nmax, rj = j / s->nmax;          /* get_ring_id (src/rings/states.jl:142) */
+    int ti = s->types[ri] - 1, tj = s->types[rj] - 1;
+    double k_rep = rc->inter_k_rep[ti][tj], k_atr = rc->inter_k_atr[ti][tj];
+    double dist_eq = rc->inter_dist_eq[ti][tj], dist_max = rc->inter_dist_max[ti][tj];
+    V2 dr = calc_diff(s, P(s, i), P(s, j));
+    double dist = sqrt(sum_sq(dr));
+    if (dist > dist_max) return v2(0, 0);
+    if (ri == rj) {
+        int64_t diff = llabs(i - j);
+        int64_t num_p = rc->num_particles[ti];
+        if (diff == 1 || diff == num_p - 1) return v2(0, 0);
+    }
+    double fmod_;
+    if (dist < dist_eq) fmod_ = -k_rep * (dist / dist_eq - 1);
+    else fmod_ = (ri == rj) ? 0.0 : -k_atr * (dist / dist_eq - 1);
+    return vscale(fmod_ / dist, dr);
+}
+
+/* calc_interaction (src/integration.jl:62-109): force on i exerted by j. */
+static inline V2 calc_interaction(const OracleSys* s, int64_t i, int64_t j) {
+    const MaviDynamicCfg* d = &s->p.dyn;
+    switch (d->kind) {
+    case MAVI_DYN_HARM_TRUNC: {          /* :62-66 */
+        V2 dr = calc_diff(s, P(s, i), P(s, j));
+        return harm_trunc_force(dr, sqrt(sum_sq(dr)), d->k_rep, d->k_atr, d->dist_eq, d->dist_max);
+    }
+    case MAVI_DYN_LEN_JONES: {           /* :62-66 */
+        V2 dr = calc_diff(s, P(s, i), P(s, j));
+        return len_jones_force(dr, sqrt(sum_sq(dr)), d->sigma, d->epsilon);
+    }
+    case MAVI_DYN_SZABO: {               /* :68-87 */
+        V2 dr = calc_diff(s, P(s, i), P(s, j));
+        double dist = sqrt(sum_sq(dr));
+        if (dist > d->r_max) return v2(0, 0);
+        double f_mod = (dist > d->r_eq) ? d->k_adh / (d->r_eq) : d->k_rep / (d->r_max - d->r_eq);
+        double r = dist - d->r_eq;
+        return vscale(-f_mod * r, dr);
+    }
+    case MAVI_DYN_RUN_TUMBLE: {          /* :89-109 */
+        V2 dr = calc_diff(s, P(s, i), P(s, j));
+        double dist = sqrt(sum_sq(dr));
+        double sigma = d->sigma, epsilon = d->epsilon;
+        double cutoff = pow(2.0, 1.0 / 6.0) * sigma;
+        if (dist > cutoff) return v2(0, 0);
+        double fmod_ = -4 * epsilon * (-12 * pow(sigma, 12) / pow(dist, 13) + 6 * pow(sigma, 6) / pow(dist, 7));
+        return vscale(fmod_ / dist, dr);
+    }
+    case MAVI_DYN_RINGS:
+        return rings_pair_force(s, i, j);
+    }
+    return v2(NAN, NAN);
+}
+
+/* ------------------------------------------------------------------------ */
+/* chunks (src/chunks.jl)                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* get_id inside get_neighbors(…, ::PeriodicWalls) (src/chunks.jl:64-73), 1-based. */
+static int64_t periodic_get_id(int64_t x, int64_t num_t) {
+    if (x == 0) return num_t;
+    if (x % (num_t + 1) == 0) return 1;
+    return x;
+}
+
+static void add_nbr(OracleSys* s, int64_t row1, int64_t col1, int64_t nrow1, int64_t ncol1) {
+    int64_t c = (col1 - 1) * s->rows + (row1 - 1);
+    int64_t nc = (ncol1 - 1) * s->rows + (nrow1 - 1);
+    s->nbr[c * 4 + s->nbr_cnt[c]] = (int32_t)nc;
+    s->nbr_cnt[c] += 1;
+}
+
+/* get_neighbors: periodic (src/chunks.jl:61-87) and open (:89-118). */
+static int build_neighbors(OracleSys* s, int periodic) {
+    int64_t R = s->rows, C = s->cols;
+    memset(s->nbr_cnt, 0, sizeof(int32_t) * R * C);
+    if (periodic) {
+        for (int64_t i = 1; i <= R; i++)
+            for (int64_t j = 1; j <= C; j++) {
+                add_nbr(s, i, j, periodic_get_id(i + 1, R), periodic_get_id(j, C));
+                add_nbr(s, i, j, periodic_get_id(i + 1, R), periodic_get_id(j + 1, C));
+                add_nbr(s, i, j, periodic_get_id(i, R), periodic_get_id(j + 1, C));
+                add_nbr(s, i, j, periodic_get_id(i - 1, R), periodic_get_id(j + 1, C));
+            }
+        return MAVI_OK;
+    }
+    if (C < 2) return MAVI_ERR_UNSUPPORTED; /* reference indexes column 0 (BoundsError) */
+    for (int64_t i = 1; i <= R - 1; i++) {
+        int64_t c1 = (1 - 1) * R + (i - 1);
+        s->nbr_cnt[c1] = 0;
+        add_nbr(s, i, 1, i + 1, 1);
+        add_nbr(s, i, 1, i + 1, 2);
+        add_nbr(s, i, 1, i, 2);
+        for (int64_t j = 2; j <= C - 1; j++) {
+            add_nbr(s, i, j, i + 1, j - 1);
+            add_nbr(s, i, j, i + 1, j);
+            add_nbr(s, i, j, i + 1, j + 1);
+            add_nbr(s, i, j, i, j + 1);
+        }
+        int64_t cl = (C - 1) * R + (i - 1);
+        s->nbr_cnt[cl] = 0;    /* neighbors[i, num_cols] is assigned, not appended */
+        add_nbr(s, i, C, i + 1, C - 1);
+        add_nbr(s, i, C, i + 1, C);
+    }
+    for (int64_t j = 1; j <= C - 1; j++) add_nbr(s, R, j, R, j + 1);
+    return MAVI_OK;
+}
+
+/* update_particle_chunk! index computation (src/chunks.jl:120-142). */
+int32_t oracle_chunk_of(OracleSys* s, double x, double y, int64_t* row, int64_t* col) {
+    double qr = oracle_julia_div(-y + s->bb_bly + s->bb_h, s->chunk_h);
+    double qc = oracle_julia_div(x - s->bb_blx, s->chunk_l);
+    if (!isfinite(qr) || !isfinite(qc)) return MAVI_ERR_NONFINITE;
+    int64_t r = (int64_t)qr + 1;
+    int64_t c = (int64_t)qc + 1;
+    r -= (r == s->rows + 1) ? 1 : 0;
+    c -= (c == s->cols + 1) ? 1 : 0;
+    *row = r; *col = c;
+    return MAVI_OK;
+}
+
+/* update_chunks! (src/chunks.jl:150-161; State-aware variant
+ * src/integration.jl:54-59; rings src/rings/integration.jl:18-23):
+ * particles are appended in ascending id order. */
+int32_t oracle_update_chunks(OracleSys* s) {
+    if (!s->has_chunks) return MAVI_OK;
+    int64_t nch = (int64_t)s->rows * s->cols;
+    memset(s->num_in_chunk, 0, sizeof(int32_t) * nch);
+    for (int64_t k = 0; k < s->npids; k++) {
+        int64_t i = s->pids[k];
+        int64_t r, c;
+        int32_t st = oracle_chunk_of(s, s->pos[2 * i], s->pos[2 * i + 1], &r, &c);
+        if (st) return s->err = st;
+        if (r < 1 || r > s->rows || c < 1 || c > s->cols) return s->err = MAVI_ERR_OUT_OF_GRID;
+        int64_t ch = (c - 1) * s->rows + (r - 1);
+        int32_t pi = s->num_in_chunk[ch];
+        if (pi >= s->cap) return s->err = MAVI_ERR_CHUNK_OVERFLOW;
+        s->chunk_particles[ch * s->cap + pi] = (int32_t)i;
+        s->num_in_chunk[ch] += 1;
+    }
+    return MAVI_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* calc_forces!                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Chunk loop body shared by Sequencial (src/integration.jl:112-157) and each
+ * thread of Threaded (:159-194): columns [c0, c1). */
+static void chunk_force_columns(const OracleSys* s, double* F, int64_t c0, int64_t c1) {
+    for (int64_t col = c0; col < c1; col++) {
+        for (int64_t row = 0; row < s->rows; row++) {
+            int64_t ch = col * s->rows + row;
+            int32_t np = s->num_in_chunk[ch];
+            const int32_t* chunk = s->chunk_particles + ch * s->cap;
+            for (int32_t i = 0; i < np; i++) {
+                int64_t p1 = chunk[i];
+                for (int32_t j = i + 1; j < np; j++) {
+                    int64_t p2 = chunk[j];
+                    V2 f1 = calc_interaction(s, p1, p2);
+                    F[2 * p1] += f1.x; F[2 * p1 + 1] += f1.y;
+                    F[2 * p2] -= f1.x; F[2 * p2 + 1] -= f1.y;
+                }
+                for (int32_t k = 0; k < s->nbr_cnt[ch]; k++) {
+                    int64_t nb = s->nbr[ch * 4 + k];
+                    int32_t nnp = s->num_in_chunk[nb];
+                    const int32_t* nchunk = s->chunk_particles + nb * s->cap;
+                    for (int32_t j = 0; j < nnp; j++) {
+                        int64_t p2 = nchunk[j];
+                        V2 f1 = calc_interaction(s, p1, p2);
+                        F[2 * p1] += f1.x; F[2 * p1 + 1] += f1.y;
+                        F[2 * p2] -= f1.x; F[2 * p2 + 1] -= f1.y;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* calc_forces!(system, ::Nothing, ::Sequencial) (src/integration.jl:197-224). */
+static void all_pairs_forces(const OracleSys* s, double* F) {
+    for (int64_t a = 0; a < s->npids; a++)
+        for (int64_t b = a + 1; b < s->npids; b++) {
+            int64_t pi = s->pids[a], pj = s->pids[b];
+            V2 f = calc_interaction(s, pi, pj);
+            F[2 * pi] += f.x; F[2 * pi + 1] += f.y;
+            F[2 * pj] -= f.x; F[2 * pj + 1] -= f.y;
+        }
+}
+
+static void clean_forces(OracleSys* s) {     /* src/systems.jl:119-123 */
+    memset(s->forces, 0, sizeof(double) * 2 * s->n);
+    if (s->slices) memset(s->slices, 0, sizeof(double) * 2 * s->n * (s->nthreads - 1));
+}
+
+static int32_t calc_forces(OracleSys* s, int32_t mode) {
+    if (mode == ORACLE_FORCES_ALL_PAIRS || !s->has_chunks) {
+        all_pairs_forces(s, s->forces);
+        return MAVI_OK;
+    }
+    if (mode == ORACLE_FORCES_SEQUENTIAL || s->nthreads <= 1) {
+        chunk_force_columns(s, s->forces, 0, s->cols);
+        return MAVI_OK;
+    }
+    /* Threads.@threads :static over columns: contiguous blocks, the first
+     * `rem` blocks one column longer; private slices summed in slice order. */
+    int nt = s->nthreads;
+    int64_t len = s->cols / nt, rem = s->cols % nt;
+#pragma omp parallel for schedule(static, 1) num_threads(nt)
+    for (int t = 0; t < nt; t++) {
+        int64_t f = t * len, l = f + len;
+        if (rem > 0) {
+            if (t < rem) { f += t; l += t + 1; }
+            else { f += rem; l += rem; }
+        }
+        double* F = (t == 0) ? s->forces : s->slices + (int64_t)(t - 1) * 2 * s->n;
+        chunk_force_columns(s, F, f, l);
+    }
+    /* get_forces(system) .= sum(system.forces) */
+    for (int64_t k = 0; k < 2 * s->n; k++) {
+        double acc = s->forces[k];
+        for (int t = 1; t < nt; t++) acc += s->slices[(int64_t)(t - 1) * 2 * s->n + k];
+        s->forces[k] = acc;
+    }
+    return MAVI_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* calc_walls_forces! (src/integration.jl:228-266)                           */
+/* ------------------------------------------------------------------------ */
+
+static double process_dist(int mode, double dist, double inside_flag) {  /* src/configs.jl:259-261 */
+    if (mode == MAVI_POTMODE_OUTSIDE) return inside_flag * dist;
+    if (mode == MAVI_POTMODE_INSIDE) return -inside_flag * dist;
+    return dist;
+}
+
+static V2 wall_potential_force(const MaviSpace* sp, V2 dr, double dist) {
+    if (sp->pot_kind == MAVI_DYN_LEN_JONES)
+        return len_jones_force(dr, dist, sp->pot_params[0], sp->pot_params[1]);
+    return harm_trunc_force(dr, dist, sp->pot_params[0], sp->pot_params[1], sp->pot_params[2], sp->pot_params[3]);
+}
+
+static void walls_forces_space(OracleSys* s, const MaviSpace* sp) {
+    if (sp->wall != MAVI_WALL_POTENTIAL) return;
+    for (int64_t k = 0; k < s->npids; k++) {
+        int64_t i = s->pids[k];
+        V2 pos = P(s, i);
+        if (sp->geometry == MAVI_GEOM_CIRCLE) {
+            /* signed_pos(point, ::CircleCfg) (src/configs.jl:154-163) */
+            V2 dr = vsub(pos, v2(sp->cx, sp->cy));
+            double dist = pow(sum_sq(dr), .5);
+            V2 dr_hat = v2(dr.x / dist, dr.y / dist);
+            dr = vsub(dr, v2(dr_hat.x * sp->radius, dr_hat.y * sp->radius));
+            double sign_dist = dist - sp->radius;
+            double d2 = process_dist(sp->pot_mode, fabs(sign_dist), jsign(sign_dist));
+            V2 f = wall_potential_force(sp, dr, d2);
+            s->forces[2 * i] += f.x; s->forces[2 * i + 1] += f.y;
+        } else if (sp->geometry == MAVI_GEOM_LINES) {
+            for (int l = 0; l < sp->num_lines; l++) {
+                /* Line2D (src/configs.jl:102-117) + signed_pos(point, ::Line2D) (:119-135) */
+                V2 p1 = v2(sp->lines[l][0], sp->lines[l][1]);
+                V2 p2 = v2(sp->lines[l][2], sp->lines[l][3]);
+                V2 d = vsub(p2, p1);
+                double norm = sqrt(d.x * d.x + d.y * d.y);
+                V2 t = v2(d.x / norm, d.y / norm);
+                V2 dr = vsub(pos, p1);
+                double delta_t = dr.x * t.x + dr.y * t.y;
+                if (delta_t > 0) {
+                    if (delta_t < norm) {
+                        V2 base = vadd(p1, v2(t.x * delta_t, t.y * delta_t));
+                        dr = vsub(pos, base);
+                    } else {
+                        dr = vsub(pos, p2);
+                    }
+                }
+                double dist = sqrt(sum_sq(dr));
+                double d2 = process_dist(sp->pot_mode, dist, 1.0);
+                V2 f = wall_potential_force(sp, dr, d2);
+                s->forces[2 * i] += f.x; s->forces[2 * i + 1] += f.y;
+            }
+        }
+    }
+}
+
+static void calc_walls_forces(OracleSys* s) {
+    for (int k = 0; k < s->p.num_spaces; k++) walls_forces_space(s, &s->p.spaces[k]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* walls! (src/integration.jl:268-412)                                       */
+/* ------------------------------------------------------------------------ */
+
+/* get_particle_radius (src/systems.jl:131; rings per type src/rings/rings.jl:45-53). */
+static double particle_radius_at(const OracleSys* s, int64_t pid) {
+    if (s->p.state_kind == MAVI_STATE_RINGS) {
+        int t = s->types[pid / s->nmax] - 1;
+        return s->p.rings.inter_dist_eq[t][t] / 2.0;
+    }
+    return particle_radius_of(&s->p);
+}
+
+static void walls_space(OracleSys* s, const MaviSpace* sp) {
+    double r = particle_radius_of(&s->p);
+    if (sp->wall == MAVI_WALL_RIGID && sp->geometry == MAVI_GEOM_RECTANGLE) {   /* :271-285 */
+        if (!s->vel) return;
+        for (int64_t k = 0; k < s->npids; k++) {
+            int64_t i = s->pids[k];
+            double rx = s->pos[2 * i] - sp->bl_x, ry = s->pos[2 * i + 1] - sp->bl_y;
+            int ox = (rx + r) > sp->length || (rx - r) < 0;
+            int oy = (ry + r) > sp->height || (ry - r) < 0;
+            if (ox || oy) {
+                s->vel[2 * i] = s->vel[2 * i] * (-2 * ox + 1);
+                s->vel[2 * i + 1] = s->vel[2 * i + 1] * (-2 * oy + 1);
+            }
+        }
+    } else if (sp->wall == MAVI_WALL_RIGID && sp->geometry == MAVI_GEOM_CIRCLE) {  /* :287-306 */
+        if (!s->vel) return;
+        double max_r2 = (sp->radius - r) * (sp->radius - r);
+        for (int64_t k = 0; k < s->npids; k++) {
+            int64_t i = s->pids[k];
+            double px = s->pos[2 * i], py = s->pos[2 * i + 1];
+            double dx = px - sp->cx, dy = py - sp->cy;
+            double d2x = dx * dx, d2y = dy * dy;
+            double r2 = d2x + d2y;
+            if (r2 <= max_r2) continue;
+            double vx = s->vel[2 * i], vy = s->vel[2 * i + 1];
+            double nvx = (vx * (d2y - d2x) - 2 * vy * px * py) / r2;
+            double nvy = (-vy * (d2y - d2x) - 2 * vx * px * py) / r2;
+            s->vel[2 * i] = nvx; s->vel[2 * i + 1] = nvy;
+        }
+    } else if (sp->wall == MAVI_WALL_PERIODIC && sp->geometry == MAVI_GEOM_RECTANGLE) { /* :309-324 */
+        double cx = sp->bl_x + sp->length / 2, cy = sp->bl_y + sp->height / 2;
+        double hx = sp->length / 2, hy = sp->height / 2;
+        for (int64_t k = 0; k < s->npids; k++) {
+            int64_t i = s->pids[k];
+            double px = s->pos[2 * i], py = s->pos[2 * i + 1];
+            double dx = px - cx, dy = py - cy;
+            int ox = fabs(dx) > hx, oy = fabs(dy) > hy;
+            if (ox || oy) {
+                if (ox) s->pos[2 * i] = px - jsign(dx) * (hx * 2);
+                if (oy) s->pos[2 * i + 1] = py - jsign(dy) * (hy * 2);
+            }
+        }
+    } else if (sp->wall == MAVI_WALL_SLIPPERY && sp->geometry == MAVI_GEOM_LINES) {  /* :327-378 */
+        for (int64_t k = 0; k < s->npids; k++) {
+            int64_t pid = s->pids[k];
+            double p_radius = particle_radius_at(s, pid);
+            V2 pos_i = P(s, pid);     /* read once, as the reference does */
+            for (int l = 0; l < sp->num_lines; l++) {
+                V2 p1 = v2(sp->lines[l][0], sp->lines[l][1]);
+                V2 p2 = v2(sp->lines[l][2], sp->lines[l][3]);
+                V2 d = vsub(p2, p1);
+                double norm = sqrt(d.x * d.x + d.y * d.y);
+                V2 nrm = v2(-d.y / norm, d.x / norm);
+                V2 tan_ = v2(d.x / norm, d.y / norm);
+                V2 dr = vsub(pos_i, p1);
+                double delta_s = dr.x * nrm.x + dr.y * nrm.y;
+                if (fabs(delta_s) > p_radius) continue;
+                double delta_t = dr.x * tan_.x + dr.y * tan_.y;
+                int is_corner = 0; V2 corner_p = p1;
+                if (delta_t > 0) {
+                    if (delta_t > norm) {
+                        if (delta_t > (norm + p_radius)) continue;
+                        is_corner = 1; corner_p = p2;
+                    }
+                } else if (delta_t > -p_radius) {
+                    is_corner = 1; corner_p = p1;
+                } else {
+                    continue;
+                }
+                if (is_corner) {
+                    V2 drc = vsub(pos_i, corner_p);
+                    double nn = sqrt(drc.x * drc.x + drc.y * drc.y);
+                    if (nn > p_radius) continue;
+                    double alpha = p_radius / nn - 1;
+                    s->pos[2 * pid] += alpha * drc.x; s->pos[2 * pid + 1] += alpha * drc.y;
+                } else {
+                    double sgn = jsign(delta_s);
+                    double alpha = sgn * (p_radius - sgn * delta_s);
+                    s->pos[2 * pid] += alpha * nrm.x; s->pos[2 * pid + 1] += alpha * nrm.y;
+                }
+            }
+        }
+    } else if (sp->wall == MAVI_WALL_SLIPPERY && sp->geometry == MAVI_GEOM_CIRCLE) {  /* :380-401 */
+        for (int64_t k = 0; k < s->npids; k++) {
+            int64_t pid = s->pids[k];
+            V2 p = P(s, pid);
+            double pr = particle_radius_at(s, pid);
+            double max_r_2 = (sp->radius + pr) * (sp->radius + pr);
+            V2 dr = calc_diff(s, p, v2(sp->cx, sp->cy));
+            double dr_2 = sum_sq(dr);
+            if (dr_2 > max_r_2) continue;
+            double dr_norm = sqrt(dr_2);
+            double kk = sp->radius + pr - dr_norm;
+            s->pos[2 * pid] = p.x + kk * dr.x / dr_norm;
+            s->pos[2 * pid + 1] = p.y + kk * dr.y / dr_norm;
+        }
+    }
+}
+
+static void walls(OracleSys* s) {           /* ManyWalls: in order (:404-408) */
+    for (int k = 0; k < s->p.num_spaces; k++) walls_space(s, &s->p.spaces[k]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* rings terms (src/rings/integration.jl)                                    */
+/* ------------------------------------------------------------------------ */
+
+static inline int32_t ring_n(const OracleSys* s, int64_t ring) {
+    return s->p.rings.num_particles[s->types[ring] - 1];
+}
+
+/* update_continuos_pos! (src/rings/integration.jl:118-138): periodic only. */
+static void update_continuos_pos(OracleSys* s) {
+    const MaviSpace* sp = &s->p.spaces[0];
+    int periodic = (sp->wall == MAVI_WALL_PERIODIC);
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        int64_t base = ring * s->nmax;
+        for (int64_t i = 0; i < s->nmax; i++) {
+            s->cont_pos[2 * (base + i)] = s->pos[2 * (base + i)];
+            s->cont_pos[2 * (base + i) + 1] = s->pos[2 * (base + i) + 1];
+        }
+        if (!periodic) continue;
+        for (int64_t i = 1; i < ring_n(s, ring); i++) {
+            V2 dr = calc_diff(s, P(s, base + i), P(s, base + i - 1));
+            s->cont_pos[2 * (base + i)] = s->cont_pos[2 * (base + i - 1)] + dr.x;
+            s->cont_pos[2 * (base + i) + 1] = s->cont_pos[2 * (base + i - 1) + 1] + dr.y;
+        }
+    }
+}
+
+/* calc_area (src/rings/integration.jl:103-116). */
+static double calc_area(const double* rp, int32_t n) {
+    double area = 0.0;
+    for (int32_t i = 0; i < n - 1; i++)
+        area += rp[2 * i] * rp[2 * (i + 1) + 1] - rp[2 * i + 1] * rp[2 * (i + 1)];
+    area += rp[2 * (n - 1)] * rp[1] - rp[2 * (n - 1) + 1] * rp[0];
+    return area / 2.0;
+}
+
+/* forces!: springs (src/rings/integration.jl:79-97, 205-223), area_forces!
+ * (:140-195), then the bending term (an addition, zero when k_bend == 0):
+ * E = k_bend * sum_i (1 - cos theta_i), theta_i the angle between the bonds
+ * entering and leaving particle i. */
+static void rings_bonded_forces(OracleSys* s) {
+    const MaviRingsCfg* rc = &s->p.rings;
+    double* F = s->forces;
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        int t = s->types[ring] - 1;
+        int32_t n = rc->num_particles[t];
+        double k = rc->k_spring[t], l = rc->l_spring[t];
+        for (int32_t sid = 0; sid < n; sid++) {
+            int64_t p1 = ring * s->nmax + sid;
+            int64_t p2 = ring * s->nmax + ((sid == n - 1) ? 0 : sid + 1);
+            V2 dr = calc_diff(s, P(s, p1), P(s, p2));
+            double dist = sqrt(sum_sq(dr));
+            double fmod_ = -k * (dist - l);
+            V2 f = vscale(fmod_ / dist, dr);
+            F[2 * p1] += f.x; F[2 * p1 + 1] += f.y;
+            F[2 * p2] -= f.x; F[2 * p2 + 1] -= f.y;
+        }
+    }
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        int t = s->types[ring] - 1;
+        int32_t n = rc->num_particles[t];
+        double area = calc_area(s->cont_pos + 2 * ring * s->nmax, n);
+        s->areas[ring] = area;
+        double k_area = rc->k_area[t], p0 = rc->p0[t], l0 = rc->l_spring[t];
+        double a0 = (n * l0 / p0);
+        double area0 = a0 * a0;
+        for (int32_t i = 0; i < n; i++) {
+            double fmod_ = k_area * (area - area0);
+            int32_t id1 = (i == 0) ? n - 1 : i - 1;
+            int32_t id2 = (i == n - 1) ? 0 : i + 1;
+            V2 dr = calc_diff(s, P(s, ring * s->nmax + id2), P(s, ring * s->nmax + id1));
+            V2 a_deriv = v2(dr.y / 2, -dr.x / 2);
+            int64_t idx = ring * s->nmax + i;
+            F[2 * idx] -= fmod_ * a_deriv.x; F[2 * idx + 1] -= fmod_ * a_deriv.y;
+        }
+    }
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        int t = s->types[ring] - 1;
+        int32_t n = rc->num_particles[t];
+        double kb = rc->k_bend[t];
+        if (kb == 0.0) continue;
+        for (int32_t i = 0; i < n; i++) {
+            int64_t im = ring * s->nmax + ((i == 0) ? n - 1 : i - 1);
+            int64_t ic = ring * s->nmax + i;
+            int64_t ip = ring * s->nmax + ((i == n - 1) ? 0 : i + 1);
+            V2 a = calc_diff(s, P(s, ic), P(s, im));
+            V2 b = calc_diff(s, P(s, ip), P(s, ic));
+            double la = sqrt(sum_sq(a)), lb = sqrt(sum_sq(b));
+            double c = (a.x * b.x + a.y * b.y) / (la * lb);
+            /* dc/da = b/(|a||b|) - c a/|a|^2 ; dc/db = a/(|a||b|) - c b/|b|^2 */
+            V2 dca = v2(b.x / (la * lb) - c * a.x / (la * la), b.y / (la * lb) - c * a.y / (la * la));
+            V2 dcb = v2(a.x / (la * lb) - c * b.x / (lb * lb), a.y / (la * lb) - c * b.y / (lb * lb));
+            F[2 * im] += -kb * dca.x;            F[2 * im + 1] += -kb * dca.y;
+            F[2 * ic] += kb * (dca.x - dcb.x);   F[2 * ic + 1] += kb * (dca.y - dcb.y);
+            F[2 * ip] += kb * dcb.x;             F[2 * ip + 1] += kb * dcb.y;
+        }
+    }
+}
+
+/* update! (src/rings/integration.jl:300-351); noise: one N(0,1) per ring. */
+static void rings_update(OracleSys* s, const double* noise) {
+    const MaviRingsCfg* rc = &s->p.rings;
+    double dt = s->p.dt;
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        int t = s->types[ring] - 1;
+        int32_t n = rc->num_particles[t];
+        double vo = rc->vo[t], relax_time = rc->relax_time[t], mu = rc->mobility[t], dr = rc->rot_diff[t];
+        double theta = s->pol[ring];
+        V2 pol = v2(cos(theta), sin(theta));
+        V2 vel_cm = v2(0, 0);
+        for (int32_t i = 0; i < n; i++) {
+            int64_t p = ring * s->nmax + i;
+            V2 vel = vadd(vscale(vo, pol), vscale(mu, v2(s->forces[2 * p], s->forces[2 * p + 1])));
+            vel_cm = vadd(vel_cm, vel);
+            s->pos[2 * p] += vel.x * dt; s->pos[2 * p + 1] += vel.y * dt;
+        }
+        vel_cm = v2(vel_cm.x / n, vel_cm.y / n);
+        double speed = sqrt(sum_sq(vel_cm));
+        double cross;
+        if (speed == 0) cross = 0;
+        else {
+            cross = (pol.x * vel_cm.y - pol.y * vel_cm.x) / speed;
+            if (fabs(cross) > 1) cross = jsign(cross);
+        }
+        double d_theta = 1 / relax_time * asin(cross) * dt + sqrt(2 * dr * dt) * noise[ring];
+        s->pol[ring] += d_theta;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* integrators (src/integration.jl:415-498)                                  */
+/* ------------------------------------------------------------------------ */
+
+static void update_szabo(OracleSys* s, const double* noise) {      /* :433-465 */
+    const MaviDynamicCfg* d = &s->p.dyn;
+    double dt = s->p.dt;
+    double vo = d->vo, relax_time = d->relax_time, mu = d->mobility, dr = d->rot_diff;
+    for (int64_t i = 0; i < s->n; i++) {
+        double theta = s->pol[i];
+        V2 pol = v2(cos(theta), sin(theta));
+        V2 vel = vadd(vscale(vo, pol), vscale(mu, v2(s->forces[2 * i], s->forces[2 * i + 1])));
+        double speed = sqrt(fabs(vel.x) + fabs(vel.y));
+        double cross = (speed > 0) ? (pol.x * vel.y - pol.y * vel.x) / speed : 0;
+        if (fabs(cross) > 1) cross = jsign(cross);
+        double d_theta = 1 / relax_time * asin(cross) * dt + sqrt(2 * dr * dt) * noise[i];
+        s->pos[2 * i] += vel.x * dt; s->pos[2 * i + 1] += vel.y * dt;
+        s->pol[i] += d_theta;
+    }
+}
+
+static void update_rtp(OracleSys* s, const double* noise) {        /* :467-498 */
+    const MaviDynamicCfg* d = &s->p.dyn;
+    double dt = s->p.dt;
+    for (int64_t i = 0; i < s->n; i++) {
+        double theta = s->pol[i];
+        V2 pol = v2(cos(theta), sin(theta));
+        V2 vel = vadd(vscale(d->vo, pol), v2(s->forces[2 * i], s->forces[2 * i + 1]));
+        s->pos[2 * i] += vel.x * dt; s->pos[2 * i + 1] += vel.y * dt;
+        double u = noise[2 * i];
+        if (u < d->tumble_rate * dt) s->pol[i] = 2 * M_PI * noise[2 * i + 1];
+    }
+}
+
+int64_t oracle_noise_count(OracleSys* s) {
+    switch (s->p.step_kind) {
+    case MAVI_STEP_SZABO: return s->n;
+    case MAVI_STEP_RTP: return 2 * s->n;
+    case MAVI_STEP_RINGS: return s->num_rings;
+    }
+    return 0;
+}
+
+static void update_time(OracleSys* s) {                            /* :500-503 */
+    s->time += s->p.dt;
+    s->num_steps += 1;
+}
+
+/* One step of the replica's step function. */
+static int32_t step_once(OracleSys* s, int32_t fm, const double* noise) {
+    int32_t st;
+    double dt = s->p.dt;
+    switch (s->p.step_kind) {
+    case MAVI_STEP_NEWTON: {                                        /* :507-515 */
+        clean_forces(s);
+        if ((st = oracle_update_chunks(s))) return st;
+        calc_forces(s, fm);
+        calc_walls_forces(s);
+        /* update_verlet! (:415-431) */
+        double* old = (double*)malloc(sizeof(double) * 2 * s->n);
+        memcpy(old, s->forces, sizeof(double) * 2 * s->n);
+        double term = dt * dt / 2;
+        for (int64_t k = 0; k < 2 * s->n; k++) s->pos[k] += s->vel[k] * dt + s->forces[k] * term;
+        clean_forces(s);
+        calc_forces(s, fm);
+        for (int64_t k = 0; k < 2 * s->n; k++) s->vel[k] += dt / 2 * (s->forces[k] + old[k]);
+        free(old);
+        walls(s);
+        update_time(s);
+        return MAVI_OK;
+    }
+    case MAVI_STEP_OVERDAMPED: {
+        clean_forces(s);
+        if ((st = oracle_update_chunks(s))) return st;
+        calc_forces(s, fm);
+        calc_walls_forces(s);
+        double mdt = s->p.dyn.mobility * dt;
+        for (int64_t k = 0; k < 2 * s->n; k++) s->pos[k] += s->forces[k] * mdt;
+        walls(s);
+        update_time(s);
+        return MAVI_OK;
+    }
+    case MAVI_STEP_SZABO:                                           /* :517-525 */
+    case MAVI_STEP_RTP:                                             /* :527-535 */
+        clean_forces(s);
+        if ((st = oracle_update_chunks(s))) return st;
+        calc_forces(s, fm);
+        calc_walls_forces(s);
+        if (s->p.step_kind == MAVI_STEP_SZABO) update_szabo(s, noise);
+        else update_rtp(s, noise);
+        walls(s);
+        update_time(s);
+        return MAVI_OK;
+    case MAVI_STEP_RINGS:                           /* src/rings/integration.jl:522-543 */
+        if ((st = oracle_update_chunks(s))) return st;
+        update_continuos_pos(s);
+        clean_forces(s);
+        calc_forces(s, fm);
+        rings_bonded_forces(s);
+        calc_walls_forces(s);
+        rings_update(s, noise);
+        walls(s);
+        s->num_steps += 1;
+        s->time += dt;
+        return MAVI_OK;
+    }
+    return MAVI_ERR_UNSUPPORTED;
+}
+
+int32_t oracle_step(OracleSys* s, int64_t nsteps, int32_t force_mode, const double* noise) {
+    int64_t nc = oracle_noise_count(s);
+    for (int64_t k = 0; k < nsteps; k++) {
+        int32_t st = step_once(s, force_mode, noise ? noise + k * nc : NULL);
+        if (st) return s->err = st;
+    }
+    return MAVI_OK;
+}
+
+int32_t oracle_calc_forces(OracleSys* s, int32_t mode, int32_t include_walls, double* out) {
+    int32_t st;
+    clean_forces(s);
+    if ((st = oracle_update_chunks(s))) return st;
+    if (s->p.state_kind == MAVI_STATE_RINGS) update_continuos_pos(s);
+    calc_forces(s, mode);
+    if (s->p.state_kind == MAVI_STATE_RINGS) rings_bonded_forces(s);
+    if (include_walls) calc_walls_forces(s);
+    memcpy(out, s->forces, sizeof(double) * 2 * s->n);
+    return MAVI_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* energies (src/quantities.jl)                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Pair potential consistent with each force law. LenJones follows
+ * src/quantities.jl:46-66; the HarmTrunc energy of the reference
+ * (:21-44) reads fields that do not exist, so it is written from the force
+ * law: U = k/(2 dist_eq) (d - dist_eq)^2, k = k_rep below dist_eq, k_atr
+ * above, 0 beyond dist_max. RunTumble is the unshifted WCA. */
+static double pair_energy(const OracleSys* s, int64_t i, int64_t j) {
+    const MaviDynamicCfg* d = &s->p.dyn;
+    V2 dr = calc_diff(s, P(s, i), P(s, j));
+    double dist = sqrt(sum_sq(dr));
+    switch (d->kind) {
+    case MAVI_DYN_LEN_JONES:
+        return pow(d->sigma / dist, 12) - pow(d->sigma / dist, 6);     /* times 4 eps later */
+    case MAVI_DYN_HARM_TRUNC: {
+        if (dist > d->dist_max) return 0.0;
+        double k = dist < d->dist_eq ? d->k_rep : d->k_atr;
+        double x = dist - d->dist_eq;
+        return k / (2 * d->dist_eq) * x * x;
+    }
+    case MAVI_DYN_RUN_TUMBLE: {
+        if (dist > pow(2.0, 1.0 / 6.0) * d->sigma) return 0.0;
+        return pow(d->sigma / dist, 12) - pow(d->sigma / dist, 6);
+    }
+    }
+    return NAN;
+}
+
+int32_t oracle_energies(OracleSys* s, int32_t pe_mode, double* ke, double* pe) {
+    double k = 0;
+    if (s->vel) {
+        for (int64_t i = 0; i < s->n; i++) k += s->vel[2 * i] * s->vel[2 * i] + s->vel[2 * i + 1] * s->vel[2 * i + 1];
+    }
+    *ke = k / 2;
+    int kind = s->p.dyn.kind;
+    if (kind != MAVI_DYN_LEN_JONES && kind != MAVI_DYN_HARM_TRUNC && kind != MAVI_DYN_RUN_TUMBLE) {
+        *pe = NAN;
+        return MAVI_OK;
+    }
+    double pot = 0.0;
+    if (pe_mode == MAVI_PE_ALL_PAIRS || !s->has_chunks) {
+        for (int64_t a = 0; a < s->npids; a++)
+            for (int64_t b = a + 1; b < s->npids; b++) pot += pair_energy(s, s->pids[a], s->pids[b]);
+    } else {
+        int32_t st = oracle_update_chunks(s);
+        if (st) return st;
+        for (int64_t col = 0; col < s->cols; col++)
+            for (int64_t row = 0; row < s->rows; row++) {
+                int64_t ch = col * s->rows + row;
+                int32_t np = s->num_in_chunk[ch];
+                const int32_t* chunk = s->chunk_particles + ch * s->cap;
+                for (int32_t i = 0; i < np; i++) {
+                    for (int32_t j = i + 1; j < np; j++) pot += pair_energy(s, chunk[i], chunk[j]);
+                    for (int32_t kk = 0; kk < s->nbr_cnt[ch]; kk++) {
+                        int64_t nb = s->nbr[ch * 4 + kk];
+                        for (int32_t j = 0; j < s->num_in_chunk[nb]; j++)
+                            pot += pair_energy(s, chunk[i], s->chunk_particles[nb * s->cap + j]);
+                    }
+                }
+            }
+    }
+    if (kind != MAVI_DYN_HARM_TRUNC) pot *= 4 * s->p.dyn.epsilon;
+    *pe = pot;
+    return MAVI_OK;
+}
+
+int64_t oracle_count_pairs(OracleSys* s) {
+    if (!s->has_chunks) return s->npids * (s->npids - 1) / 2;
+    if (oracle_update_chunks(s)) return -1;
+    int64_t pairs = 0;
+    for (int64_t ch = 0; ch < (int64_t)s->rows * s->cols; ch++) {
+        int64_t np = s->num_in_chunk[ch];
+        pairs += np * (np - 1) / 2;
+        for (int32_t k = 0; k < s->nbr_cnt[ch]; k++) pairs += np * s->num_in_chunk[s->nbr[ch * 4 + k]];
+    }
+    return pairs;
+}
+
+/* ------------------------------------------------------------------------ */
+/* construction                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* check_inside (src/space_checks.jl:9-37, 53-60): rectangle bounds; circle
+ * tests |p|^2 > R^2 around the origin (the reference ignores the centre). */
+static int outside_space(const OracleSys* s) {
+    if (s->p.num_spaces != 1) return 0;           /* ManyGeometries: no check */
+    const MaviSpace* sp = &s->p.spaces[0];
+    for (int64_t k = 0; k < s->npids; k++) {
+        int64_t i = s->pids[k];
+        double x = s->pos[2 * i], y = s->pos[2 * i + 1];
+        if (sp->geometry == MAVI_GEOM_RECTANGLE) {
+            if (x < sp->bl_x || y < sp->bl_y || x > sp->bl_x + sp->length || y > sp->bl_y + sp->height) return 1;
+        } else if (sp->geometry == MAVI_GEOM_CIRCLE) {
+            if (x * x + y * y > sp->radius * sp->radius) return 1;
+        }
+    }
+    return 0;
+}
+
+OracleSys* oracle_create(const MaviReplicaParams* p, const double* pos, const double* vel,
+                         const double* pol, const int32_t* ring_types, int32_t nthreads,
+                         int32_t* status) {
+    OracleSys* s = (OracleSys*)calloc(1, sizeof(OracleSys));
+    s->p = *p;
+    s->n = p->num_particles;
+    s->pos = (double*)malloc(sizeof(double) * 2 * s->n);
+    memcpy(s->pos, pos, sizeof(double) * 2 * s->n);
+    if (p->state_kind == MAVI_STATE_SECOND_LAW && vel) {
+        s->vel = (double*)malloc(sizeof(double) * 2 * s->n);
+        memcpy(s->vel, vel, sizeof(double) * 2 * s->n);
+    }
+    s->forces = (double*)calloc(2 * s->n, sizeof(double));
+    if (p->state_kind == MAVI_STATE_RINGS) {
+        s->num_rings = p->rings.num_rings;
+        s->nmax = p->rings.nmax;
+        s->types = (int32_t*)malloc(sizeof(int32_t) * s->num_rings);
+        for (int64_t r = 0; r < s->num_rings; r++) s->types[r] = ring_types ? ring_types[r] : 1;
+        s->pol = (double*)malloc(sizeof(double) * s->num_rings);
+        memcpy(s->pol, pol, sizeof(double) * s->num_rings);
+        s->cont_pos = (double*)calloc(2 * s->n, sizeof(double));
+        s->areas = (double*)calloc(s->num_rings, sizeof(double));
+        /* FixRingsIds p_ids (src/rings/states.jl:46-62) */
+        s->pids = (int64_t*)malloc(sizeof(int64_t) * s->n);
+        s->npids = 0;
+        for (int64_t r = 0; r < s->num_rings; r++)
+            for (int32_t i = 0; i < ring_n(s, r); i++) s->pids[s->npids++] = r * s->nmax + i;
+    } else {
+        if (p->state_kind == MAVI_STATE_SELF_PROPELLED) {
+            s->pol = (double*)malloc(sizeof(double) * s->n);
+            memcpy(s->pol, pol, sizeof(double) * s->n);
+        }
+        s->pids = (int64_t*)malloc(sizeof(int64_t) * s->n);
+        for (int64_t i = 0; i < s->n; i++) s->pids[i] = i;
+        s->npids = s->n;
+    }
+    *status = MAVI_OK;
+    if (outside_space(s)) { *status = MAVI_ERR_OUTSIDE_SPACE; }
+    s->nthreads = 1;
+    oracle_set_threads(s, nthreads);
+    if (p->chunk_cols > 0 && p->chunk_rows > 0) {
+        /* get_chunks (src/systems.jl:14-28) + Chunks (src/chunks.jl:26-40) */
+        s->has_chunks = 1;
+        s->rows = p->chunk_rows; s->cols = p->chunk_cols;
+        bbox_of(p, &s->bb_len, &s->bb_h, &s->bb_blx, &s->bb_bly);
+        s->chunk_l = s->bb_len / s->cols;
+        s->chunk_h = s->bb_h / s->rows;
+        double pr = particle_radius_of(p);
+        double nc = (ceil(0.5 * s->chunk_l / pr) + 1) * ((ceil(0.5 * s->chunk_h / pr) + 1));
+        s->cap = (int32_t)ceil(nc * 2);
+        int64_t nch = (int64_t)s->rows * s->cols;
+        s->chunk_particles = (int32_t*)malloc(sizeof(int32_t) * nch * s->cap);
+        s->num_in_chunk = (int32_t*)calloc(nch, sizeof(int32_t));
+        s->nbr = (int32_t*)calloc(nch * 4, sizeof(int32_t));
+        s->nbr_cnt = (int32_t*)calloc(nch, sizeof(int32_t));
+        int32_t st = build_neighbors(s, p->spaces[0].wall == MAVI_WALL_PERIODIC);
+        if (st && *status == MAVI_OK) *status = st;
+        if (*status == MAVI_OK) {
+            st = oracle_update_chunks(s);
+            if (st) *status = st;
+        }
+    }
+    return s;
+}
+
+int32_t oracle_set_threads(OracleSys* s, int32_t nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    free(s->slices);
+    s->slices = NULL;
+    s->nthreads = nthreads;
+    if (nthreads > 1) s->slices = (double*)calloc((size_t)(nthreads - 1) * 2 * s->n, sizeof(double));
+    return MAVI_OK;
+}
+
+void oracle_destroy(OracleSys* s) {
+    if (!s) return;
+    free(s->pos); free(s->vel); free(s->pol); free(s->types); free(s->forces); free(s->slices);
+    free(s->pids); free(s->chunk_particles); free(s->num_in_chunk); free(s->nbr); free(s->nbr_cnt);
+    free(s->cont_pos); free(s->areas);
+    free(s);
+}
+
+int32_t oracle_chunk_geometry(OracleSys* s, int32_t* rows, int32_t* cols, int32_t* cap) {
+    *rows = s->rows; *cols = s->cols; *cap = s->cap;
+    return MAVI_OK;
+}
+
+int32_t oracle_get_chunks(OracleSys* s, int32_t* num_in_chunk, int32_t* chunk_particles) {
+    if (!s->has_chunks) return MAVI_ERR_INVALID_ARG;
+    int64_t nch = (int64_t)s->rows * s->cols;
+    memcpy(num_in_chunk, s->num_in_chunk, sizeof(int32_t) * nch);
+    for (int64_t c = 0; c < nch; c++)
+        for (int32_t k = 0; k < s->cap; k++)
+            chunk_particles[c * s->cap + k] = (k < s->num_in_chunk[c]) ? s->chunk_particles[c * s->cap + k] : -1;
+    return MAVI_OK;
+}
+
+int32_t oracle_get_neighbors(OracleSys* s, int32_t* counts, int32_t* nbr) {
+    if (!s->has_chunks) return MAVI_ERR_INVALID_ARG;
+    int64_t nch = (int64_t)s->rows * s->cols;
+    memcpy(counts, s->nbr_cnt, sizeof(int32_t) * nch);
+    memcpy(nbr, s->nbr, sizeof(int32_t) * nch * 4);
+    return MAVI_OK;
+}
+
+int32_t oracle_get_state(OracleSys* s, double* pos, double* vel, double* pol) {
+    if (pos) memcpy(pos, s->pos, sizeof(double) * 2 * s->n);
+    if (vel && s->vel) memcpy(vel, s->vel, sizeof(double) * 2 * s->n);
+    if (pol && s->pol) {
+        int64_t np = (s->p.state_kind == MAVI_STATE_RINGS) ? s->num_rings : s->n;
+        memcpy(pol, s->pol, sizeof(double) * np);
+    }
+    return MAVI_OK;
+}
+
+int32_t oracle_set_state(OracleSys* s, const double* pos, const double* vel, const double* pol) {
+    if (pos) memcpy(s->pos, pos, sizeof(double) * 2 * s->n);
+    if (vel && s->vel) memcpy(s->vel, vel, sizeof(double) * 2 * s->n);
+    if (pol && s->pol) {
+        int64_t np = (s->p.state_kind == MAVI_STATE_RINGS) ? s->num_rings : s->n;
+        memcpy(s->pol, pol, sizeof(double) * np);
+    }
+    return MAVI_OK;
+}
+
+int32_t oracle_get_time(OracleSys* s, int64_t* num_steps, double* time) {
+    *num_steps = s->num_steps; *time = s->time;
+    return MAVI_OK;
+}
+
+int32_t oracle_get_areas(OracleSys* s, double* areas) {
+    if (!s->areas) return MAVI_ERR_INVALID_ARG;
+    memcpy(areas, s->areas, sizeof(double) * s->num_rings);
+    return MAVI_OK;
+}
+
+/* sizeof of the shared ABI structs as this C compiler lays them out, so tests
+ * can check the Python ctypes mirror byte for byte. */
+int32_t oracle_struct_sizes(int64_t* out) {
+    out[0] = (int64_t)sizeof(MaviSpace);
+    out[1] = (int64_t)sizeof(MaviRingsCfg);
+    out[2] = (int64_t)sizeof(MaviDynamicCfg);
+    out[3] = (int64_t)sizeof(MaviReplicaParams);
+    out[4] = (int64_t)sizeof(MaviOptions);
+    out[5] = (int64_t)sizeof(MaviStats);
+    out[6] = (int64_t)sizeof(MaviProfile);
+    return 7;
+}

@@ -1,0 +1,214 @@
+"""ctypes wrapper of the oracle library — TEST INFRASTRUCTURE ONLY.
+
+The oracle is the CPU FP64 restatement of Mavi.jl's step loop
+(oracle/mavi_oracle.c). Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg use it, as the checker; the product (libmavi_cuda.so and the
+mavi_gb300 package) never imports or calls it.
+
+It consumes the same MaviReplicaParams struct as the CUDA library, so one
+parameter block drives both sides of every parity test.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+
+SEQUENTIAL = 0
+THREADED = 1
+ALL_PAIRS = 2
+
+_lib = None
+
+
+def _load_lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_oracle_build", HERE / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    path = mod.build()
+    lib = C.CDLL(str(path))
+    from mavi_gb300 import abi
+    dp, ip, lp = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+    vp = C.c_void_p
+    sig = {
+        "oracle_create": (vp, [C.POINTER(abi.MaviReplicaParams), dp, dp, dp, ip, C.c_int32, ip]),
+        "oracle_destroy": (None, [vp]),
+        "oracle_set_threads": (C.c_int32, [vp, C.c_int32]),
+        "oracle_update_chunks": (C.c_int32, [vp]),
+        "oracle_chunk_geometry": (C.c_int32, [vp, ip, ip, ip]),
+        "oracle_get_chunks": (C.c_int32, [vp, ip, ip]),
+        "oracle_get_neighbors": (C.c_int32, [vp, ip, ip]),
+        "oracle_calc_forces": (C.c_int32, [vp, C.c_int32, C.c_int32, dp]),
+        "oracle_noise_count": (C.c_int64, [vp]),
+        "oracle_step": (C.c_int32, [vp, C.c_int64, C.c_int32, dp]),
+        "oracle_get_state": (C.c_int32, [vp, dp, dp, dp]),
+        "oracle_set_state": (C.c_int32, [vp, dp, dp, dp]),
+        "oracle_energies": (C.c_int32, [vp, C.c_int32, dp, dp]),
+        "oracle_get_time": (C.c_int32, [vp, lp, dp]),
+        "oracle_get_areas": (C.c_int32, [vp, dp]),
+        "oracle_count_pairs": (C.c_int64, [vp]),
+        "oracle_julia_div": (C.c_double, [C.c_double, C.c_double]),
+        "oracle_chunk_of": (C.c_int32, [vp, C.c_double, C.c_double, lp, lp]),
+        "oracle_struct_sizes": (C.c_int32, [lp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OracleError(RuntimeError):
+    def __init__(self, status, what):
+        super().__init__(f"oracle {what}: status {status}")
+        self.status = status
+
+
+class OracleSystem:
+    """One replica (a Julia ``System``) on the CPU oracle."""
+
+    def __init__(self, params, pos, vel=None, pol=None, types=None, nthreads: int = 1):
+        self.lib = _load_lib()
+        self.params = params
+        self.n = int(params.num_particles)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        pol = None if pol is None else np.ascontiguousarray(pol, dtype=np.float64).reshape(-1)
+        self.types = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
+        st = C.c_int32()
+        self.h = self.lib.oracle_create(C.byref(params), _dp(pos), _dp(vel), _dp(pol),
+                                        None if self.types is None else self.types.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        int(nthreads), C.byref(st))
+        self.status = st.value
+        self.has_vel = vel is not None
+        self.npol = 0 if pol is None else pol.size
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st, what):
+        if st != 0:
+            raise OracleError(st, what)
+
+    def set_threads(self, n: int):
+        self.lib.oracle_set_threads(self.h, int(n))
+
+    def update_chunks(self):
+        return self.lib.oracle_update_chunks(self.h)
+
+    def chunk_geometry(self):
+        r, c, k = C.c_int32(), C.c_int32(), C.c_int32()
+        self.lib.oracle_chunk_geometry(self.h, C.byref(r), C.byref(c), C.byref(k))
+        return r.value, c.value, k.value
+
+    def chunks(self):
+        """Reference layout: (num_in_chunk[rows, cols], chunk_particles[cap, rows, cols]), 0-based ids."""
+        r, c, k = self.chunk_geometry()
+        counts = np.zeros(r * c, dtype=np.int32)
+        members = np.zeros(r * c * k, dtype=np.int32)
+        self._ck(self.lib.oracle_get_chunks(self.h, counts.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            members.ctypes.data_as(C.POINTER(C.c_int32))), "get_chunks")
+        return counts.reshape(c, r).T.copy(), members.reshape(c, r, k).transpose(2, 1, 0).copy()
+
+    def neighbors(self):
+        r, c, _ = self.chunk_geometry()
+        cnt = np.zeros(r * c, dtype=np.int32)
+        nb = np.zeros(r * c * 4, dtype=np.int32)
+        self._ck(self.lib.oracle_get_neighbors(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               nb.ctypes.data_as(C.POINTER(C.c_int32))), "get_neighbors")
+        return cnt, nb.reshape(r * c, 4)
+
+    def forces(self, mode=SEQUENTIAL, include_walls=False):
+        out = np.zeros(2 * self.n)
+        self._ck(self.lib.oracle_calc_forces(self.h, mode, 1 if include_walls else 0, _dp(out)), "calc_forces")
+        return out.reshape(-1, 2)
+
+    def noise_count(self) -> int:
+        return int(self.lib.oracle_noise_count(self.h))
+
+    def step(self, nsteps: int = 1, mode=SEQUENTIAL, noise=None):
+        noise = None if noise is None else np.ascontiguousarray(noise, dtype=np.float64).reshape(-1)
+        st = self.lib.oracle_step(self.h, int(nsteps), mode, _dp(noise))
+        self._ck(st, "step")
+
+    def state(self):
+        pos = np.zeros(2 * self.n)
+        vel = np.zeros(2 * self.n) if self.has_vel else None
+        pol = np.zeros(self.npol) if self.npol else None
+        self.lib.oracle_get_state(self.h, _dp(pos), _dp(vel), _dp(pol))
+        return pos.reshape(-1, 2), (None if vel is None else vel.reshape(-1, 2)), pol
+
+    def set_state(self, pos, vel=None, pol=None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        pol = None if pol is None else np.ascontiguousarray(pol, dtype=np.float64).reshape(-1)
+        self.lib.oracle_set_state(self.h, _dp(pos), _dp(vel), _dp(pol))
+
+    def energies(self, pe_mode=0):
+        ke, pe = C.c_double(), C.c_double()
+        self._ck(self.lib.oracle_energies(self.h, pe_mode, C.byref(ke), C.byref(pe)), "energies")
+        return ke.value, pe.value
+
+    def time(self):
+        n, t = C.c_int64(), C.c_double()
+        self.lib.oracle_get_time(self.h, C.byref(n), C.byref(t))
+        return n.value, t.value
+
+    def areas(self, num_rings):
+        a = np.zeros(num_rings)
+        self._ck(self.lib.oracle_get_areas(self.h, _dp(a)), "areas")
+        return a
+
+    def count_pairs(self) -> int:
+        return int(self.lib.oracle_count_pairs(self.h))
+
+    def chunk_of(self, x, y):
+        r, c = C.c_int64(), C.c_int64()
+        st = self.lib.oracle_chunk_of(self.h, float(x), float(y), C.byref(r), C.byref(c))
+        return st, r.value, c.value
+
+
+def julia_div(x: float, y: float) -> float:
+    return _load_lib().oracle_julia_div(float(x), float(y))
+
+
+def struct_sizes():
+    out = (C.c_int64 * 16)()
+    n = _load_lib().oracle_struct_sizes(out)
+    names = ["MaviSpace", "MaviRingsCfg", "MaviDynamicCfg", "MaviReplicaParams", "MaviOptions", "MaviStats",
+             "MaviProfile"]
+    return {names[k]: out[k] for k in range(n)}
+
+
+def from_system(system, nthreads: int = 1, step_kind=None) -> OracleSystem:
+    """An oracle replica with the same parameters and state as a mavi_gb300 System."""
+    from mavi_gb300 import abi
+    from mavi_gb300.system import get_step_function
+    p = abi.MaviReplicaParams()
+    kind = step_kind if step_kind is not None else get_step_function(system).kind
+    system.fill_params(p, kind)
+    st = system.state
+    vel = getattr(st, "vel", None)
+    pol = st.pol_array()
+    types = st.types_array() if getattr(system, "is_rings", False) else None
+    return OracleSystem(p, st.pos, vel, pol, types, nthreads=nthreads)

@@ -1,0 +1,60 @@
+"""The C ABI: the library loads, exports every entry point the header
+declares, and the ctypes mirror matches the C struct layout. No GPU needed."""
+import ctypes as C
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    text = (ROOT / "include" / "mavi_cuda.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mavi_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_entry_point(lib):
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in include/mavi_cuda.h but not exported"
+
+
+def test_ctypes_signatures_cover_header(mg):
+    from mavi_gb300 import abi
+    assert set(header_functions()) == set(abi.SIGNATURES)
+
+
+def test_struct_layout_matches_c(mg, orc):
+    from mavi_gb300 import abi
+    sizes = orc.struct_sizes()
+    for name, size in sizes.items():
+        assert C.sizeof(abi.STRUCTS[name]) == size, name
+
+
+def test_status_strings_and_version(lib):
+    assert lib.mavi_abi_version() == 1
+    for st in range(10):
+        assert lib.mavi_status_string(st)
+    assert lib.mavi_status_string(0) == b"ok"
+
+
+def test_null_arguments_are_rejected_without_a_gpu(lib):
+    from mavi_gb300 import abi
+    h = C.c_void_p()
+    assert lib.mavi_create(None, 1, None, None, None, None, None, C.byref(h)) == abi.MAVI_ERR_INVALID_ARG
+    assert lib.mavi_step(None, 1) == abi.MAVI_ERR_INVALID_ARG
+    assert lib.mavi_destroy(None) == abi.MAVI_OK
+
+
+def test_missing_library_fails_loudly(mg, tmp_path):
+    from mavi_gb300 import abi
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        abi.load_library(tmp_path / "libmavi_cuda.so")
+
+
+def test_product_never_imports_the_oracle():
+    pkg = ROOT / "mavi.jl_gb300"
+    for p in list(pkg.rglob("*.py")) + list(pkg.rglob("*.cu")) + list(pkg.rglob("*.cuh")):
+        assert "oracle" not in p.read_text().lower().replace("oracle/", ""), p

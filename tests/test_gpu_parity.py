@@ -1,0 +1,217 @@
+"""Parity of the CUDA library (through its C ABI) with the oracle on the same
+seeded inputs. Chunk sets must be bit-exact; FP64 forces agree to 1e-12 of
+the RMS force (summation order differs); mixed-precision forces to 1e-5."""
+import numpy as np
+import pytest
+
+from helpers import lj_grid, soft_disks, lj_circle, self_propelled, rings_normal, rings_types, rel_force_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+def chunks_equal(sys_, ref):
+    c_gpu, m_gpu = sys_.chunks()
+    c_ref, m_ref = ref.chunks()
+    return np.array_equal(c_gpu, c_ref) and np.array_equal(m_gpu, m_ref)
+
+
+@pytest.mark.parametrize("wall", ["rigid", "periodic"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lj_grid_chunks_and_forces(mg, orc, wall, precision):
+    s = lj_grid(mg, 32, 32, wall=wall, chunks=(17, 17), precision=precision)
+    ref = orc.from_system(s)
+    assert chunks_equal(s, ref)
+    err = rel_force_err(s.calc_forces(), ref.forces())
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lj_trajectory_rigid(mg, orc, precision):
+    s = lj_grid(mg, 32, 32, wall="rigid", chunks=(17, 17), precision=precision)
+    ref = orc.from_system(s)
+    mg.run_system(s, num_steps=200)
+    ref.step(200)
+    p, v, _ = ref.state()
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert np.max(np.abs(s.state.pos - p)) < tol
+    assert np.max(np.abs(s.state.vel - v)) < tol * 10
+    assert s.time_info.num_steps == 200 and ref.time()[0] == 200
+    assert chunks_equal(s, ref) if precision == "fp64" else True
+    s.close()
+
+
+def test_lj_trajectory_periodic_chunks_bit_exact_after_steps(mg, orc):
+    s = lj_grid(mg, 24, 24, wall="periodic", speed=1.0)
+    ref = orc.from_system(s)
+    for _ in range(4):
+        mg.run_system(s, num_steps=50)
+        ref.step(50)
+        ref.set_state(s.state.pos, s.state.vel)   # same FP64 state on both sides
+        assert chunks_equal(s, ref)
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overdamped_soft_disks(mg, orc, precision):
+    s = soft_disks(mg, 4096, precision=precision)
+    ref = orc.from_system(s, step_kind=mg.overdamped_step.kind)
+    assert chunks_equal(s, ref)
+    err = rel_force_err(s.calc_forces(), ref.forces())
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+    mg.run_system(s, num_steps=50, step_func=mg.overdamped_step)
+    ref.step(50)
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert np.max(np.abs(s.state.pos - ref.state()[0])) < tol
+    s.close()
+
+
+@pytest.mark.parametrize("wall", ["rigid", "slippery"])
+def test_circle_walls(mg, orc, wall):
+    s = lj_circle(mg, 300, wall=wall)
+    ref = orc.from_system(s)
+    assert chunks_equal(s, ref)
+    mg.run_system(s, num_steps=100)
+    ref.step(100)
+    assert np.max(np.abs(s.state.pos - ref.state()[0])) < 1e-9
+    s.close()
+
+
+@pytest.mark.parametrize("kind", ["szabo", "rtp"])
+def test_self_propelled_injected_noise(mg, orc, kind):
+    s = self_propelled(mg, kind, 400)
+    step = mg.szabo_step if kind == "szabo" else mg.rtp_step
+    ref = orc.from_system(s)
+    n = s.handle.noise_count()
+    assert n == ref.noise_count()
+    rng = np.random.default_rng(11)
+    steps = 30
+    noise = rng.normal(size=n * steps) if kind == "szabo" else rng.random(n * steps)
+    s.run(steps, step, noise=noise)
+    ref.step(steps, noise=noise)
+    p, _, pol = ref.state()
+    assert np.max(np.abs(s.state.pos - p)) < 1e-9
+    assert np.max(np.abs(s.state.pol_angle - pol)) < 1e-9
+    s.close()
+
+
+@pytest.mark.parametrize("factory", ["normal", "types"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rings(mg, orc, factory, precision):
+    s = rings_normal(mg, precision=precision) if factory == "normal" else rings_types(mg, precision=precision)
+    ref = orc.from_system(s)
+    assert chunks_equal(s, ref)
+    err = rel_force_err(s.calc_forces(), ref.forces())
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+    n = s.handle.noise_count()
+    steps = 100
+    noise = np.random.default_rng(3).normal(size=n * steps)
+    s.run(steps, noise=noise)
+    ref.step(steps, noise=noise)
+    p, _, pol = ref.state()
+    active = np.array([k % s.state.nmax < s.state.ring_num_particles(k // s.state.nmax)
+                       for k in range(s.num_slots)])
+    tol = 1e-8 if precision == "fp64" else 1e-3
+    assert np.max(np.abs(s.state.pos[active] - p[active])) < tol
+    assert np.max(np.abs(s.state.pol - pol)) < tol
+    s.close()
+
+
+def test_rings_bending_forces(mg, orc):
+    s = rings_normal(mg, k_bend=2.0)
+    ref = orc.from_system(s)
+    assert rel_force_err(s.calc_forces(), ref.forces()) < FP64_TOL
+    s.close()
+
+
+def test_all_pairs_without_chunks(mg, orc):
+    s = lj_grid(mg, 10, 10, wall="rigid", chunks=False)
+    ref = orc.from_system(s)
+    assert rel_force_err(s.calc_forces(), ref.forces(orc.ALL_PAIRS)) < FP64_TOL
+    mg.run_system(s, num_steps=50)
+    ref.step(50)
+    assert np.max(np.abs(s.state.pos - ref.state()[0])) < 1e-10
+    s.close()
+
+
+def test_energies(mg, orc):
+    s = lj_grid(mg, 20, 20, wall="periodic")
+    ref = orc.from_system(s)
+    ke, pe = s.energies(mg.abi.MAVI_PE_STENCIL)
+    rke, rpe = ref.energies(mg.abi.MAVI_PE_STENCIL)
+    assert ke == pytest.approx(rke, rel=1e-13) and pe == pytest.approx(rpe, rel=1e-12)
+    ke2, pe2 = s.energies(mg.abi.MAVI_PE_ALL_PAIRS)
+    rke2, rpe2 = ref.energies(mg.abi.MAVI_PE_ALL_PAIRS)
+    assert pe2 == pytest.approx(rpe2, rel=1e-12)
+    s.close()
+
+
+def test_batch_equals_single_replicas_bitwise(mg):
+    singles = [lj_grid(mg, 12 + 2 * k, 12 + k, wall=("rigid" if k % 2 else "periodic"), seed=k) for k in range(4)]
+    batch_sys = [lj_grid(mg, 12 + 2 * k, 12 + k, wall=("rigid" if k % 2 else "periodic"), seed=k) for k in range(4)]
+    for s in singles:
+        mg.run_system(s, num_steps=40)
+    b = mg.SystemBatch(batch_sys)
+    b.run(40)
+    for s, t in zip(singles, batch_sys):
+        assert np.array_equal(s.state.pos, t.state.pos)
+        assert np.array_equal(s.state.vel, t.state.vel)
+        s.close()
+    b.close()
+
+
+def test_deterministic_and_graph_equals_eager(mg):
+    a = lj_grid(mg, 20, 20, wall="periodic", use_graph=True)
+    b = lj_grid(mg, 20, 20, wall="periodic", use_graph=True)
+    c = lj_grid(mg, 20, 20, wall="periodic", use_graph=False)
+    for s in (a, b, c):
+        mg.run_system(s, num_steps=100)
+    assert np.array_equal(a.state.pos, b.state.pos)
+    assert np.array_equal(a.state.pos, c.state.pos)
+    for s in (a, b, c):
+        s.close()
+
+
+def test_out_of_grid_reports_error(mg):
+    """A particle more than one chunk outside the grid is a BoundsError in the
+    reference (src/chunks.jl:144-146); here the status is returned, no trap."""
+    s = lj_grid(mg, 8, 8, wall="rigid", chunks=(4, 4))
+    s.calc_forces()
+    s.state.pos[5] = (-20.0, 3.0)
+    with pytest.raises(mg.MaviError) as e:
+        s.upload()
+    assert e.value.status == mg.abi.MAVI_ERR_OUT_OF_GRID
+    s.state.pos[5] = (1.0, 1.0)
+    s.upload()                      # the handle stays usable
+    s.calc_forces()
+    s.close()
+
+
+def test_particle_escaping_during_steps_reports_error(mg):
+    s = lj_grid(mg, 8, 8, wall="periodic", chunks=(4, 4))
+    s.calc_forces()
+    s.state.vel[3] = (1e6, 0.0)     # crosses several chunks in one step
+    s.upload()
+    with pytest.raises(mg.MaviError) as e:
+        mg.run_system(s, num_steps=2)
+    assert e.value.status == mg.abi.MAVI_ERR_OUT_OF_GRID
+    s.close()
+
+
+def test_outside_space_rejected_at_creation(mg):
+    s = lj_grid(mg, 8, 8, wall="rigid", chunks=(4, 4))
+    s.state.pos[0] = (-5.0, 1.0)
+    with pytest.raises(mg.MaviError) as e:
+        s.calc_forces()
+    assert e.value.status == mg.abi.MAVI_ERR_OUTSIDE_SPACE
+
+
+def test_chunk_overflow_reports_error(mg):
+    s = soft_disks(mg, 256, phi=0.3)
+    s.state.pos[:60] = s.state.pos[0]
+    with pytest.raises(mg.MaviError) as e:
+        s.calc_forces()
+    assert e.value.status == mg.abi.MAVI_ERR_CHUNK_OVERFLOW
