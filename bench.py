@@ -113,7 +113,7 @@ class Clocks:
 
 
 def launches_per_step(step_kind, abi):
-    rebin = 5   # scan reduce, scan tiles, scan apply, scatter, per-chunk order + permutation
+    rebin = 3   # scan, scatter, deterministic per-chunk order + permutation
     body = {abi.MAVI_STEP_NEWTON: 2, abi.MAVI_STEP_OVERDAMPED: 1, abi.MAVI_STEP_SZABO: 1, abi.MAVI_STEP_RTP: 1,
             abi.MAVI_STEP_RINGS: 3}[step_kind]
     return rebin + body
@@ -161,7 +161,7 @@ def e2e_form(mg, system, step_func, K, torch):
     n = system.num_slots
     pos_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     pos_h.copy_(torch.from_numpy(system.state.pos))
-    has_vel = system.state.kind == mg.abi.MAVI_STATE_SECOND_LAW
+    has_vel = system.state.kind == mg.abi.MAVI_STATE_SECOND_LAW and system.state.vel is not None
     vel_h = None
     if has_vel:
         vel_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
@@ -184,26 +184,29 @@ def e2e_form(mg, system, step_func, K, torch):
     return {"seconds": dt, "h2d": bi, "d2h": bo}
 
 
-def algorithmic_bytes(kind, precision, step_kind, abi):
-    """Algorithmic HBM bytes per particle of one launch of each kernel kind
-    (unique data each launch must move once)."""
+def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
+    """Algorithmic HBM bytes per particle of one launch of each kernel kind:
+    the unique data the launch must read and write once (neighbour reads hit
+    in L1/L2 and are not counted)."""
     mixed = precision == "mixed"
+    off = 8 if mixed else 0          # int2 fixed-point chunk offset
+    vel = 16 if has_vel else 0
     if kind == "force":
-        # own position (+FP32 offset), uid, replica, chunk, chunk starts (~1/particle);
-        # writes: position, uid, replica, new chunk, rank (+vel for Verlet pass 2)
-        own = 16 + (8 if mixed else 0) + 4 + 4 + 4 + 4
-        out = 16 + 4 + 4 + 4 + 4
         if step_kind == abi.MAVI_STEP_NEWTON:
-            # pass 1: read x, v; write x', F(t); pass 2: read x', v, F(t); write x, v, ...
-            own += 16 + 16
-            out += 16 + (8 if mixed else 16)
-        return own + out
+            # pass 1: r x, v, uid, rep, cell, (off) ; w x', F(t), (off')
+            p1 = (16 + 16 + 4 + 4 + 4 + off) + (16 + (8 if mixed else 16) + off)
+            # pass 2: r x', v, F(t), (off') ; w x, v, uid, rep, cell, rank, (off)
+            p2 = (16 + 16 + (8 if mixed else 16) + 4 + 4 + 4 + off) + (16 + 16 + 4 + 4 + 4 + 4 + off)
+            return p1 + p2
+        # final pass: r x, (v), uid, rep, cell, (off); w x, (v), uid, rep, cell, rank, (off)
+        return (16 + vel + 4 + 4 + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
     if kind == "bin_sort":
-        return (16 + 4 + 4 + 4) * 2 + 4 + (8 if mixed else 0) + 4
+        # r src_of, cell, uid, x, (v), rep, (off); w x, (v), uid, rep, cell, slot_of, (off)
+        return (4 + 4 + 4 + 16 + vel + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
     if kind == "bin_scatter":
-        return 4 + 4 + 4 + 4
+        return 4 + 4 + 4          # r cell, rank; w src_of
     if kind == "bin_scan":
-        return 4 * 3
+        return 0                  # per chunk, not per particle (counted in the chunk term)
     return 0
 
 
@@ -212,11 +215,11 @@ def algorithmic_bytes(kind, precision, step_kind, abi):
 FLOPS_PER_PAIR = {0: 16, 1: 23, 2: 14, 3: 23, 4: 16}
 
 
-def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind):
+def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind, has_vel):
     kinds = meas["kinds"]
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     avg_ms = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1)
-    bpp = algorithmic_bytes(dom, precision, step_kind, abi)
+    bpp = algorithmic_bytes(dom, precision, step_kind, abi, has_vel)
     traffic_bytes = bpp * n
     achieved = traffic_bytes / (avg_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -380,8 +383,9 @@ def main():
         v = world * n * K / (m["total_ms"] * 1e-3)
         dyn_kind = abi.MaviReplicaParams()
         results[precision]["system"].fill_params(dyn_kind, results[precision]["step"].kind)
+        st = results[precision]["system"].state
         rf = roofline(m, n, precision, results[precision]["step"].kind, abi, peaks, stats.candidate_pairs,
-                      fma[precision], dyn_kind.dyn.kind)
+                      fma[precision], dyn_kind.dyn.kind, getattr(st, "vel", None) is not None)
         line_forms[precision] = {"value": v, "ms_per_step": m["total_ms"] / K, "roofline": rf,
                                  "kernels_ms_per_step": {k: d["ms"] / K for k, d in m["kinds"].items()},
                                  "gpu_launches": m["launches_per_step"] * K}

@@ -190,7 +190,8 @@ typedef struct MaviOptions {
     int32_t device;          /* CUDA device ordinal                                */
     int32_t use_graph;       /* capture the step in a CUDA graph when nonzero      */
     int32_t block_size;      /* threads per block for particle kernels (0 = tuned) */
-    int32_t _pad0;
+    int32_t gather_mode;     /* pair gather: 0 = warp-staged shared-memory window,
+                                1 = per-thread global loads (same results)          */
 } MaviOptions;
 
 /* Work counters of the last force pass (for roofline accounting). */

@@ -65,6 +65,13 @@ MAVI_MAX_SPACES = 4
 MAVI_MAX_LINES = 16
 MAVI_MAX_TYPES = 4
 
+MAVI_KERNEL_BIN_COUNT = 0
+MAVI_KERNEL_BIN_SCAN = 1
+MAVI_KERNEL_BIN_SCATTER = 2
+MAVI_KERNEL_BIN_SORT = 3
+MAVI_KERNEL_FORCE = 4
+MAVI_KERNEL_UPDATE = 5
+MAVI_KERNEL_OTHER = 6
 MAVI_KERNEL_NAMES = ("bin_count", "bin_scan", "bin_scatter", "bin_sort", "force", "update", "other")
 MAVI_NUM_KERNEL_KINDS = 7
 
@@ -123,7 +130,7 @@ class MaviReplicaParams(C.Structure):
 class MaviOptions(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("noise_mode", C.c_int32), ("seed", C.c_uint64),
-        ("device", C.c_int32), ("use_graph", C.c_int32), ("block_size", C.c_int32), ("_pad0", C.c_int32),
+        ("device", C.c_int32), ("use_graph", C.c_int32), ("block_size", C.c_int32), ("gather_mode", C.c_int32),
     ]
 
 

@@ -281,6 +281,7 @@ class CUDADevice:
     use_graph: bool = True
     noise: str = "device"
     seed: int = 0
+    gather: str = "staged"
 
     def options(self) -> abi.MaviOptions:
         o = abi.MaviOptions()
@@ -289,6 +290,7 @@ class CUDADevice:
         o.seed = int(self.seed) & ((1 << 64) - 1)
         o.device = int(self.device)
         o.use_graph = 1 if self.use_graph else 0
+        o.gather_mode = {"staged": 0, "global": 1}[self.gather]
         return o
 
 

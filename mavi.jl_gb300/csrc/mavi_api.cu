@@ -19,26 +19,28 @@ using namespace mavi;
 static void launch_count(MaviSystem* s) {
     record_begin(s, MAVI_KERNEL_BIN_COUNT);
     cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
-    k_count<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+    cudaMemsetAsync(s->C.tile_sum, 0, sizeof(int32_t) * s->ntiles, s->stream);
+    if (s->prec == MAVI_PREC_FP64) count_fp64(s, 0);
+    else count_mixed(s, 0);
     record_end(s, MAVI_KERNEL_BIN_COUNT);
 }
 
 // update_chunks! (src/chunks.jl:150-161): chunk lists from the histogram of the
 // *_out state: scan -> scatter -> per-chunk order + permutation into *_cur.
+// The scan clears the counts and the scatter the tile sums, so the histogram
+// of the next step starts from zero without memset launches.
 static void launch_rebin(MaviSystem* s, bool advance) {
     if (!s->counts_valid) launch_count(s);
     record_begin(s, MAVI_KERNEL_BIN_SCAN);
-    k_scan_reduce<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->tile_sum);
-    k_scan_tiles<<<1, 1024, 0, s->stream>>>(s->tile_sum, s->ntiles, s->C.start, s->Ctot, s->C.d_step, advance ? 1 : 0);
-    k_scan_apply<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->tile_sum, s->C.start);
+    k_scan<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->C.tile_sum, s->C.start,
+                                                               s->C.d_step, advance ? 1 : 0);
     record_end(s, MAVI_KERNEL_BIN_SCAN);
     record_begin(s, MAVI_KERNEL_BIN_SCATTER);
-    k_scatter<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+    k_scatter<<<nblocks(std::max(s->M, s->ntiles)), kBlock, 0, s->stream>>>(s->C);
     record_end(s, MAVI_KERNEL_BIN_SCATTER);
     record_begin(s, MAVI_KERNEL_BIN_SORT);
     if (s->prec == MAVI_PREC_FP64) sort_permute_fp64(s);
     else sort_permute_mixed(s);
-    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
     record_end(s, MAVI_KERNEL_BIN_SORT);
     s->counts_valid = false;
 }
@@ -46,13 +48,13 @@ static void launch_rebin(MaviSystem* s, bool advance) {
 // One whole step; its last kernel leaves the histogram for the next step.
 static void launch_step(MaviSystem* s) {
     if (s->profiling) {
-        cudaEventRecord(s->ev.step_a, s->stream);
+        cudaEventRecordWithFlags(s->ev.step_a, s->stream, cudaEventRecordExternal);
         s->ev.step_used = 1;
     }
     launch_rebin(s, true);
     if (s->prec == MAVI_PREC_FP64) step_body_fp64(s);
     else step_body_mixed(s);
-    if (s->profiling) cudaEventRecord(s->ev.step_b, s->stream);
+    if (s->profiling) cudaEventRecordWithFlags(s->ev.step_b, s->stream, cudaEventRecordExternal);
     s->counts_valid = true;
 }
 
@@ -241,6 +243,83 @@ static void pack_pair_params(const MaviDynamicCfg& d, DevRep& R) {
     for (int k = 0; k < 8; k++) R.pf[k] = (float)R.pd[k];
 }
 
+
+// Fixed-point geometry of the mixed form: unit u = max(chunk_l, chunk_h)/2^28,
+// chunk and box sizes in units, and when the minimum image may be skipped for
+// neighbours that do not wrap (|dr| < 2 chunks + drift <= L/2 needs >= 6
+// chunks per side). Walls run for edge-chunk particles only when every space is
+// a rigid or periodic rectangle equal to the chunk bounding box and the
+// particle radius is below a chunk.
+static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
+    double u = std::max(R.chunk_l, R.chunk_h) / (double)(1 << kFixBits);
+    R.inv_u = 1.0 / u;
+    R.u_f = (float)u;
+    R.u2_f = (float)(u * u);
+    R.sx_u = std::llround(R.chunk_l / u);
+    R.sy_u = std::llround(R.chunk_h / u);
+    R.bx_u = R.sx_u * R.cols;
+    R.by_u = R.sy_u * R.rows;
+    R.half_bx_u = R.bx_u / 2;
+    R.half_by_u = R.by_u / 2;
+    R.sx_i = (int32_t)R.sx_u;
+    R.sy_i = (int32_t)R.sy_u;
+    R.half_sx_i = R.sx_i / 2;
+    R.half_sy_i = R.sy_i / 2;
+    R.cx0 = R.bb_blx + 0.5 * R.chunk_l;
+    R.cy0 = R.bb_bly + R.bb_h - 0.5 * R.chunk_h;
+    // the minimum image only matters for |dr| > L/2 with dr <= ~2 chunks,
+    // i.e. grids of < 6 chunks per side, whose box fits int32 units
+    const long long lim = (1ll << 31) - 1;
+    R.bx_i = (int32_t)std::min(R.bx_u, lim);
+    R.by_i = (int32_t)std::min(R.by_u, lim);
+    R.half_bx_i = (int32_t)std::min(R.half_bx_u, lim);
+    R.half_by_i = (int32_t)std::min(R.half_by_u, lim);
+    R.mi_small = (!R.has_chunks || R.rows < 6 || R.cols < 6) ? 1 : 0;
+    bool edge_only = R.has_chunks && p.num_spaces == 1 && R.radius < std::min(R.chunk_l, R.chunk_h);
+    const MaviSpace& sp = p.spaces[0];
+    edge_only = edge_only && sp.geometry == MAVI_GEOM_RECTANGLE &&
+                (sp.wall == MAVI_WALL_RIGID || sp.wall == MAVI_WALL_PERIODIC) && sp.length == R.bb_len &&
+                sp.height == R.bb_h && sp.bl_x == R.bb_blx && sp.bl_y == R.bb_bly;
+    R.walls_edge_only = edge_only ? 1 : 0;
+}
+
+// Fixed-point pair constants (units of the replica) per (type, type).
+static void fill_fix_pairs(const MaviReplicaParams& p, const DevRep& R, FixPair* out) {
+    double inv_u = R.inv_u;
+    auto sq = [&](double len) { double v = len * inv_u; return (unsigned long long)std::llround(v * v); };
+    for (int t = 0; t < MAVI_MAX_TYPES * MAVI_MAX_TYPES; t++) out[t] = FixPair{};
+    const MaviDynamicCfg& d = p.dyn;
+    FixPair f{};
+    switch (d.kind) {
+    case MAVI_DYN_HARM_TRUNC:
+        f.cut2 = sq(d.dist_max); f.eq2 = (long long)sq(d.dist_eq); f.eq = (float)(d.dist_eq * inv_u);
+        f.k_rep = (float)d.k_rep; f.k_atr = (float)d.k_atr;
+        out[0] = f;
+        break;
+    case MAVI_DYN_SZABO:
+        f.cut2 = sq(d.r_max); f.eq2 = (long long)sq(d.r_eq); f.eq = (float)(d.r_eq * inv_u);
+        f.k_rep = (float)(d.k_rep / (d.r_max - d.r_eq)); f.k_atr = (float)(d.k_adh / d.r_eq);
+        out[0] = f;
+        break;
+    case MAVI_DYN_RUN_TUMBLE:
+        f.cut2 = sq(std::pow(2.0, 1.0 / 6.0) * d.sigma);
+        out[0] = f;
+        break;
+    case MAVI_DYN_RINGS:
+        for (int a = 0; a < p.rings.num_types; a++)
+            for (int b = 0; b < p.rings.num_types; b++) {
+                FixPair g{};
+                g.cut2 = sq(p.rings.inter_dist_max[a][b]);
+                g.eq2 = (long long)sq(p.rings.inter_dist_eq[a][b]);
+                g.eq = (float)(p.rings.inter_dist_eq[a][b] * inv_u);
+                g.k_rep = (float)p.rings.inter_k_rep[a][b];
+                g.k_atr = (float)p.rings.inter_k_atr[a][b];
+                out[a * MAVI_MAX_TYPES + b] = g;
+            }
+        break;
+    }
+}
+
 static int check_device_error(MaviSystem* s) {
     DevError e{};
     CUDA_TRY(s, cudaMemcpyAsync(&e, s->C.err, sizeof(DevError), cudaMemcpyDeviceToHost, s->stream));
@@ -348,10 +427,21 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     s->dyn = p0.dyn.kind;
     s->step_kind = p0.step_kind;
     s->state_kind = p0.state_kind;
-    s->has_vel = s->state_kind == MAVI_STATE_SECOND_LAW;
+    // SecondLaw states carry velocities; the overdamped step may run on
+    // positions only (vel == NULL), which spares moving dead velocities.
+    s->has_vel = s->state_kind == MAVI_STATE_SECOND_LAW && vel != nullptr;
     s->has_pol = s->state_kind == MAVI_STATE_SELF_PROPELLED;
     s->is_rings = s->state_kind == MAVI_STATE_RINGS;
-    if (s->has_vel && !vel) { delete s; return MAVI_ERR_INVALID_ARG; }
+    if (s->state_kind == MAVI_STATE_SECOND_LAW && !vel && s->step_kind != MAVI_STEP_OVERDAMPED) {
+        delete s;
+        return MAVI_ERR_INVALID_ARG;
+    }
+    for (int r = 0; r < num_replicas && !s->has_vel; r++)
+        for (int k = 0; k < replicas[r].num_spaces; k++)
+            if (replicas[r].spaces[k].wall == MAVI_WALL_RIGID) {
+                delete s;
+                return MAVI_ERR_UNSUPPORTED;   // rigid walls reflect velocities
+            }
     if ((s->has_pol || s->is_rings) && !pol) { delete s; return MAVI_ERR_INVALID_ARG; }
 
     // per-replica layout
@@ -410,7 +500,10 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
             else R.has_walls = 1;
         }
         pack_pair_params(p.dyn, R);
+        set_fixed_point(p, R);
         R.mobility = p.dyn.mobility;
+        R.mdt = p.dyn.mobility * p.dt;
+        R.mdt_f = (float)R.mdt;
         R.vo = p.dyn.vo;
         R.relax_time = p.dyn.relax_time;
         R.rot_diff = p.dyn.rot_diff;
@@ -477,7 +570,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     ALLOC(C.pos_cur, M); ALLOC(C.pos_mid, M); ALLOC(C.pos_out, M);
     if (s->has_vel) { ALLOC(C.vel_cur, M); ALLOC(C.vel_out, M); }
     if (s->has_pol) { ALLOC(C.pol_cur, M); ALLOC(C.pol_out, M); }
-    if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.off_cur, M); ALLOC(C.off_mid, M); ALLOC(C.ff, M); }
+    if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.off_cur, M); ALLOC(C.off_mid, M); ALLOC(C.off_out, M); ALLOC(C.ff, M); }
     else { ALLOC(C.fd, M); }
     if (s->step_kind == MAVI_STEP_NEWTON) {
         if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.fold_f, M); } else { ALLOC(C.fold_d, M); }
@@ -486,13 +579,15 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.rank, M); ALLOC(C.src_of, M);
     ALLOC(C.slot_of, N);
     ALLOC(C.count, s->Ctot); ALLOC(C.start, s->Ctot + 1);
-    ALLOC(s->tile_sum, s->ntiles);
+    ALLOC(C.tile_sum, s->ntiles);
     int32_t* ring_types_d = nullptr;
     if (s->is_rings) { ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings); }
     DevRep* reps_d = nullptr;
     MaviSpace* spaces_d = nullptr;
     MaviRingsCfg* rcfg_d = nullptr;
+    FixPair* fix_d = nullptr;
     ALLOC(reps_d, s->R); ALLOC(spaces_d, (int64_t)s->R * MAVI_MAX_SPACES); ALLOC(rcfg_d, s->R);
+    ALLOC(fix_d, (int64_t)s->R * MAVI_MAX_TYPES * MAVI_MAX_TYPES);
     ALLOC(C.err, 1); ALLOC(C.d_step, 1);
     ALLOC(s->pos_user, N); ALLOC(s->f_user, N);
     if (s->has_vel) { ALLOC(s->vel_user, N); }
@@ -505,10 +600,13 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     C.reps = reps_d;
     C.spaces = spaces_d;
     C.rcfg = rcfg_d;
+    C.fix = fix_d;
     C.M = M;
     C.Ctot = s->Ctot;
+    C.ntiles = s->ntiles;
     C.noise = s->noise_cur;
     C.noise_mode = opt->noise_mode;
+    C.gather_mode = opt->gather_mode;
     C.num_reps = s->R;
     C.seed = opt->seed;
 
@@ -551,6 +649,10 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     CUDA_TRY(s, cudaMemcpyAsync(reps_d, s->reps_h.data(), sizeof(DevRep) * s->R, cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(spaces_d, spaces_h.data(), sizeof(MaviSpace) * spaces_h.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(rcfg_d, rcfg_h.data(), sizeof(MaviRingsCfg) * s->R, cudaMemcpyHostToDevice, s->stream));
+    std::vector<FixPair> fix_h((size_t)s->R * MAVI_MAX_TYPES * MAVI_MAX_TYPES);
+    for (int r = 0; r < s->R; r++) fill_fix_pairs(replicas[r], s->reps_h[r], fix_h.data() + (size_t)r * MAVI_MAX_TYPES * MAVI_MAX_TYPES);
+    CUDA_TRY(s, cudaMemcpyAsync(fix_d, fix_h.data(), sizeof(FixPair) * fix_h.size(), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(C.uid_out, uid_h.data(), sizeof(int32_t) * M, cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(C.rep_out, rep_h.data(), sizeof(int32_t) * M, cudaMemcpyHostToDevice, s->stream));
     if (s->is_rings) {

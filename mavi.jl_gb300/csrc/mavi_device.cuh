@@ -53,6 +53,21 @@ struct DevRep {
     double pd[8];          // pair-law parameters (double)
     float pf[8];           // same in float
     double mobility, vo, relax_time, rot_diff, tumble_rate;
+    // mixed form: fixed-point unit u = max(chunk_l, chunk_h) / 2^28
+    double inv_u;          // 1/u
+    float u_f, u2_f;       // u, u^2
+    long long sx_u, sy_u;  // chunk width / height in units
+    long long bx_u, by_u;  // box in units (cols*sx_u, rows*sy_u)
+    long long half_bx_u, half_by_u;
+    int32_t sx_i, sy_i;    // chunk width / height in units (int32 copies, < 2^29)
+    int32_t bx_i, by_i;    // box in units when it fits int32 (minimum image on small grids)
+    int32_t half_bx_i, half_by_i;
+    int32_t half_sx_i, half_sy_i;  // half chunk in units
+    double cx0, cy0;       // centre of chunk (row 0, col 0)
+    double mdt;            // mobility * dt
+    float mdt_f;
+    int32_t mi_small;      // grid too small to skip the minimum image for unwrapped neighbours
+    int32_t walls_edge_only; // every wall acts on the bounding rectangle only
 };
 
 // ---------------------------------------------------------------------------

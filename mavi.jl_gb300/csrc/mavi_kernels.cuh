@@ -5,25 +5,51 @@
 //    then chunk (column-major, as Julia's chunk arrays), then ascending user
 //    id inside a chunk — exactly the order of the reference's
 //    chunk_particles[:, row, col] lists (src/chunks.jl:144-146);
-//  * SoA arrays: positions double2, velocities double2, FP32 chunk-centre
-//    offsets float2 (mixed form), user id int32, replica int32;
+//  * SoA arrays: FP64 positions/velocities (double2), the user id and the
+//    replica (int32), and in the mixed form each particle's offset from its
+//    chunk centre in int32 fixed point (int2, 2^-28 chunk units);
 //  * chunks in CSR form: count[c], start[c] over all replicas' chunks.
 // A step reads the state in "previous order" (*_out arrays, written by the
-// last step together with each particle's new chunk and its rank inside it),
-// rebuilds the chunk lists (scan -> scatter -> per-chunk order + permutation
-// into *_cur arrays) and runs the fused force/update passes.
+// last step together with each particle's new chunk, its rank of arrival in
+// it and, in the mixed form, its new offset), rebuilds the chunk lists
+// (scan -> scatter -> deterministic per-chunk order + permutation into *_cur)
+// and runs the fused force/update passes.
+//
+// GB300 executes FP64 at ~1/70 of the FP32 rate, so the per-particle FP64
+// work outside the pair loop is kept to a few tens of operations: the
+// Julia-exact chunk index is found by verifying a guess with exactly-signed
+// FMA residuals, wall tests only run for particles in edge chunks, and the
+// mixed form's pair loop is integer + FP32 only.
 #pragma once
+
+#include <type_traits>
 
 #include "mavi_device.cuh"
 
 namespace mavi {
+
+constexpr int kFixBits = 28;                       // fixed-point offsets: chunk = 2^28 units
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
+constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
+
+// Fixed-point parameters of the pair laws of one (type, type) pair, in units
+// u = max(chunk_l, chunk_h) / 2^28 of the replica.
+struct FixPair {
+    unsigned long long cut2;   // squared cutoff (dist_max / r_max / WCA cutoff), units^2
+    long long eq2;             // squared equilibrium distance (dist_eq / r_eq), units^2
+    float eq;                  // equilibrium distance, units
+    float k_rep, k_atr;        // HarmTrunc constants; Szabo: f_mod below / above r_eq
+    float pad;
+};
 
 struct Ctx {
     // particle arrays in sorted order
     double2 *pos_cur, *pos_mid, *pos_out;
     double2 *vel_cur, *vel_out;
     double *pol_cur, *pol_out;
-    float2 *off_cur, *off_mid;
+    int2 *off_cur, *off_mid, *off_out;   // mixed form: fixed-point chunk offsets
     double2 *fd;     // pair-pass force (FP64 form)
     float2 *ff;      // pair-pass force (mixed form)
     double2 *fold_d; // Verlet F(t), FP64 form
@@ -31,6 +57,8 @@ struct Ctx {
     int32_t *uid_cur, *uid_out, *rep_cur, *rep_out;
     int32_t *cell_cur, *cell_out, *rank;
     int32_t *count, *start, *src_of, *slot_of;
+    int32_t *tile_sum;   // chunk counts per scan tile, accumulated with the histogram
+    int64_t ntiles;
     // per ring (global ring index)
     double *ring_pol;
     double *ring_area;
@@ -39,6 +67,7 @@ struct Ctx {
     const DevRep *reps;
     const MaviSpace *spaces;     // [replica][MAVI_MAX_SPACES]
     const MaviRingsCfg *rcfg;    // [replica]
+    const FixPair *fix;          // [replica][MAVI_MAX_TYPES][MAVI_MAX_TYPES]
     DevError *err;
     int64_t M;        // active particles
     int64_t Ctot;     // chunks over all replicas
@@ -46,26 +75,84 @@ struct Ctx {
     const double *noise;
     int32_t noise_mode;
     int32_t num_reps;
+    int32_t gather_mode;   // 0: warp-staged window in shared memory, 1: global loads
     uint64_t seed;
 };
 
 // ===========================================================================
-// chunk index of a position, with bounds/finite checks (src/chunks.jl:120-147)
+// Julia-exact chunk index (src/chunks.jl:120-147)
 // ===========================================================================
-__device__ __forceinline__ int64_t cell_of(const DevRep& R, double x, double y, DevError* err,
-                                           int64_t s, bool valid) {
-    if (!R.has_chunks) return R.c0;
-    int64_t row, col;
-    bool finite;
-    chunk_row_col(R, x, y, row, col, finite);
-    if (valid) {
-        if (!finite) raise_error(err, MAVI_ERR_NONFINITE, s, 0);
-        else if (row < 0 || row >= R.rows || col < 0 || col >= R.cols)
-            raise_error(err, MAVI_ERR_OUT_OF_GRID, s, row * 1000003 + col);
+// trunc(Int, div(t, l)) for the numerator t of update_particle_chunk!. For
+// t >= 0 Julia's float div is floor(t / l) exactly; it is found by checking
+// a guess g: sign(fma(-q, l, t)) is the exact sign of t - q*l (one rounding of
+// a nonzero value cannot reach zero at these magnitudes). Particles move far
+// less than a chunk per step, so the guess (the current chunk) or a
+// neighbour resolves it; otherwise the literal formula runs.
+static __device__ __forceinline__ int64_t julia_trunc_div_slow(double t, double l) {
+    double q = julia_div(t, l);
+    return q < 4e18 ? (int64_t)q : (int64_t)4e18;
+}
+
+__device__ __forceinline__ int64_t julia_trunc_div(double t, double l, int64_t g, bool has_guess) {
+    if (t < 0) return (t + l > 0) ? 0 : -1;     // div = -0.0 above -l; below it the grid is left
+    if (has_guess && g >= 0) {
+        double gd = (double)g;
+        if (fma(-gd, l, t) >= 0) {
+            if (fma(-(gd + 1.0), l, t) < 0) return g;
+            if (fma(-(gd + 2.0), l, t) < 0) return g + 1;
+        } else if (g >= 1 && fma(-(gd - 1.0), l, t) >= 0) {
+            return g - 1;
+        }
     }
+    return julia_trunc_div_slow(t, l);
+}
+
+// Row/col (0-based, with the clamp of index n+1) of a position; the FP64
+// numerators tx = x - bl_x and ty = -y + bl_y + H are returned for the
+// offset computation.
+__device__ __forceinline__ void bin_position(const DevRep& R, double x, double y, int64_t grow, int64_t gcol,
+                                             bool has_guess, int64_t& row, int64_t& col, double& tx, double& ty,
+                                             bool& finite) {
+    tx = __dsub_rn(x, R.bb_blx);
+    ty = __dadd_rn(__dadd_rn(-y, R.bb_bly), R.bb_h);
+    finite = isfinite(tx) && isfinite(ty);
+    if (!finite) { row = 0; col = 0; return; }
+    int64_t qr = julia_trunc_div(ty, R.chunk_h, grow, has_guess);
+    int64_t qc = julia_trunc_div(tx, R.chunk_l, gcol, has_guess);
+    int64_t r = qr + 1, c = qc + 1;
+    r -= (r == (int64_t)R.rows + 1) ? 1 : 0;
+    c -= (c == (int64_t)R.cols + 1) ? 1 : 0;
+    row = r - 1;
+    col = c - 1;
+}
+
+// Fixed-point offset of a position from the centre of chunk (row, col),
+// computed from the binning numerators (x - cx = tx - (col + 1/2) l,
+// y - cy = (row + 1/2) h - ty).
+__device__ __forceinline__ int2 fixed_offset(const DevRep& R, int64_t row, int64_t col, double tx, double ty) {
+    double ox = fma(-((double)col + 0.5), R.chunk_l, tx) * R.inv_u;
+    double oy = fma((double)row + 0.5, R.chunk_h, -ty) * R.inv_u;
+    // the conversion saturates; the clamp keeps differences inside int32
+    int32_t ix = min(max(__double2int_rn(ox), -kFixClamp), kFixClamp);
+    int32_t iy = min(max(__double2int_rn(oy), -kFixClamp), kFixClamp);
+    return make_int2(ix, iy);
+}
+
+// Bounds/finite checks; returns the clamped global chunk.
+__device__ __forceinline__ int64_t checked_cell(const DevRep& R, int64_t& row, int64_t& col, bool finite,
+                                                DevError* err, int64_t s) {
+    if (!finite) raise_error(err, MAVI_ERR_NONFINITE, s, 0);
+    else if (row < 0 || row >= R.rows || col < 0 || col >= R.cols)
+        raise_error(err, MAVI_ERR_OUT_OF_GRID, s, row * 1000003 + col);
     row = row < 0 ? 0 : (row >= R.rows ? R.rows - 1 : row);
     col = col < 0 ? 0 : (col >= R.cols ? R.cols - 1 : col);
     return R.c0 + col * (int64_t)R.rows + row;
+}
+
+// Whether the chunk touches the bounding box (walls of the bounding
+// rectangle can only act on particles there).
+__device__ __forceinline__ bool edge_chunk(const DevRep& R, int64_t row, int64_t col) {
+    return row <= 0 || col <= 0 || row >= R.rows - 1 || col >= R.cols - 1;
 }
 
 // Warp-aggregated histogram update: lanes with the same chunk share one
@@ -81,6 +168,11 @@ __device__ __forceinline__ void count_into_chunk(const Ctx& C, bool valid, int64
     int base = 0;
     if (valid && lane == leader) base = atomicAdd(&C.count[cell], __popc(peers));
     base = __shfl_sync(full, base, leader);
+    // scan-tile totals: one atomic per warp and tile (consecutive particles
+    // share a tile; per-particle atomics on one address would serialise)
+    int tkey = valid ? (int)(cell / kScanTile) : -1;
+    unsigned tpeers = __match_any_sync(full, tkey);
+    if (valid && lane == __ffs(tpeers) - 1) atomicAdd(&C.tile_sum[tkey], __popc(tpeers));
     if (valid) {
         int r = base + __popc(peers & ((1u << lane) - 1u));
         C.cell_out[s] = (int32_t)cell;
@@ -89,8 +181,61 @@ __device__ __forceinline__ void count_into_chunk(const Ctx& C, bool valid, int64
     }
 }
 
-// Standalone histogram of the *_out state (upload, explicit update_chunks!).
-static __global__ void k_count(Ctx C) {
+// Chunk (and mixed-form offset) of a final position; `guess_cell` is the
+// particle's current chunk or -1.
+template <int PREC>
+__device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int64_t s, double x, double y,
+                                            int64_t guess_cell) {
+    if (!R.has_chunks) {
+        if constexpr (PREC == kPrecMixed) {
+            double tx = __dsub_rn(x, R.bb_blx), ty = __dadd_rn(__dadd_rn(-y, R.bb_bly), R.bb_h);
+            C.off_out[s] = fixed_offset(R, 0, 0, tx, ty);
+        }
+        return R.c0;
+    }
+    int64_t grow = 0, gcol = 0;
+    bool has_guess = guess_cell >= 0;
+    if (has_guess) {
+        int32_t lc = (int32_t)(guess_cell - R.c0);
+        gcol = lc / R.rows;
+        grow = lc - gcol * R.rows;
+    }
+    int64_t row, col;
+    double tx, ty;
+    bool finite;
+    bin_position(R, x, y, grow, gcol, has_guess, row, col, tx, ty, finite);
+    int64_t cell = checked_cell(R, row, col, finite, C.err, s);
+    if constexpr (PREC == kPrecMixed) C.off_out[s] = fixed_offset(R, row, col, tx, ty);
+    return cell;
+}
+
+// Chunk of a final position, fast path first: the offset from the centre of
+// the current chunk is computed in fixed-point units; when it lies more than
+// one unit inside the chunk, the particle is > u/2 (~1e-9 of a chunk) inside,
+// far beyond the rounding of the FP64 numerator of the Julia formula (an ulp
+// of the position), so the Julia quotient is the current chunk and the exact
+// checks are skipped. Returns -1 when the exact path is needed.
+template <int PREC>
+__device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64_t s, double x, double y,
+                                           int32_t cell) {
+    if (!R.has_chunks) return -1;
+    int32_t lc = (int32_t)(cell - R.c0);
+    int32_t col = lc / R.rows, row = lc - col * R.rows;
+    double cx = fma((double)col, R.chunk_l, R.cx0);
+    double cy = fma(-(double)row, R.chunk_h, R.cy0);
+    int32_t ix = __double2int_rn((x - cx) * R.inv_u);
+    int32_t iy = __double2int_rn((y - cy) * R.inv_u);
+    if (abs(ix) < R.half_sx_i - 1 && abs(iy) < R.half_sy_i - 1) {
+        if constexpr (PREC == kPrecMixed) C.off_out[s] = make_int2(ix, iy);
+        return cell;
+    }
+    return -1;
+}
+
+// Standalone histogram of the *_out state (upload, explicit update_chunks!,
+// the rings step). With use_guess the current chunk of the slot is the guess.
+template <int PREC>
+__global__ void k_count(Ctx C, int32_t use_guess) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = s < C.M;
     int64_t cell = 0;
@@ -98,7 +243,7 @@ static __global__ void k_count(Ctx C) {
     if (valid) {
         const DevRep& R = C.reps[C.rep_out[s]];
         double2 p = C.pos_out[s];
-        cell = cell_of(R, p.x, p.y, C.err, s, true);
+        cell = bin_final<PREC>(C, R, s, p.x, p.y, use_guess ? (int64_t)C.cell_cur[s] : -1);
         cap = R.has_chunks ? R.cap : (1 << 30);
     }
     count_into_chunk(C, valid, s, cell, cap);
@@ -107,10 +252,6 @@ static __global__ void k_count(Ctx C) {
 // ===========================================================================
 // exclusive scan of chunk counts -> start (three passes over 2048-chunk tiles)
 // ===========================================================================
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
-
 __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total) {
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int x = v;
@@ -188,11 +329,46 @@ static __global__ void k_scan_apply(const int32_t* __restrict__ count, int64_t n
     }
 }
 
+// Single-kernel exclusive scan: the histogram already accumulated each tile's
+// total, so every block sums the tiles before its own, scans its tile and
+// clears the counts it consumed (the next histogram starts from zero).
+static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int32_t* __restrict__ tile_sum,
+                              int32_t* __restrict__ start, int64_t* d_step, int32_t advance) {
+    __shared__ int smem[32];
+    int pre = 0;
+    for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
+    int tile_off;
+    block_exclusive_scan(pre, smem, tile_off);
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < n) ? count[base + k] : 0;
+        sum += v[k];
+    }
+    int total;
+    int ex = block_exclusive_scan(sum, smem, total) + tile_off;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) {
+            start[base + k] = ex;
+            count[base + k] = 0;
+        }
+        ex += v[k];
+    }
+    if (threadIdx.x == 0) {
+        if (blockIdx.x == gridDim.x - 1) start[n] = tile_off + total;
+        if (advance && blockIdx.x == 0) d_step[0] += 1;
+    }
+}
+
 // ===========================================================================
 // scatter: each particle claims start[cell] + rank
 // ===========================================================================
 static __global__ void k_scatter(Ctx C) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < C.ntiles) C.tile_sum[s] = 0;   // k_scan has consumed the tile sums
     if (s >= C.M) return;
     int32_t c = C.cell_out[s];
     int32_t dst = C.start[c] + C.rank[s];
@@ -201,55 +377,29 @@ static __global__ void k_scatter(Ctx C) {
 }
 
 // ===========================================================================
-// per chunk: order members by user id (the reference appends particles in
-// ascending id, src/chunks.jl:150-161) and permute the state into *_cur.
+// Per claimed slot: the particle's place inside its chunk is its rank by user
+// id (the reference appends particles in ascending id, src/chunks.jl:150-161),
+// which makes the order deterministic; the state moves into *_cur.
 // ===========================================================================
-constexpr int kSortMax = 64;
-
 template <int PREC, bool HAS_VEL, bool HAS_POL>
-__global__ void k_sort_permute(Ctx C) {
-    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C.Ctot) return;
+__global__ void k_permute(Ctx C) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= C.M) return;
+    int32_t sm = C.src_of[p];
+    int32_t c = C.cell_out[sm];
     int32_t b = C.start[c], e = C.start[c + 1];
-    int32_t k = e - b;
-    if (k <= 0) return;
-    int32_t src[kSortMax];
-    int32_t key[kSortMax];
-    bool sorted = k <= kSortMax;
-    if (sorted) {
-        for (int m = 0; m < k; m++) {
-            int32_t sm = C.src_of[b + m];
-            int32_t km = C.uid_out[sm];
-            int q = m;
-            while (q > 0 && key[q - 1] > km) {
-                key[q] = key[q - 1];
-                src[q] = src[q - 1];
-                q--;
-            }
-            key[q] = km;
-            src[q] = sm;
-        }
-    }
-    for (int m = 0; m < k; m++) {
-        int32_t sm = sorted ? src[m] : C.src_of[b + m];
-        int32_t dst = b + m;
-        double2 p = C.pos_out[sm];
-        int32_t u = C.uid_out[sm];
-        int32_t r = C.rep_out[sm];
-        C.pos_cur[dst] = p;
-        C.uid_cur[dst] = u;
-        C.rep_cur[dst] = r;
-        C.cell_cur[dst] = (int32_t)c;
-        C.slot_of[u] = dst;
-        if constexpr (HAS_VEL) C.vel_cur[dst] = C.vel_out[sm];
-        if constexpr (HAS_POL) C.pol_cur[dst] = C.pol_out[sm];
-        if constexpr (PREC == kPrecMixed) {
-            const DevRep& R = C.reps[r];
-            int64_t lc = c - R.c0;
-            int64_t row = lc % R.rows, col = lc / R.rows;
-            C.off_cur[dst] = make_float2((float)(p.x - chunk_cx(R, col)), (float)(p.y - chunk_cy(R, row)));
-        }
-    }
+    int32_t u = C.uid_out[sm];
+    int32_t rank = 0;
+    for (int32_t q = b; q < e; q++) rank += (C.uid_out[C.src_of[q]] < u) ? 1 : 0;
+    int32_t dst = b + rank;
+    C.pos_cur[dst] = C.pos_out[sm];
+    C.uid_cur[dst] = u;
+    C.rep_cur[dst] = C.rep_out[sm];
+    C.cell_cur[dst] = c;
+    C.slot_of[u] = dst;
+    if constexpr (HAS_VEL) C.vel_cur[dst] = C.vel_out[sm];
+    if constexpr (HAS_POL) C.pol_cur[dst] = C.pol_out[sm];
+    if constexpr (PREC == kPrecMixed) C.off_cur[dst] = C.off_out[sm];
 }
 
 // ===========================================================================
@@ -262,50 +412,13 @@ __global__ void k_sort_permute(Ctx C) {
 // wrapped when periodic with >= 3 chunks per side), so every particle
 // receives exactly the reference's pair terms, without atomics and in a fixed
 // order (deterministic).
+//
+// FP64 form: differences of FP64 positions, FP64 pair law.
+// Mixed form: differences of fixed-point offsets plus the exact stencil shift
+// are exact integers (so are the squared distance, the minimum image and the
+// cutoff test); the pair law runs in FP32, with the cancelling term of the
+// harmonic laws (dist_eq^2 - d^2) formed exactly in int64 first.
 // ===========================================================================
-
-// Accumulator: FP64, or FP32 with Kahan compensation.
-template <int PREC> struct Acc;
-template <> struct Acc<kPrecFP64> {
-    double x = 0, y = 0;
-    __device__ __forceinline__ void add(double fx, double fy) { x += fx; y += fy; }
-    __device__ __forceinline__ double gx() const { return x; }
-    __device__ __forceinline__ double gy() const { return y; }
-};
-template <> struct Acc<kPrecMixed> {
-    float x = 0, y = 0, cx = 0, cy = 0;
-    __device__ __forceinline__ void add(float fx, float fy) {
-        float yx = fx - cx, tx = x + yx;
-        cx = (tx - x) - yx;
-        x = tx;
-        float yy = fy - cy, ty = y + yy;
-        cy = (ty - y) - yy;
-        y = ty;
-    }
-    __device__ __forceinline__ double gx() const { return (double)x - (double)cx; }
-    __device__ __forceinline__ double gy() const { return (double)y - (double)cy; }
-};
-
-// Rings pair term (src/rings/integration.jl:32-77): interaction matrix by ring
-// type, zero beyond dist_max, bonded neighbours of the same ring excluded,
-// attraction only between different rings.
-template <typename T>
-__device__ __forceinline__ T rings_pair_scalar(const MaviRingsCfg& rc, int ti, int tj, bool same_ring,
-                                               int32_t pi, int32_t pj, int32_t n_i, T d2) {
-    T dmax = (T)rc.inter_dist_max[ti][tj];
-    if (d2 > dmax * dmax) return T(0);
-    if (same_ring) {
-        int32_t diff = pi > pj ? pi - pj : pj - pi;
-        if (diff == 1 || diff == n_i - 1) return T(0);
-    }
-    T deq = (T)rc.inter_dist_eq[ti][tj];
-    T inv_d = rsqrt_<T>(d2);
-    T k;
-    if (d2 < deq * deq) k = (T)rc.inter_k_rep[ti][tj];
-    else k = same_ring ? T(0) : (T)rc.inter_k_atr[ti][tj];
-    // fmod/dist = -k (dist/deq - 1)/dist = k (1/dist - 1/deq)
-    return k * (inv_d - T(1) / deq);
-}
 
 struct RingInfo {
     int32_t ring;   // replica-local ring index
@@ -322,85 +435,366 @@ __device__ __forceinline__ RingInfo ring_info(const Ctx& C, const DevRep& R, int
     return ri;
 }
 
-template <int PREC, int DYN>
-__device__ __forceinline__ void gather_pair_forces(const Ctx& C, const DevRep& R, int64_t s, int32_t cell,
-                                                   const double2* __restrict__ P,
-                                                   const float2* __restrict__ O, Acc<PREC>& acc) {
-    using T = typename std::conditional<PREC == kPrecFP64, double, float>::type;
-    const T* prm;
-    if constexpr (PREC == kPrecFP64) prm = R.pd; else prm = R.pf;
-    T pix, piy;
-    if constexpr (PREC == kPrecFP64) { double2 p = P[s]; pix = p.x; piy = p.y; }
-    else { float2 o = O[s]; pix = o.x; piy = o.y; }
-    const bool mi = R.min_image;
-    T bx, by, hx, hy;
-    if constexpr (PREC == kPrecFP64) { bx = R.box_x; by = R.box_y; hx = R.half_box_x; hy = R.half_box_y; }
-    else { bx = R.box_xf; by = R.box_yf; hx = R.half_box_xf; hy = R.half_box_yf; }
-
-    RingInfo me{0, 0, 0};
-    const MaviRingsCfg* rc = nullptr;
-    int32_t n_me = 0;
-    if constexpr (DYN == MAVI_DYN_RINGS) {
-        me = ring_info(C, R, C.uid_cur[s]);
-        rc = &C.rcfg[C.rep_cur[s]];
-        n_me = rc->num_particles[me.type];
+// Rings pair term (src/rings/integration.jl:32-77), FP64: interaction matrix
+// by ring type, zero beyond dist_max, bonded neighbours of the same ring
+// excluded, attraction only between different rings.
+__device__ __forceinline__ double rings_pair_scalar_d(const MaviRingsCfg& rc, int ti, int tj, bool same_ring,
+                                                      int32_t pi, int32_t pj, int32_t n_i, double d2) {
+    double dmax = rc.inter_dist_max[ti][tj];
+    if (d2 > dmax * dmax) return 0.0;
+    if (same_ring) {
+        int32_t diff = pi > pj ? pi - pj : pj - pi;
+        if (diff == 1 || diff == n_i - 1) return 0.0;
     }
+    double deq = rc.inter_dist_eq[ti][tj];
+    double k;
+    if (d2 < deq * deq) k = rc.inter_k_rep[ti][tj];
+    else k = same_ring ? 0.0 : rc.inter_k_atr[ti][tj];
+    return k * (rsqrt(d2) - 1.0 / deq);
+}
 
-    auto visit = [&](int32_t b, int32_t e, T shx, T shy) {
+// int64 -> float without a 64-bit conversion instruction (those run on the
+// FP64 pipe, ~1/70 of the FP32 rate on GB300): hi * 2^32 + lo, hi exact.
+__device__ __forceinline__ float i64_to_f32(long long v) {
+    int32_t hi = (int32_t)(v >> 32);
+    uint32_t lo = (uint32_t)v;
+    return fmaf((float)hi, 4294967296.0f, (float)lo);
+}
+__device__ __forceinline__ float u64_to_f32(unsigned long long v) {
+    uint32_t hi = (uint32_t)(v >> 32);
+    uint32_t lo = (uint32_t)v;
+    return fmaf((float)hi, 4294967296.0f, (float)lo);
+}
+
+// Mixed-form pair laws on exact integer differences (units u of the replica).
+// dxi, dyi are int32 (|d| < 2^31 units = 8 chunks); d2 = dxi^2 + dyi^2 is
+// exact in 64 bits. Returns the force components on i.
+template <int DYN>
+__device__ __forceinline__ void pair_fixed(const DevRep& R, const FixPair& fp, int32_t dxi, int32_t dyi,
+                                           unsigned long long d2, float& fx, float& fy) {
+    fx = 0.f;
+    fy = 0.f;
+    if constexpr (DYN == MAVI_DYN_HARM_TRUNC || DYN == MAVI_DYN_RINGS) {
+        // f = k (1/d - 1/deq) dr = k (deq^2 - d^2) / (d deq (deq + d)) dr
+        if (d2 > fp.cut2) return;
+        long long D = fp.eq2 - (long long)d2;
+        float k = D > 0 ? fp.k_rep : fp.k_atr;
+        float du = sqrtf(u64_to_f32(d2));
+        float sc = __fdividef(k * i64_to_f32(D), du * fp.eq * (fp.eq + du));
+        fx = sc * (float)dxi;
+        fy = sc * (float)dyi;
+    } else if constexpr (DYN == MAVI_DYN_SZABO) {
+        // f = -f_mod (d - r_eq) dr = -f_mod (d^2 - r_eq^2)/(d + r_eq) dr
+        if (d2 > fp.cut2) return;
+        long long D = (long long)d2 - fp.eq2;
+        float fm = D > 0 ? fp.k_atr : fp.k_rep;
+        float du = sqrtf(u64_to_f32(d2));
+        float sc = __fdividef(-fm * i64_to_f32(D) * R.u2_f, du + fp.eq);
+        fx = sc * (float)dxi;
+        fy = sc * (float)dyi;
+    } else {  // LenJones / RunTumble (WCA)
+        if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
+            if (d2 > fp.cut2) return;
+        }
+        float r2 = u64_to_f32(d2) * R.u2_f;
+        float ir2 = __frcp_rn(r2);
+        float ir6 = ir2 * ir2 * ir2;
+        float sc = ir6 * ir2 * (R.pf[0] * ir6 - R.pf[1]) * R.u_f;
+        fx = sc * (float)dxi;
+        fy = sc * (float)dyi;
+    }
+}
+
+// Force accumulators. Mixed form: FP32, Kahan-compensated for Lennard-Jones
+// (no cutoff: tens of terms with cancellation), plain for the short-range laws.
+template <int PREC, int DYN> struct Acc;
+template <int DYN> struct Acc<kPrecFP64, DYN> {
+    double x = 0, y = 0;
+    __device__ __forceinline__ double gx() const { return x; }
+    __device__ __forceinline__ double gy() const { return y; }
+};
+template <int DYN> struct Acc<kPrecMixed, DYN> {
+    float x = 0, y = 0, cx = 0, cy = 0;
+    __device__ __forceinline__ void add(float fx, float fy) {
+        if constexpr (DYN == MAVI_DYN_LEN_JONES) {
+            float yx = fx - cx, tx = x + yx;
+            cx = (tx - x) - yx;
+            x = tx;
+            float yy = fy - cy, ty = y + yy;
+            cy = (ty - y) - yy;
+            y = ty;
+        } else {
+            x += fx;
+            y += fy;
+        }
+    }
+    __device__ __forceinline__ float gx() const { return x - cx; }
+    __device__ __forceinline__ float gy() const { return y - cy; }
+};
+
+template <int PREC> struct PartOf { using T = int2; };            // fixed-point offset
+template <> struct PartOf<kPrecFP64> { using T = double2; };       // FP64 position
+
+// The particle whose force a lane sums.
+template <int PREC, int DYN> struct Me {
+    typename PartOf<PREC>::T p;
+    RingInfo ri;
+    int32_t n_ring;
+    const FixPair* fixr;
+    FixPair fp0;
+};
+
+template <int PREC, int DYN>
+__device__ __forceinline__ Me<PREC, DYN> make_me(const Ctx& C, const DevRep& R, int32_t rep, int64_t s,
+                                                 const typename PartOf<PREC>::T* __restrict__ P) {
+    Me<PREC, DYN> m;
+    m.p = P[s];
+    m.ri = RingInfo{0, 0, 0};
+    m.n_ring = 0;
+    m.fixr = C.fix + (int64_t)rep * MAVI_MAX_TYPES * MAVI_MAX_TYPES;
+    if constexpr (PREC == kPrecMixed) m.fp0 = m.fixr[0];
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        m.ri = ring_info(C, R, C.uid_cur[s]);
+        m.n_ring = C.rcfg[rep].num_particles[m.ri.type];
+    }
+    return m;
+}
+
+// One pair term added to acc: q is the neighbour's position (FP64) or
+// offset (mixed), uq its user id (rings), (shx, shy) the stencil shift in
+// fixed-point units, mi whether the minimum image applies. The global and the
+// staged gathers both call this, in the same order, so they agree bitwise.
+template <int DYN>
+__device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t rep, const Me<kPrecFP64, DYN>& me,
+                                          double2 q, int32_t uq, int32_t, int32_t, bool mi,
+                                          Acc<kPrecFP64, DYN>& acc) {
+    double dx = me.p.x - q.x, dy = me.p.y - q.y;
+    if (mi) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
+    double d2 = dx * dx + dy * dy;
+    double sc;
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        RingInfo o = ring_info(C, R, uq);
+        sc = rings_pair_scalar_d(C.rcfg[rep], me.ri.type, o.type, o.ring == me.ri.ring, me.ri.p, o.p, me.n_ring, d2);
+    } else {
+        sc = pair_scalar<DYN, double>(R.pd, d2);
+    }
+    acc.x = fma(sc, dx, acc.x);
+    acc.y = fma(sc, dy, acc.y);
+}
+
+template <int DYN>
+__device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t, const Me<kPrecMixed, DYN>& me,
+                                          int2 oj, int32_t uq, int32_t shx, int32_t shy, bool mi,
+                                          Acc<kPrecMixed, DYN>& acc) {
+    // offsets are clamped to +-4 chunks and neighbours are <= 1 chunk apart,
+    // so the differences fit int32 (wrapping arithmetic)
+    int32_t dxi = (int32_t)((uint32_t)me.p.x - (uint32_t)oj.x + (uint32_t)shx);
+    int32_t dyi = (int32_t)((uint32_t)me.p.y - (uint32_t)oj.y + (uint32_t)shy);
+    if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
+        if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
+        if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
+    }
+    unsigned long long d2 = (unsigned long long)((long long)dxi * dxi) + (unsigned long long)((long long)dyi * dyi);
+    float fx, fy;
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        RingInfo o = ring_info(C, R, uq);
+        bool same = o.ring == me.ri.ring;
+        if (same) {
+            int32_t diff = me.ri.p > o.p ? me.ri.p - o.p : o.p - me.ri.p;
+            if (diff == 1 || diff == me.n_ring - 1) return;
+        }
+        FixPair fp = me.fixr[me.ri.type * MAVI_MAX_TYPES + o.type];
+        if (same) fp.k_atr = 0.f;
+        pair_fixed<DYN>(R, fp, dxi, dyi, d2, fx, fy);
+    } else {
+        pair_fixed<DYN>(R, me.fp0, dxi, dyi, d2, fx, fy);
+    }
+    acc.add(fx, fy);
+}
+
+// Global-memory gather of one lane (also the all-pairs mode without chunks).
+template <int PREC, int DYN>
+__device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
+                                              const typename PartOf<PREC>::T* __restrict__ P,
+                                              const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc) {
+    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
         for (int32_t j = b; j < e; j++) {
             if (j == (int32_t)s) continue;
-            T dx, dy;
-            if constexpr (PREC == kPrecFP64) {
-                double2 q = P[j];
-                dx = pix - q.x;
-                dy = piy - q.y;
-            } else {
-                float2 q = O[j];
-                dx = (pix - q.x) + shx;
-                dy = (piy - q.y) + shy;
-            }
-            if (mi) {
-                if constexpr (PREC == kPrecFP64) { dx = min_image1(dx, bx, hx); dy = min_image1(dy, by, hy); }
-                else { dx = min_image1f(dx, bx, hx); dy = min_image1f(dy, by, hy); }
-            }
-            T d2 = dx * dx + dy * dy;
-            T sc;
-            if constexpr (DYN == MAVI_DYN_RINGS) {
-                RingInfo o = ring_info(C, R, C.uid_cur[j]);
-                sc = rings_pair_scalar<T>(*rc, me.type, o.type, o.ring == me.ring, me.p, o.p, n_me, d2);
-            } else {
-                sc = pair_scalar<DYN, T>(prm, d2);
-            }
-            acc.add(sc * dx, sc * dy);
+            int32_t uq = 0;
+            if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
+            pair_term<DYN>(C, R, rep, me, P[j], uq, shx, shy, mi, acc);
         }
     };
-
     if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224)
-        visit((int32_t)R.a0, (int32_t)(R.a0 + R.na), T(0), T(0));
+        visit((int32_t)R.a0, (int32_t)(R.a0 + R.na), 0, 0, R.min_image);
         return;
     }
-    int64_t lc = cell - R.c0;
-    int32_t row = (int32_t)(lc % R.rows), col = (int32_t)(lc / R.rows);
-    T cl, ch;
-    if constexpr (PREC == kPrecFP64) { cl = R.chunk_l; ch = R.chunk_h; } else { cl = R.chunk_lf; ch = R.chunk_hf; }
+    int32_t lc = (int32_t)(cell - R.c0);
+    int32_t col = lc / R.rows, row = lc - col * R.rows;
 #pragma unroll 1
     for (int dc = -1; dc <= 1; dc++) {
         int ncol = col + dc;
-        if (R.periodic) ncol = ncol < 0 ? ncol + R.cols : (ncol >= R.cols ? ncol - R.cols : ncol);
-        else if (ncol < 0 || ncol >= R.cols) continue;
+        bool wrapped = false;
+        if (R.periodic) {
+            if (ncol < 0) { ncol += R.cols; wrapped = true; }
+            else if (ncol >= R.cols) { ncol -= R.cols; wrapped = true; }
+        } else if (ncol < 0 || ncol >= R.cols) continue;
 #pragma unroll 1
         for (int dr = -1; dr <= 1; dr++) {
             int nrow = row + dr;
-            if (R.periodic) nrow = nrow < 0 ? nrow + R.rows : (nrow >= R.rows ? nrow - R.rows : nrow);
-            else if (nrow < 0 || nrow >= R.rows) continue;
+            bool wr = wrapped;
+            if (R.periodic) {
+                if (nrow < 0) { nrow += R.rows; wr = true; }
+                else if (nrow >= R.rows) { nrow -= R.rows; wr = true; }
+            } else if (nrow < 0 || nrow >= R.rows) continue;
             int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
-            int32_t b = C.start[nc], e = C.start[nc + 1];
-            // offset of the neighbour chunk centre relative to ours:
-            // x grows with the column, y decreases with the row.
-            T shx = -(T)dc * cl, shy = (T)dr * ch;
-            visit(b, e, shx, shy);
+            // centre of the neighbour chunk relative to ours, in units:
+            // x grows with the column, y decreases with the row
+            visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small));
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-staged gather. The 32 particles of a warp are consecutive in chunk
+// order, so they sit in a short run of rows of one (or two) chunk columns.
+// For each column present, the warp loads the chunk boundaries of the window
+// rows [rmin-1, rmax+1] of the three neighbouring columns, then copies the
+// particles of those rows into shared memory with coalesced loads, and each
+// lane sums its terms from shared memory — a handful of memory round trips
+// per warp instead of ~18 dependent loads per lane. Windows that do not fit
+// fall back to the global gather (same order, bitwise-identical result).
+// ---------------------------------------------------------------------------
+constexpr int kStageRows = 64;     // rows in a window
+constexpr int kStageParts = 256;   // staged particles per window
+constexpr int kPassThreads = 128;
+constexpr int kPassWarps = kPassThreads / 32;
+
+template <int PREC, int DYN> struct Stage {
+    typename PartOf<PREC>::T part[kStageParts];
+    int32_t uid[DYN == MAVI_DYN_RINGS ? kStageParts : 1];
+    int32_t gb[3 * kStageRows];    // global first particle of (column k, window row w)
+    int32_t rn[3 * kStageRows];    // particles in it
+    int32_t rb[3 * kStageRows];    // first shared-memory slot
+};
+
+template <int PREC, int DYN>
+__device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s, int32_t rep, const DevRep& R,
+                                            int32_t cell, const typename PartOf<PREC>::T* __restrict__ P,
+                                            Stage<PREC, DYN>& st, Acc<PREC, DYN>& acc) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool want = valid && R.has_chunks;
+    // all lanes of a staged window must belong to one replica
+    unsigned vmask = __ballot_sync(full, valid);
+    int first = vmask ? __ffs(vmask) - 1 : 0;
+    int32_t rep0 = __shfl_sync(full, rep, first);
+    bool uniform = __all_sync(full, !valid || rep == rep0);
+    Me<PREC, DYN> me;
+    if (valid) me = make_me<PREC, DYN>(C, R, rep, s, P);
+    int32_t col = 0, row = 0;
+    if (want) {
+        int32_t lc = (int32_t)(cell - R.c0);
+        col = lc / R.rows;
+        row = lc - col * R.rows;
+    }
+    unsigned pending = (uniform && C.gather_mode == 0) ? __ballot_sync(full, want) : 0u;
+    while (pending) {
+        int leader = __ffs(pending) - 1;
+        int ccur = __shfl_sync(full, col, leader);
+        bool act = ((pending >> lane) & 1u) && col == ccur;
+        unsigned amask = __ballot_sync(full, act);
+        int rmin = __reduce_min_sync(full, act ? row : 0x7fffffff);
+        int rmax = __reduce_max_sync(full, act ? row : -0x7fffffff);
+        const int W = rmax - rmin + 3;
+        // R is the replica of every active lane (uniform window)
+        const int nrows = __shfl_sync(full, R.rows, leader), ncols = __shfl_sync(full, R.cols, leader);
+        const int periodic = __shfl_sync(full, R.periodic, leader);
+        const long long c0 = __shfl_sync(full, R.c0, leader);
+        bool ok = W <= kStageRows && (!periodic || W <= nrows);
+        if (ok) {
+            for (int q = lane; q < 3 * W; q += 32) {
+                int k = q / W, w = q - k * W;
+                int ncol = ccur + k - 1, r = rmin - 1 + w;
+                bool inside = true;
+                if (periodic) {
+                    ncol = ncol < 0 ? ncol + ncols : (ncol >= ncols ? ncol - ncols : ncol);
+                    r = r < 0 ? r + nrows : (r >= nrows ? r - nrows : r);
+                } else {
+                    inside = ncol >= 0 && ncol < ncols && r >= 0 && r < nrows;
+                }
+                int32_t b = 0, n = 0;
+                if (inside) {
+                    long long ch = c0 + (long long)ncol * nrows + r;
+                    b = C.start[ch];
+                    n = C.start[ch + 1] - b;
+                }
+                st.gb[q] = b;
+                st.rn[q] = n;
+            }
+            __syncwarp();
+            // exclusive scan of the row counts -> shared-memory slots
+            const int per = (3 * W + 31) / 32;
+            const int q0 = lane * per;
+            int local = 0;
+            for (int t = 0; t < per; t++) local += (q0 + t < 3 * W) ? st.rn[q0 + t] : 0;
+            int incl = local;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int ex = incl - local;
+            const int total = __shfl_sync(full, incl, 31);
+            for (int t = 0; t < per; t++) {
+                int q = q0 + t;
+                if (q < 3 * W) { st.rb[q] = ex; ex += st.rn[q]; }
+            }
+            __syncwarp();
+            ok = total <= kStageParts;
+            if (ok) {
+                // row by row: a lane copies whole rows (rows are short and
+                // consecutive rows are consecutive in memory)
+                for (int q = lane; q < 3 * W; q += 32) {
+                    const int b = st.rb[q], g = st.gb[q], n = st.rn[q];
+                    for (int m = 0; m < n; m++) {
+                        st.part[b + m] = P[g + m];
+                        if constexpr (DYN == MAVI_DYN_RINGS) st.uid[b + m] = C.uid_cur[g + m];
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (act) {
+            if (ok) {
+                const int wme = row - rmin + 1;
+#pragma unroll 1
+                for (int k = 0; k < 3; k++) {
+                    const int dc = k - 1;
+                    const bool cw = periodic && (ccur + dc < 0 || ccur + dc >= ncols);
+#pragma unroll 1
+                    for (int dr = -1; dr <= 1; dr++) {
+                        const int q = k * W + wme + dr;
+                        const bool rw = periodic && (row + dr < 0 || row + dr >= nrows);
+                        const bool mi = R.min_image && (cw || rw || R.mi_small);
+                        const int b = st.rb[q], e = b + st.rn[q];
+                        const int self = (dc == 0 && dr == 0) ? b + (int)(s - st.gb[q]) : -1;
+                        for (int idx = b; idx < e; idx++) {
+                            if (idx == self) continue;
+                            int32_t uq = 0;
+                            if constexpr (DYN == MAVI_DYN_RINGS) uq = st.uid[idx];
+                            pair_term<DYN>(C, R, rep, me, st.part[idx], uq, -dc * R.sx_i, dr * R.sy_i, mi, acc);
+                        }
+                    }
+                }
+            } else {
+                gather_global<PREC, DYN>(C, R, rep, s, cell, P, me, acc);
+            }
+        }
+        __syncwarp();
+        pending &= ~amask;
+    }
+    if (valid && (!want || !uniform || C.gather_mode != 0)) gather_global<PREC, DYN>(C, R, rep, s, cell, P, me, acc);
 }
 
 // ===========================================================================
@@ -432,7 +826,7 @@ __device__ __forceinline__ double proc_dist(int mode, double dist, double flag) 
     return dist;
 }
 
-static __device__ void add_wall_forces(const Ctx& C, int32_t rep, const DevRep& R, double x, double y,
+static __device__ __forceinline__ void add_wall_forces(const Ctx& C, int32_t rep, const DevRep& R, double x, double y,
                                 double& fx, double& fy) {
     const MaviSpace* sps = C.spaces + (int64_t)rep * MAVI_MAX_SPACES;
     for (int k = 0; k < R.num_spaces; k++) {
@@ -465,7 +859,7 @@ static __device__ void add_wall_forces(const Ctx& C, int32_t rep, const DevRep& 
     }
 }
 
-static __device__ void apply_walls(const Ctx& C, int32_t rep, const DevRep& R, double radius, double& x, double& y,
+static __device__ __forceinline__ void apply_walls(const Ctx& C, int32_t rep, const DevRep& R, double radius, double& x, double& y,
                             double& vx, double& vy, bool has_vel) {
     const MaviSpace* sps = C.spaces + (int64_t)rep * MAVI_MAX_SPACES;
     for (int k = 0; k < R.num_spaces; k++) {
@@ -558,21 +952,46 @@ constexpr int kPassOverdamped = 3; // x += mobility F dt, walls!, histogram
 constexpr int kPassSzabo = 4;      // update_szabo!, walls!, histogram
 constexpr int kPassRTP = 5;        // update_rtp!, walls!, histogram
 
+// walls! then the chunk of the final position. When every wall acts on the
+// bounding rectangle only, a particle whose pre-wall chunk is interior cannot
+// be touched by a wall, so the walls run for edge-chunk particles only.
+template <int PREC>
+__device__ __forceinline__ int64_t walls_and_bin(const Ctx& C, int32_t rep, const DevRep& R, int64_t s,
+                                                int32_t cell, double& x, double& y, double& vx, double& vy,
+                                                bool has_vel) {
+    int64_t fast = bin_fast<PREC>(C, R, s, x, y, cell);
+    if (fast >= 0) {
+        if (!R.has_walls) return fast;
+        if (R.walls_edge_only) {
+            int32_t lc = (int32_t)(cell - R.c0);
+            int32_t col = lc / R.rows, row = lc - col * R.rows;
+            if (!edge_chunk(R, row, col)) return fast;   // no bounding-box wall can act
+        }
+    }
+    if (R.has_walls) apply_walls(C, rep, R, R.radius, x, y, vx, vy, has_vel);
+    return bin_final<PREC>(C, R, s, x, y, cell);
+}
+
 template <int PREC, int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
-__global__ void __launch_bounds__(256) k_pass(Ctx C, int32_t with_wall_forces) {
+__global__ void __launch_bounds__(kPassThreads, 4) k_pass(Ctx C, int32_t with_wall_forces) {
+    __shared__ Stage<PREC, DYN> stage[kPassWarps];
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = s < C.M;
     int64_t new_cell = 0;
     int32_t cap = 1 << 30;
+    int32_t rep = valid ? C.rep_cur[s] : 0;
+    const DevRep& R = C.reps[rep];
+    int32_t cell = valid ? C.cell_cur[s] : 0;
+    const double2* P = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    Acc<PREC, DYN> acc;
+    if constexpr (PREC == kPrecFP64) {
+        gather_warp<PREC, DYN>(C, valid, s, rep, R, cell, P, stage[threadIdx.x >> 5], acc);
+    } else {
+        gather_warp<PREC, DYN>(C, valid, s, rep, R, cell, (PASS == kPassVerlet2) ? C.off_mid : C.off_cur,
+                               stage[threadIdx.x >> 5], acc);
+    }
     if (valid) {
-        int32_t rep = C.rep_cur[s];
-        const DevRep& R = C.reps[rep];
-        int32_t cell = C.cell_cur[s];
-        Acc<PREC> acc;
-        const double2* P = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
-        const float2* O = (PASS == kPassVerlet2) ? C.off_mid : C.off_cur;
-        gather_pair_forces<PREC, DYN>(C, R, s, cell, P, O, acc);
-        double fx = acc.gx(), fy = acc.gy();
+        double fx = (double)acc.gx(), fy = (double)acc.gy();
         double2 p = P[s];
         bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
         if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
@@ -590,9 +1009,11 @@ __global__ void __launch_bounds__(256) k_pass(Ctx C, int32_t with_wall_forces) {
             if constexpr (PREC == kPrecFP64) C.fold_d[s] = make_double2(fx, fy);
             else {
                 C.fold_f[s] = make_float2((float)fx, (float)fy);
-                int64_t lc = cell - R.c0;
-                int64_t row = lc % R.rows, col = lc / R.rows;
-                C.off_mid[s] = make_float2((float)(nx - chunk_cx(R, col)), (float)(ny - chunk_cy(R, row)));
+                // offsets of x(t+dt) from the (stale) chunk of this step
+                int32_t lc = (int32_t)(cell - R.c0);
+                int64_t col = lc / R.rows, row = lc - col * R.rows;
+                double tx = __dsub_rn(nx, R.bb_blx), ty = __dadd_rn(__dadd_rn(-ny, R.bb_bly), R.bb_h);
+                C.off_mid[s] = fixed_offset(R, row, col, tx, ty);
             }
         } else {
             double x = p.x, y = p.y, vx = 0, vy = 0;
@@ -605,9 +1026,14 @@ __global__ void __launch_bounds__(256) k_pass(Ctx C, int32_t with_wall_forces) {
                 vx = __dadd_rn(vx, __dmul_rn(h, __dadd_rn(fx, ox)));
                 vy = __dadd_rn(vy, __dmul_rn(h, __dadd_rn(fy, oy)));
             } else if constexpr (PASS == kPassOverdamped) {
-                double mdt = R.mobility * dt;
-                x = __dadd_rn(x, __dmul_rn(fx, mdt));
-                y = __dadd_rn(y, __dmul_rn(fy, mdt));
+                if constexpr (PREC == kPrecFP64) {
+                    x = __dadd_rn(x, __dmul_rn(fx, R.mdt));
+                    y = __dadd_rn(y, __dmul_rn(fy, R.mdt));
+                } else {
+                    // FP32 displacement (relative error 6e-8 of a step), FP64 position
+                    x = __dadd_rn(x, (double)(acc.gx() * R.mdt_f));
+                    y = __dadd_rn(y, (double)(acc.gy() * R.mdt_f));
+                }
             } else if constexpr (PASS == kPassSzabo || PASS == kPassRTP) {
                 int32_t uid = C.uid_cur[s];
                 double theta = C.pol_cur[s];
@@ -648,13 +1074,12 @@ __global__ void __launch_bounds__(256) k_pass(Ctx C, int32_t with_wall_forces) {
                 }
                 C.pol_out[s] = theta;
             }
-            apply_walls(C, rep, R, R.radius, x, y, vx, vy, HAS_VEL);
+            new_cell = walls_and_bin<PREC>(C, rep, R, s, cell, x, y, vx, vy, HAS_VEL);
             C.pos_out[s] = make_double2(x, y);
             if constexpr (HAS_VEL) C.vel_out[s] = make_double2(vx, vy);
             if constexpr (HAS_POL && !(PASS == kPassSzabo || PASS == kPassRTP)) C.pol_out[s] = C.pol_cur[s];
             C.uid_out[s] = C.uid_cur[s];
             C.rep_out[s] = rep;
-            new_cell = cell_of(R, x, y, C.err, s, true);
             cap = R.has_chunks ? R.cap : (1 << 30);
         }
     }

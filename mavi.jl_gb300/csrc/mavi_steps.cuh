@@ -10,18 +10,23 @@ namespace steps {
 
 template <int PREC>
 void sort_permute(MaviSystem* s) {
-    unsigned g = nblocks(s->Ctot);
-    if (s->has_vel) k_sort_permute<PREC, true, false><<<g, kBlock, 0, s->stream>>>(s->C);
-    else if (s->has_pol) k_sort_permute<PREC, false, true><<<g, kBlock, 0, s->stream>>>(s->C);
-    else k_sort_permute<PREC, false, false><<<g, kBlock, 0, s->stream>>>(s->C);
+    unsigned g = nblocks(s->M);
+    if (s->has_vel) k_permute<PREC, true, false><<<g, kBlock, 0, s->stream>>>(s->C);
+    else if (s->has_pol) k_permute<PREC, false, true><<<g, kBlock, 0, s->stream>>>(s->C);
+    else k_permute<PREC, false, false><<<g, kBlock, 0, s->stream>>>(s->C);
+}
+
+template <int PREC>
+void count(MaviSystem* s, int use_guess) {
+    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, use_guess);
 }
 
 template <int PREC, int DYN, int PASS>
 void pass(MaviSystem* s, int with_walls) {
-    unsigned g = nblocks(s->M);
-    if (s->has_vel) k_pass<PREC, DYN, PASS, true, false><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
-    else if (s->has_pol) k_pass<PREC, DYN, PASS, false, true><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
-    else k_pass<PREC, DYN, PASS, false, false><<<g, kBlock, 0, s->stream>>>(s->C, with_walls);
+    unsigned g = nblocks(s->M, kPassThreads);
+    if (s->has_vel) k_pass<PREC, DYN, PASS, true, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+    else if (s->has_pol) k_pass<PREC, DYN, PASS, false, true><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+    else k_pass<PREC, DYN, PASS, false, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
 }
 
 template <int PREC>
@@ -70,7 +75,7 @@ void step_body(MaviSystem* s) {
             record_end(s, MAVI_KERNEL_FORCE);
             record_begin(s, MAVI_KERNEL_UPDATE);
             rings_terms<PREC>(s, 1);
-            k_count<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
+            count<PREC>(s, 1);
             record_end(s, MAVI_KERNEL_UPDATE);
         }
         break;
@@ -112,6 +117,7 @@ void forces_to_user(MaviSystem* s) {
 #define MAVI_DEFINE_STEPS(SUFFIX, PREC)                                                      \
     namespace mavi {                                                                         \
     void sort_permute_##SUFFIX(MaviSystem* s) { steps::sort_permute<PREC>(s); }              \
+    void count_##SUFFIX(MaviSystem* s, int g) { steps::count<PREC>(s, g); }                  \
     void step_body_##SUFFIX(MaviSystem* s) { steps::step_body_dispatch<PREC>(s); }           \
     void forces_only_##SUFFIX(MaviSystem* s, int w) { steps::forces_only<PREC>(s, w); }      \
     void rings_terms_##SUFFIX(MaviSystem* s, int u) { steps::rings_terms<PREC>(s, u); }      \

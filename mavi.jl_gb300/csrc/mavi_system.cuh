@@ -43,7 +43,6 @@ struct MaviSystem {
     std::vector<void*> allocs;
     double2 *pos_user = nullptr, *vel_user = nullptr, *f_user = nullptr;
     double* pol_user = nullptr;
-    int32_t* tile_sum = nullptr;
     double *ke_t = nullptr, *pe_t = nullptr, *ke_r = nullptr, *pe_r = nullptr;
     unsigned long long* d_pairs = nullptr;
     double* noise_cur = nullptr;
@@ -102,13 +101,13 @@ inline unsigned nblocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 
 inline void record_begin(MaviSystem* s, int kind) {
     if (!s->profiling) return;
     int u = s->ev.used[kind];
-    if (u < 4) cudaEventRecord(s->ev.a[kind][u], s->stream);
+    if (u < 4) cudaEventRecordWithFlags(s->ev.a[kind][u], s->stream, cudaEventRecordExternal);
 }
 inline void record_end(MaviSystem* s, int kind) {
     if (!s->profiling) return;
     int u = s->ev.used[kind];
     if (u < 4) {
-        cudaEventRecord(s->ev.b[kind][u], s->stream);
+        cudaEventRecordWithFlags(s->ev.b[kind][u], s->stream, cudaEventRecordExternal);
         s->ev.used[kind] = u + 1;
     }
 }
@@ -123,6 +122,8 @@ inline void collect_profile(MaviSystem* s, const int* used) {
             if (cudaEventElapsedTime(&ms, s->ev.a[k][u], s->ev.b[k][u]) == cudaSuccess) {
                 s->prof.ms[k] += ms;
                 s->prof.launches[k] += 1;
+            } else {
+                cudaGetLastError();   // a missing timing must not poison later error checks
             }
         }
         s->ev.used[k] = 0;
@@ -136,12 +137,16 @@ inline void collect_step_time(MaviSystem* s, int used) {
     if (cudaEventElapsedTime(&ms, s->ev.step_a, s->ev.step_b) == cudaSuccess) {
         s->prof.step_ms += ms;
         s->prof.last_step_ms = ms;
+    } else {
+        cudaGetLastError();
     }
 }
 
 
 // Per-precision launch sequences (mavi_steps_fp64.cu / mavi_steps_mixed.cu).
 void sort_permute_fp64(MaviSystem* s);
+void count_fp64(MaviSystem* s, int use_guess);
+void count_mixed(MaviSystem* s, int use_guess);
 void sort_permute_mixed(MaviSystem* s);
 void step_body_fp64(MaviSystem* s);
 void step_body_mixed(MaviSystem* s);

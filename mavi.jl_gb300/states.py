@@ -21,13 +21,16 @@ def _as_xy(a) -> np.ndarray:
 
 
 class SecondLawState:
-    """Positions and velocities for Newton's second law (src/states.jl:75-101)."""
+    """Positions and velocities for Newton's second law (src/states.jl:75-101).
+
+    ``vel=None`` gives a positions-only state, accepted by the overdamped step
+    only (velocities play no part in it)."""
     kind = abi.MAVI_STATE_SECOND_LAW
 
     def __init__(self, pos, vel):
         self.pos = _as_xy(pos)
-        self.vel = _as_xy(vel)
-        if self.pos.shape != self.vel.shape:
+        self.vel = None if vel is None else _as_xy(vel)
+        if self.vel is not None and self.pos.shape != self.vel.shape:
             raise ValueError("pos and vel must have the same number of particles")
 
     @property

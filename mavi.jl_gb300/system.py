@@ -82,6 +82,8 @@ def get_step_function(system) -> StepFunction:
     from .configs import RunTumbleCfg, SzaboCfg
     if getattr(system, "is_rings", False):
         return rings_step
+    if isinstance(system.state, SecondLawState) and system.state.vel is None:
+        return overdamped_step      # positions-only state: only the overdamped step applies
     if isinstance(system.dynamic_cfg, SzaboCfg):
         return szabo_step
     if isinstance(system.dynamic_cfg, RunTumbleCfg):
@@ -119,7 +121,7 @@ class _Handle:
             s.fill_params(self.params[k], step_kind)
         pos = np.ascontiguousarray(np.concatenate([s.state.pos.reshape(-1) for s in self.systems]))
         vel = pol = types = None
-        if self.systems[0].state.kind == abi.MAVI_STATE_SECOND_LAW:
+        if self.systems[0].state.kind == abi.MAVI_STATE_SECOND_LAW and self.systems[0].state.vel is not None:
             vel = np.ascontiguousarray(np.concatenate([s.state.vel.reshape(-1) for s in self.systems]))
         p0 = self.systems[0].state.pol_array()
         if p0 is not None:
@@ -152,7 +154,7 @@ class _Handle:
         n2 = int(self.slot_offsets[-1])
         pos = np.zeros((n2, 2))
         s0 = self.systems[0].state
-        vel = np.zeros((n2, 2)) if s0.kind == abi.MAVI_STATE_SECOND_LAW else None
+        vel = np.zeros((n2, 2)) if (s0.kind == abi.MAVI_STATE_SECOND_LAW and s0.vel is not None) else None
         pol = np.zeros(int(self.pol_offsets[-1])) if self.pol_offsets[-1] > 0 else None
         self.check(self.lib.mavi_download_state(self.handle, abi.as_dptr(pos), abi.as_dptr(vel), abi.as_dptr(pol)),
                    "mavi_download_state")
@@ -167,7 +169,7 @@ class _Handle:
     def upload(self):
         pos = np.ascontiguousarray(np.concatenate([s.state.pos.reshape(-1) for s in self.systems]))
         vel = pol = None
-        if self.systems[0].state.kind == abi.MAVI_STATE_SECOND_LAW:
+        if self.systems[0].state.kind == abi.MAVI_STATE_SECOND_LAW and self.systems[0].state.vel is not None:
             vel = np.ascontiguousarray(np.concatenate([s.state.vel.reshape(-1) for s in self.systems]))
         if self.systems[0].state.pol_array() is not None:
             pol = np.ascontiguousarray(np.concatenate([s.state.pol_array() for s in self.systems]))
@@ -375,7 +377,7 @@ def kinetic_energy(obj) -> float:
     if isinstance(obj, System):
         return obj.energies()[0]
     v = obj.vel
-    return float(np.sum(v * v) / 2)
+    return 0.0 if v is None else float(np.sum(v * v) / 2)
 
 
 def potential_energy(system: System, pe_mode=abi.MAVI_PE_ALL_PAIRS) -> float:

@@ -52,7 +52,7 @@ def harm_system(pos, L, precision="fp64", use_graph=True):
     n = pos.shape[0]
     dyn = cf.HarmTruncCfg(k_rep=10.0, k_atr=0.0, dist_eq=2.0, dist_max=2.0, mobility=1.0)
     nc = int(L // 2.0)
-    return System(SecondLawState(pos.copy(), np.zeros((n, 2))), cf.SpaceCfg(cf.PeriodicWalls(), cf.RectangleCfg(L, L)),
+    return System(SecondLawState(pos.copy(), None), cf.SpaceCfg(cf.PeriodicWalls(), cf.RectangleCfg(L, L)),
                   dyn, cf.IntCfg(dt=1e-2, chunks_cfg=cf.ChunksCfg(nc, nc),
                                  device=cf.CUDADevice(precision=precision, use_graph=use_graph)))
 

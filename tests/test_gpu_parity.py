@@ -215,3 +215,70 @@ def test_chunk_overflow_reports_error(mg):
     with pytest.raises(mg.MaviError) as e:
         s.calc_forces()
     assert e.value.status == mg.abi.MAVI_ERR_CHUNK_OVERFLOW
+
+
+def test_profiling_events_inside_graph(mg):
+    import ctypes as C
+    s = lj_grid(mg, 20, 20, wall="periodic", use_graph=True)
+    mg.run_system(s, num_steps=2)
+    h = s.handle
+    h.check(h.lib.mavi_profile_enable(h.handle, 1), "profile")
+    h.step(3)
+    p = mg.abi.MaviProfile()
+    h.lib.mavi_profile_read(h.handle, C.byref(p))
+    assert p.steps == 3 and p.step_ms > 0 and p.last_step_ms > 0
+    assert p.launches[mg.abi.MAVI_KERNEL_FORCE] == 3
+    assert p.ms[mg.abi.MAVI_KERNEL_FORCE] > 0
+    h.check(h.lib.mavi_profile_enable(h.handle, 0), "profile off")
+    h.step(2)
+    s.close()
+
+
+def test_overdamped_positions_only_state(mg, orc):
+    """The overdamped step accepts a SecondLawState without velocities."""
+    s = soft_disks(mg, 2048, precision="mixed")
+    s.state.vel = None
+    ref = orc.from_system(s, step_kind=mg.overdamped_step.kind)
+    mg.run_system(s, num_steps=20, step_func=mg.overdamped_step)
+    ref.step(20)
+    assert np.max(np.abs(s.state.pos - ref.state()[0])) < 1e-4
+    s.close()
+
+
+def test_mixed_force_error_relaxed_packing(mg, orc):
+    """Mixed-form force error on a relaxed soft-disk packing (forces small
+    compared with the pair stiffness), normalised by the RMS force."""
+    s = soft_disks(mg, 16384, precision="fp64")
+    mg.run_system(s, num_steps=100, step_func=mg.overdamped_step)
+    pos = s.state.pos.copy()
+    s.close()
+    m = soft_disks(mg, 16384, precision="mixed")
+    m.state.pos[...] = pos
+    ref = orc.from_system(m, step_kind=mg.overdamped_step.kind)
+    err = rel_force_err(m.calc_forces(), ref.forces())
+    assert err < MIXED_TOL, err
+    m.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_staged_gather_equals_global_gather_bitwise(mg, precision):
+    """The warp-staged shared-memory gather and the per-thread global gather
+    sum the same terms in the same order."""
+    out = []
+    for gather in ("staged", "global"):
+        s = soft_disks(mg, 8192, precision=precision)
+        s.int_cfg.device.gather = gather
+        f = s.calc_forces()
+        mg.run_system(s, num_steps=20, step_func=mg.overdamped_step)
+        out.append((f, s.state.pos.copy()))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    l = []
+    for gather in ("staged", "global"):
+        s = lj_grid(mg, 40, 40, wall="periodic", precision=precision)
+        s.int_cfg.device.gather = gather
+        mg.run_system(s, num_steps=20)
+        l.append(s.state.pos.copy())
+        s.close()
+    assert np.array_equal(l[0], l[1])
