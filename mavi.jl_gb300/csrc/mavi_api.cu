@@ -288,21 +288,28 @@ static void fill_fix_pairs(const MaviReplicaParams& p, const DevRep& R, FixPair*
     double inv_u = R.inv_u;
     auto sq = [&](double len) { double v = len * inv_u; return (unsigned long long)std::llround(v * v); };
     for (int t = 0; t < MAVI_MAX_TYPES * MAVI_MAX_TYPES; t++) out[t] = FixPair{};
+    auto bands = [](FixPair& f) {
+        f.cut2_hi = (float)((double)f.cut2 * (1.0 + 1e-6));
+        f.cut2_lo = (float)((double)f.cut2 * (1.0 - 1e-6));
+    };
     const MaviDynamicCfg& d = p.dyn;
     FixPair f{};
     switch (d.kind) {
     case MAVI_DYN_HARM_TRUNC:
         f.cut2 = sq(d.dist_max); f.eq2 = (long long)sq(d.dist_eq); f.eq = (float)(d.dist_eq * inv_u);
         f.k_rep = (float)d.k_rep; f.k_atr = (float)d.k_atr;
+        bands(f);
         out[0] = f;
         break;
     case MAVI_DYN_SZABO:
         f.cut2 = sq(d.r_max); f.eq2 = (long long)sq(d.r_eq); f.eq = (float)(d.r_eq * inv_u);
         f.k_rep = (float)(d.k_rep / (d.r_max - d.r_eq)); f.k_atr = (float)(d.k_adh / d.r_eq);
+        bands(f);
         out[0] = f;
         break;
     case MAVI_DYN_RUN_TUMBLE:
         f.cut2 = sq(std::pow(2.0, 1.0 / 6.0) * d.sigma);
+        bands(f);
         out[0] = f;
         break;
     case MAVI_DYN_RINGS:
@@ -314,6 +321,7 @@ static void fill_fix_pairs(const MaviReplicaParams& p, const DevRep& R, FixPair*
                 g.eq = (float)(p.rings.inter_dist_eq[a][b] * inv_u);
                 g.k_rep = (float)p.rings.inter_k_rep[a][b];
                 g.k_atr = (float)p.rings.inter_k_atr[a][b];
+                bands(g);
                 out[a * MAVI_MAX_TYPES + b] = g;
             }
         break;

@@ -30,7 +30,7 @@ namespace mavi {
 
 constexpr int kFixBits = 28;                       // fixed-point offsets: chunk = 2^28 units
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 4;                          // one int4 per thread
 constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
 constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
 
@@ -41,6 +41,8 @@ struct FixPair {
     long long eq2;             // squared equilibrium distance (dist_eq / r_eq), units^2
     float eq;                  // equilibrium distance, units
     float k_rep, k_atr;        // HarmTrunc constants; Szabo: f_mod below / above r_eq
+    float cut2_hi, cut2_lo;    // cut2 * (1 +- 1e-6): FP32 squared distances beyond / below
+                               // these are certainly outside / inside the cutoff
     float pad;
 };
 
@@ -250,7 +252,7 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
 }
 
 // ===========================================================================
-// exclusive scan of chunk counts -> start (three passes over 2048-chunk tiles)
+// exclusive scan of chunk counts -> start (1024-chunk tiles)
 // ===========================================================================
 __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total) {
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -279,56 +281,6 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total
     return warp_prefix + x - v;
 }
 
-static __global__ void k_scan_reduce(const int32_t* __restrict__ count, int64_t n, int32_t* __restrict__ tile_sum) {
-    __shared__ int smem[32];
-    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
-    int v = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++) v += (base + k < n) ? count[base + k] : 0;
-    int total;
-    block_exclusive_scan(v, smem, total);
-    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
-}
-
-// Single block: exclusive scan of the tile sums, in 1024-wide rounds.
-static __global__ void k_scan_tiles(int32_t* __restrict__ tile_sum, int64_t ntiles, int32_t* __restrict__ start,
-                             int64_t n, int64_t* d_step, int32_t advance) {
-    __shared__ int smem[32];
-    int carry = 0;
-    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
-        int64_t i = b + threadIdx.x;
-        int v = i < ntiles ? tile_sum[i] : 0;
-        int total;
-        int ex = block_exclusive_scan(v, smem, total);
-        if (i < ntiles) tile_sum[i] = carry + ex;
-        carry += total;
-    }
-    if (threadIdx.x == 0) {
-        start[n] = carry;
-        if (advance) d_step[0] += 1;
-    }
-}
-
-static __global__ void k_scan_apply(const int32_t* __restrict__ count, int64_t n, const int32_t* __restrict__ tile_off,
-                             int32_t* __restrict__ start) {
-    __shared__ int smem[32];
-    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
-    int v[kScanItems];
-    int sum = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        v[k] = (base + k < n) ? count[base + k] : 0;
-        sum += v[k];
-    }
-    int total;
-    int ex = block_exclusive_scan(sum, smem, total) + tile_off[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        if (base + k < n) start[base + k] = ex;
-        ex += v[k];
-    }
-}
-
 // Single-kernel exclusive scan: the histogram already accumulated each tile's
 // total, so every block sums the tiles before its own, scans its tile and
 // clears the counts it consumed (the next histogram starts from zero).
@@ -339,23 +291,30 @@ static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int3
     for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
     int tile_off;
     block_exclusive_scan(pre, smem, tile_off);
-    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
-    int sum = 0;
+    const bool full4 = base + kScanItems <= n;   // count is 16-byte aligned and base a multiple of 4
+    if (full4) {
+        int4 q = *reinterpret_cast<const int4*>(count + base);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        v[k] = (base + k < n) ? count[base + k] : 0;
-        sum += v[k];
+        for (int k = 0; k < kScanItems; k++) v[k] = (base + k < n) ? count[base + k] : 0;
     }
+    int sum = v[0] + v[1] + v[2] + v[3];
     int total;
     int ex = block_exclusive_scan(sum, smem, total) + tile_off;
+    int4 o;
+    o.x = ex; o.y = ex + v[0]; o.z = o.y + v[1]; o.w = o.z + v[2];
+    if (full4) {
+        // start has n + 1 entries and the same alignment as count
+        *reinterpret_cast<int4*>(start + base) = o;
+        *reinterpret_cast<int4*>(count + base) = make_int4(0, 0, 0, 0);
+    } else {
+        const int ov[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        if (base + k < n) {
-            start[base + k] = ex;
-            count[base + k] = 0;
-        }
-        ex += v[k];
+        for (int k = 0; k < kScanItems; k++)
+            if (base + k < n) { start[base + k] = ov[k]; count[base + k] = 0; }
     }
     if (threadIdx.x == 0) {
         if (blockIdx.x == gridDim.x - 1) start[n] = tile_off + total;
@@ -467,41 +426,54 @@ __device__ __forceinline__ float u64_to_f32(unsigned long long v) {
 }
 
 // Mixed-form pair laws on exact integer differences (units u of the replica).
-// dxi, dyi are int32 (|d| < 2^31 units = 8 chunks); d2 = dxi^2 + dyi^2 is
-// exact in 64 bits. Returns the force components on i.
+// dxi, dyi are int32 (|d| < 2^31 units = 8 chunks). The cutoff is tested on
+// the FP32 squared distance (relative error < 3e-7) against a 1e-6 band, and
+// only pairs inside the band use the exact int64 squared distance; the
+// cancelling term of the harmonic laws (dist_eq^2 - d^2) is always formed
+// exactly in int64. Returns the force components on i.
 template <int DYN>
 __device__ __forceinline__ void pair_fixed(const DevRep& R, const FixPair& fp, int32_t dxi, int32_t dyi,
-                                           unsigned long long d2, float& fx, float& fy) {
+                                           float& fx, float& fy) {
     fx = 0.f;
     fy = 0.f;
-    if constexpr (DYN == MAVI_DYN_HARM_TRUNC || DYN == MAVI_DYN_RINGS) {
-        // f = k (1/d - 1/deq) dr = k (deq^2 - d^2) / (d deq (deq + d)) dr
-        if (d2 > fp.cut2) return;
-        long long D = fp.eq2 - (long long)d2;
-        float k = D > 0 ? fp.k_rep : fp.k_atr;
-        float du = sqrtf(u64_to_f32(d2));
-        float sc = __fdividef(k * i64_to_f32(D), du * fp.eq * (fp.eq + du));
-        fx = sc * (float)dxi;
-        fy = sc * (float)dyi;
-    } else if constexpr (DYN == MAVI_DYN_SZABO) {
-        // f = -f_mod (d - r_eq) dr = -f_mod (d^2 - r_eq^2)/(d + r_eq) dr
-        if (d2 > fp.cut2) return;
-        long long D = (long long)d2 - fp.eq2;
-        float fm = D > 0 ? fp.k_atr : fp.k_rep;
-        float du = sqrtf(u64_to_f32(d2));
-        float sc = __fdividef(-fm * i64_to_f32(D) * R.u2_f, du + fp.eq);
-        fx = sc * (float)dxi;
-        fy = sc * (float)dyi;
-    } else {  // LenJones / RunTumble (WCA)
-        if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
-            if (d2 > fp.cut2) return;
-        }
-        float r2 = u64_to_f32(d2) * R.u2_f;
+    const float dxf = (float)dxi, dyf = (float)dyi;
+    const float d2f = fmaf(dxf, dxf, dyf * dyf);
+    if constexpr (DYN == MAVI_DYN_LEN_JONES) {
+        float r2 = d2f * R.u2_f;
         float ir2 = __frcp_rn(r2);
         float ir6 = ir2 * ir2 * ir2;
         float sc = ir6 * ir2 * (R.pf[0] * ir6 - R.pf[1]) * R.u_f;
-        fx = sc * (float)dxi;
-        fy = sc * (float)dyi;
+        fx = sc * dxf;
+        fy = sc * dyf;
+        return;
+    }
+    if (d2f > fp.cut2_hi) return;
+    const unsigned long long d2 = (unsigned long long)((long long)dxi * dxi) + (unsigned long long)((long long)dyi * dyi);
+    if (d2f >= fp.cut2_lo && d2 > fp.cut2) return;
+    if constexpr (DYN == MAVI_DYN_HARM_TRUNC || DYN == MAVI_DYN_RINGS) {
+        // f = k (1/d - 1/deq) dr = k (deq^2 - d^2) / (d deq (deq + d)) dr
+        const long long D = fp.eq2 - (long long)d2;
+        const float k = D > 0 ? fp.k_rep : fp.k_atr;
+        const float r = rsqrtf(d2f);
+        const float d = d2f * r;
+        const float sc = __fdividef(k * i64_to_f32(D) * r, fp.eq * (fp.eq + d));
+        fx = sc * dxf;
+        fy = sc * dyf;
+    } else if constexpr (DYN == MAVI_DYN_SZABO) {
+        // f = -f_mod (d - r_eq) dr = -f_mod (d^2 - r_eq^2)/(d + r_eq) dr
+        const long long D = (long long)d2 - fp.eq2;
+        const float fm = D > 0 ? fp.k_atr : fp.k_rep;
+        const float d = d2f * rsqrtf(d2f);
+        const float sc = __fdividef(-fm * i64_to_f32(D) * R.u2_f, d + fp.eq);
+        fx = sc * dxf;
+        fy = sc * dyf;
+    } else {  // RunTumble (WCA) inside its cutoff
+        float r2 = d2f * R.u2_f;
+        float ir2 = __frcp_rn(r2);
+        float ir6 = ir2 * ir2 * ir2;
+        float sc = ir6 * ir2 * (R.pf[0] * ir6 - R.pf[1]) * R.u_f;
+        fx = sc * dxf;
+        fy = sc * dyf;
     }
 }
 
@@ -594,7 +566,6 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
         if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
         if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
     }
-    unsigned long long d2 = (unsigned long long)((long long)dxi * dxi) + (unsigned long long)((long long)dyi * dyi);
     float fx, fy;
     if constexpr (DYN == MAVI_DYN_RINGS) {
         RingInfo o = ring_info(C, R, uq);
@@ -605,9 +576,9 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
         }
         FixPair fp = me.fixr[me.ri.type * MAVI_MAX_TYPES + o.type];
         if (same) fp.k_atr = 0.f;
-        pair_fixed<DYN>(R, fp, dxi, dyi, d2, fx, fy);
+        pair_fixed<DYN>(R, fp, dxi, dyi, fx, fy);
     } else {
-        pair_fixed<DYN>(R, me.fp0, dxi, dyi, d2, fx, fy);
+        pair_fixed<DYN>(R, me.fp0, dxi, dyi, fx, fy);
     }
     acc.add(fx, fy);
 }
@@ -657,26 +628,44 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
 
 // ---------------------------------------------------------------------------
 // Warp-staged gather. The 32 particles of a warp are consecutive in chunk
-// order, so they sit in a short run of rows of one (or two) chunk columns.
-// For each column present, the warp loads the chunk boundaries of the window
-// rows [rmin-1, rmax+1] of the three neighbouring columns, then copies the
-// particles of those rows into shared memory with coalesced loads, and each
-// lane sums its terms from shared memory — a handful of memory round trips
-// per warp instead of ~18 dependent loads per lane. Windows that do not fit
-// fall back to the global gather (same order, bitwise-identical result).
+// order, so they sit in a short run of rows [rmin, rmax] of one (or two)
+// chunk columns. For each column present, the rows [rmin-1, rmax+1] of the
+// three neighbouring columns are at most two contiguous particle ranges each
+// (two when a periodic window wraps): the warp copies these <= 6 segments
+// into shared memory with coalesced loads, and each lane then reads its own
+// neighbour rows there, mapping global particle indices through the segment
+// table. Windows that do not fit fall back to the global gather (same terms
+// in the same order, bitwise-identical sums).
 // ---------------------------------------------------------------------------
-constexpr int kStageRows = 64;     // rows in a window
 constexpr int kStageParts = 256;   // staged particles per window
 constexpr int kPassThreads = 128;
 constexpr int kPassWarps = kPassThreads / 32;
 
+constexpr int kStageRows = 64;     // window rows per column
+
 template <int PREC, int DYN> struct Stage {
     typename PartOf<PREC>::T part[kStageParts];
     int32_t uid[DYN == MAVI_DYN_RINGS ? kStageParts : 1];
-    int32_t gb[3 * kStageRows];    // global first particle of (column k, window row w)
-    int32_t rn[3 * kStageRows];    // particles in it
-    int32_t rb[3 * kStageRows];    // first shared-memory slot
+    int32_t rbeg[3][kStageRows];   // global first particle of window row w of column k
+    int32_t rend[3][kStageRows];   // one past its last particle
 };
+
+// Element j of a 6-entry register table (select chain: no local memory).
+__device__ __forceinline__ int32_t pick6(const int32_t (&a)[6], int j) {
+    int32_t v = a[0];
+#pragma unroll
+    for (int t = 1; t < 6; t++) v = (j == t) ? a[t] : v;
+    return v;
+}
+
+// Shared-memory slot of global particle index g of column k (segments 2k and
+// 2k+1; g lies in one of them).
+__device__ __forceinline__ int seg_map(const int32_t (&sb)[6], const int32_t (&se)[6], const int32_t (&base)[6],
+                                       int k, int32_t g) {
+    int j = 2 * k;
+    if (!(g >= pick6(sb, j) && g < pick6(se, j))) j++;
+    return pick6(base, j) + (g - pick6(sb, j));
+}
 
 template <int PREC, int DYN>
 __device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s, int32_t rep, const DevRep& R,
@@ -700,22 +689,25 @@ __device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s,
     }
     unsigned pending = (uniform && C.gather_mode == 0) ? __ballot_sync(full, want) : 0u;
     while (pending) {
-        int leader = __ffs(pending) - 1;
-        int ccur = __shfl_sync(full, col, leader);
-        bool act = ((pending >> lane) & 1u) && col == ccur;
-        unsigned amask = __ballot_sync(full, act);
-        int rmin = __reduce_min_sync(full, act ? row : 0x7fffffff);
-        int rmax = __reduce_max_sync(full, act ? row : -0x7fffffff);
-        const int W = rmax - rmin + 3;
-        // R is the replica of every active lane (uniform window)
+        const int leader = __ffs(pending) - 1;
+        const int ccur = __shfl_sync(full, col, leader);
+        const bool act = ((pending >> lane) & 1u) && col == ccur;
+        const unsigned amask = __ballot_sync(full, act);
+        const int rmin = __reduce_min_sync(full, act ? row : 0x7fffffff);
+        const int rmax = __reduce_max_sync(full, act ? row : -0x7fffffff);
+        // the replica of every active lane (windows are replica-uniform)
         const int nrows = __shfl_sync(full, R.rows, leader), ncols = __shfl_sync(full, R.cols, leader);
         const int periodic = __shfl_sync(full, R.periodic, leader);
         const long long c0 = __shfl_sync(full, R.c0, leader);
+        const int lo = rmin - 1, hi = rmax + 1;
+        const int W = hi - lo + 1;
         bool ok = W <= kStageRows && (!periodic || W <= nrows);
         if (ok) {
-            for (int q = lane; q < 3 * W; q += 32) {
-                int k = q / W, w = q - k * W;
-                int ncol = ccur + k - 1, r = rmin - 1 + w;
+            // chunk boundaries of the window rows of the three columns
+            for (int q = lane; q < 3 * kStageRows; q += 32) {
+                const int k = q / kStageRows, w = q - k * kStageRows;
+                if (w >= W) continue;
+                int ncol = ccur + k - 1, r = lo + w;
                 bool inside = true;
                 if (periodic) {
                     ncol = ncol < 0 ? ncol + ncols : (ncol >= ncols ? ncol - ncols : ncol);
@@ -723,67 +715,108 @@ __device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s,
                 } else {
                     inside = ncol >= 0 && ncol < ncols && r >= 0 && r < nrows;
                 }
-                int32_t b = 0, n = 0;
+                int32_t b = 0, e = 0;
                 if (inside) {
-                    long long ch = c0 + (long long)ncol * nrows + r;
+                    const long long ch = c0 + (long long)ncol * nrows + r;
                     b = C.start[ch];
-                    n = C.start[ch + 1] - b;
+                    e = C.start[ch + 1];
                 }
-                st.gb[q] = b;
-                st.rn[q] = n;
+                st.rbeg[k][w] = b;
+                st.rend[k][w] = e;
             }
-            __syncwarp();
-            // exclusive scan of the row counts -> shared-memory slots
-            const int per = (3 * W + 31) / 32;
-            const int q0 = lane * per;
-            int local = 0;
-            for (int t = 0; t < per; t++) local += (q0 + t < 3 * W) ? st.rn[q0 + t] : 0;
-            int incl = local;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(full, incl, o);
-                if (lane >= o) incl += y;
-            }
-            int ex = incl - local;
-            const int total = __shfl_sync(full, incl, 31);
-            for (int t = 0; t < per; t++) {
-                int q = q0 + t;
-                if (q < 3 * W) { st.rb[q] = ex; ex += st.rn[q]; }
-            }
-            __syncwarp();
-            ok = total <= kStageParts;
-            if (ok) {
-                // row by row: a lane copies whole rows (rows are short and
-                // consecutive rows are consecutive in memory)
-                for (int q = lane; q < 3 * W; q += 32) {
-                    const int b = st.rb[q], g = st.gb[q], n = st.rn[q];
-                    for (int m = 0; m < n; m++) {
-                        st.part[b + m] = P[g + m];
-                        if constexpr (DYN == MAVI_DYN_RINGS) st.uid[b + m] = C.uid_cur[g + m];
-                    }
-                }
-            }
-            __syncwarp();
         }
+        // segment j = 2k + {0: main, 1: wrapped part}: global [sb, se)
+        int32_t sbj = 0, sej = 0;
+        if (lane < 6) {
+            const int k = lane >> 1, part = lane & 1;
+            int ncol = ccur + k - 1;
+            bool colok = true;
+            if (periodic) ncol = ncol < 0 ? ncol + ncols : (ncol >= ncols ? ncol - ncols : ncol);
+            else colok = ncol >= 0 && ncol < ncols;
+            int ra, rb;   // row range of this segment, empty when ra > rb
+            if (periodic) {
+                if (lo < 0) { if (part == 0) { ra = 0; rb = hi; } else { ra = nrows + lo; rb = nrows - 1; } }
+                else if (hi >= nrows) { if (part == 0) { ra = lo; rb = nrows - 1; } else { ra = 0; rb = hi - nrows; } }
+                else { ra = part == 0 ? lo : 1; rb = part == 0 ? hi : 0; }
+            } else {
+                ra = part == 0 ? max(lo, 0) : 1;
+                rb = part == 0 ? min(hi, nrows - 1) : 0;
+            }
+            if (colok && ra <= rb) {
+                long long cb = c0 + (long long)ncol * nrows;
+                sbj = C.start[cb + ra];
+                sej = C.start[cb + rb + 1];
+            }
+        }
+        int32_t sb[6], se[6], base[6];
+        int total = 0;
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+            sb[j] = __shfl_sync(full, sbj, j);
+            se[j] = __shfl_sync(full, sej, j);
+            base[j] = total;
+            total += se[j] - sb[j];
+        }
+        ok = ok && total <= kStageParts;
+        if (ok) {
+            for (int idx = lane; idx < total; idx += 32) {
+                // segment j: the number of segment ends at or below idx
+                int j = 0;
+#pragma unroll
+                for (int t = 0; t < 5; t++) j += idx >= base[t] + (se[t] - sb[t]) ? 1 : 0;
+                const int32_t g = pick6(sb, j) + (idx - pick6(base, j));
+                st.part[idx] = P[g];
+                if constexpr (DYN == MAVI_DYN_RINGS) st.uid[idx] = C.uid_cur[g];
+            }
+        }
+        __syncwarp();
         if (act) {
             if (ok) {
-                const int wme = row - rmin + 1;
 #pragma unroll 1
                 for (int k = 0; k < 3; k++) {
                     const int dc = k - 1;
-                    const bool cw = periodic && (ccur + dc < 0 || ccur + dc >= ncols);
-#pragma unroll 1
-                    for (int dr = -1; dr <= 1; dr++) {
-                        const int q = k * W + wme + dr;
-                        const bool rw = periodic && (row + dr < 0 || row + dr >= nrows);
-                        const bool mi = R.min_image && (cw || rw || R.mi_small);
-                        const int b = st.rb[q], e = b + st.rn[q];
-                        const int self = (dc == 0 && dr == 0) ? b + (int)(s - st.gb[q]) : -1;
+                    const int ncol = ccur + dc;
+                    bool cw = false;
+                    if (periodic) cw = ncol < 0 || ncol >= ncols;
+                    else if (ncol < 0 || ncol >= ncols) continue;
+                    const bool mi_c = R.min_image && (cw || R.mi_small);
+                    const int32_t shx = -dc * R.sx_i;
+                    const int w = row - lo;
+                    if (row >= 1 && row + 1 < nrows) {
+                        // rows row-1..row+1 are consecutive chunks: one contiguous range
+                        const int32_t g0 = st.rbeg[k][w - 1], g1 = st.rbeg[k][w];
+                        const int32_t g2 = st.rbeg[k][w + 1], g3 = st.rend[k][w + 1];
+                        if (g3 == g0) continue;
+                        const int b = seg_map(sb, se, base, k, g0);
+                        const int b1 = b + (g1 - g0), b2 = b + (g2 - g0), e = b + (g3 - g0);
+                        const int self = (dc == 0) ? b1 + (int)(s - g1) : -1;
+#pragma unroll 2
                         for (int idx = b; idx < e; idx++) {
                             if (idx == self) continue;
+                            const int dr = idx < b1 ? -1 : (idx < b2 ? 0 : 1);
                             int32_t uq = 0;
                             if constexpr (DYN == MAVI_DYN_RINGS) uq = st.uid[idx];
-                            pair_term<DYN>(C, R, rep, me, st.part[idx], uq, -dc * R.sx_i, dr * R.sy_i, mi, acc);
+                            pair_term<DYN>(C, R, rep, me, st.part[idx], uq, shx, dr * R.sy_i, mi_c, acc);
+                        }
+                    } else {
+#pragma unroll 1
+                        for (int dr = -1; dr <= 1; dr++) {
+                            int r = row + dr;
+                            bool rw = false;
+                            if (periodic) rw = r < 0 || r >= nrows;
+                            else if (r < 0 || r >= nrows) continue;
+                            const int32_t g0 = st.rbeg[k][w + dr], g1 = st.rend[k][w + dr];
+                            if (g1 == g0) continue;
+                            const int b = seg_map(sb, se, base, k, g0);
+                            const int e = b + (g1 - g0);
+                            const int self = (dc == 0 && dr == 0) ? b + (int)(s - g0) : -1;
+                            const bool mi = mi_c || (R.min_image && rw);
+                            for (int idx = b; idx < e; idx++) {
+                                if (idx == self) continue;
+                                int32_t uq = 0;
+                                if constexpr (DYN == MAVI_DYN_RINGS) uq = st.uid[idx];
+                                pair_term<DYN>(C, R, rep, me, st.part[idx], uq, shx, dr * R.sy_i, mi, acc);
+                            }
                         }
                     }
                 }
@@ -973,7 +1006,7 @@ __device__ __forceinline__ int64_t walls_and_bin(const Ctx& C, int32_t rep, cons
 }
 
 template <int PREC, int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
-__global__ void __launch_bounds__(kPassThreads, 4) k_pass(Ctx C, int32_t with_wall_forces) {
+__global__ void __launch_bounds__(kPassThreads, PREC == kPrecFP64 ? 4 : 8) k_pass(Ctx C, int32_t with_wall_forces) {
     __shared__ Stage<PREC, DYN> stage[kPassWarps];
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = s < C.M;
@@ -983,6 +1016,8 @@ __global__ void __launch_bounds__(kPassThreads, 4) k_pass(Ctx C, int32_t with_wa
     const DevRep& R = C.reps[rep];
     int32_t cell = valid ? C.cell_cur[s] : 0;
     const double2* P = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    // own FP64 position, loaded early so its latency overlaps the gather
+    const double2 p = valid ? P[s] : make_double2(0.0, 0.0);
     Acc<PREC, DYN> acc;
     if constexpr (PREC == kPrecFP64) {
         gather_warp<PREC, DYN>(C, valid, s, rep, R, cell, P, stage[threadIdx.x >> 5], acc);
@@ -992,7 +1027,6 @@ __global__ void __launch_bounds__(kPassThreads, 4) k_pass(Ctx C, int32_t with_wa
     }
     if (valid) {
         double fx = (double)acc.gx(), fy = (double)acc.gy();
-        double2 p = P[s];
         bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
         if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
         const double dt = R.dt;
