@@ -19,5 +19,7 @@ from .system import (
 )
 from .init_states import fixed_speed_vel, maxwell_vel, random_vel, rectangular_grid
 from . import rings
+from . import replicas
+from .replicas import my_replicas, shard_replicas
 
 __all__ = [n for n in dir() if not n.startswith("_")]

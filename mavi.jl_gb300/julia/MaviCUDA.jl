@@ -1,0 +1,283 @@
+"""
+    MaviCUDA
+
+Julia binding of libmavi_cuda.so (include/mavi_cuda.h): routes Mavi.jl's step
+loop for a `System` to the GPU.
+
+The hook is the reference's device mode (`IntCfg.device`, src/configs.jl:471-475):
+a system whose `int_cfg.device isa CUDADevice` gets a GPU step function from
+`get_step_function` (src/integration.jl:537-548), and `run_system`
+(src/run_system.jl:7-23) works unchanged. State arrays are passed to the
+library by pointer: `Vector{SVector{2,Float64}}` is the interleaved
+[x1, y1, x2, y2, ...] layout the ABI takes.
+
+The GPU copy of the state is authoritative while stepping; `sync!(system)`
+copies it back into `system.state` (done automatically by `run_system` here and
+by `gpu_run!`). Indices crossing the ABI are 0-based.
+"""
+module MaviCUDA
+
+using StaticArrays
+import Mavi
+using Mavi.Configs: DeviceMode, RectangleCfg, CircleCfg, LinesCfg, RigidWalls, PeriodicWalls,
+    SlipperyWalls, PotentialWalls, ManyWalls, ManyGeometries, HarmTruncCfg, LenJonesCfg, SzaboCfg,
+    RunTumbleCfg, has_chunks
+using Mavi.States: SecondLawState, SelfPropelledState
+
+const libmavi = get(ENV, "MAVI_CUDA_LIB", joinpath(@__DIR__, "..", "lib", "libmavi_cuda.so"))
+
+# ---- constants (include/mavi_cuda.h) ---------------------------------------
+const MAVI_OK = Cint(0)
+const STATE_SECOND_LAW, STATE_SELF_PROPELLED, STATE_RINGS = Int32(0), Int32(1), Int32(2)
+const DYN_HARM_TRUNC, DYN_LEN_JONES, DYN_SZABO, DYN_RUN_TUMBLE, DYN_RINGS = Int32.(0:4)
+const STEP_NEWTON, STEP_SZABO, STEP_RTP, STEP_RINGS, STEP_OVERDAMPED = Int32.(0:4)
+const GEOM_RECTANGLE, GEOM_CIRCLE, GEOM_LINES = Int32.(0:2)
+const WALL_RIGID, WALL_PERIODIC, WALL_SLIPPERY, WALL_POTENTIAL = Int32.(0:3)
+const PREC_FP64, PREC_MIXED = Int32(0), Int32(1)
+const NOISE_DEVICE, NOISE_INJECTED = Int32(0), Int32(1)
+const MAX_SPACES, MAX_LINES, MAX_TYPES = 4, 16, 4
+
+# ---- C structs (same field order and types as the header) -------------------
+struct CSpace
+    wall::Int32; geometry::Int32
+    length::Float64; height::Float64; bl_x::Float64; bl_y::Float64
+    radius::Float64; cx::Float64; cy::Float64
+    num_lines::Int32; has_bbox::Int32
+    lines::NTuple{4 * MAX_LINES, Float64}
+    bbox_length::Float64; bbox_height::Float64; bbox_bl_x::Float64; bbox_bl_y::Float64
+    pot_kind::Int32; pot_mode::Int32
+    pot_params::NTuple{4, Float64}
+end
+
+struct CRingsCfg
+    num_types::Int32; num_rings::Int32; nmax::Int32; _pad0::Int32
+    num_particles::NTuple{MAX_TYPES, Int32}
+    p0::NTuple{MAX_TYPES, Float64}; relax_time::NTuple{MAX_TYPES, Float64}
+    vo::NTuple{MAX_TYPES, Float64}; mobility::NTuple{MAX_TYPES, Float64}
+    rot_diff::NTuple{MAX_TYPES, Float64}; k_area::NTuple{MAX_TYPES, Float64}
+    k_spring::NTuple{MAX_TYPES, Float64}; l_spring::NTuple{MAX_TYPES, Float64}
+    k_bend::NTuple{MAX_TYPES, Float64}
+    inter::NTuple{4 * MAX_TYPES * MAX_TYPES, Float64}   # k_rep, k_atr, dist_eq, dist_max matrices
+end
+
+struct CDynamicCfg
+    kind::Int32; _pad0::Int32
+    k_rep::Float64; k_atr::Float64; dist_eq::Float64; dist_max::Float64
+    sigma::Float64; epsilon::Float64
+    vo::Float64; mobility::Float64; relax_time::Float64; k_adh::Float64; r_eq::Float64
+    r_max::Float64; rot_diff::Float64; tumble_rate::Float64
+end
+
+struct CReplicaParams
+    num_particles::Int64
+    state_kind::Int32; step_kind::Int32; num_spaces::Int32
+    chunk_cols::Int32; chunk_rows::Int32; _pad0::Int32
+    dt::Float64
+    spaces::NTuple{MAX_SPACES, CSpace}
+    dyn::CDynamicCfg
+    rings::CRingsCfg
+end
+
+struct COptions
+    precision::Int32; noise_mode::Int32; seed::UInt64
+    device::Int32; use_graph::Int32; block_size::Int32; gather_mode::Int32
+end
+
+"""
+    CUDADevice(; precision=:fp64, device=0, seed=0)
+
+Device mode for `IntCfg(device=CUDADevice())`. `precision = :fp64` runs every
+operation in double (the drop-in); `:mixed` runs the pair loop in FP32 on
+chunk-relative offsets with FP64 update, wrap and binning.
+"""
+Base.@kwdef struct CUDADevice <: DeviceMode
+    precision::Symbol = :fp64
+    device::Int = 0
+    seed::UInt64 = 0
+end
+
+# ---- packing -----------------------------------------------------------------
+zspace() = CSpace(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> 0.0, 4MAX_LINES), 0, 0, 0, 0, 0, 0,
+                  (0.0, 0.0, 0.0, 0.0))
+
+function cspace(wall, geom)
+    s = zspace()
+    wcode = wall isa RigidWalls ? WALL_RIGID : wall isa PeriodicWalls ? WALL_PERIODIC :
+            wall isa SlipperyWalls ? WALL_SLIPPERY : wall isa PotentialWalls ? WALL_POTENTIAL :
+            error("unsupported wall type $(typeof(wall))")
+    pk, pm, pp = Int32(0), Int32(0), (0.0, 0.0, 0.0, 0.0)
+    if wall isa PotentialWalls
+        p = wall.potential
+        pm = Int32(wall.mode isa Mavi.Configs.Outside ? 0 : wall.mode isa Mavi.Configs.Inside ? 1 : 2)
+        if p isa HarmTruncCfg
+            pk, pp = DYN_HARM_TRUNC, (p.k_rep, p.k_atr, p.dist_eq, p.dist_max)
+        else
+            pk, pp = DYN_LEN_JONES, (p.sigma, p.epsilon, 0.0, 0.0)
+        end
+    end
+    if geom isa RectangleCfg
+        return CSpace(wcode, GEOM_RECTANGLE, geom.length, geom.height, geom.bottom_left[1],
+                      geom.bottom_left[2], 0, 0, 0, 0, 0, s.lines, 0, 0, 0, 0, pk, pm, pp)
+    elseif geom isa CircleCfg
+        return CSpace(wcode, GEOM_CIRCLE, 0, 0, 0, 0, geom.radius, geom.center[1], geom.center[2],
+                      0, 0, s.lines, 0, 0, 0, 0, pk, pm, pp)
+    elseif geom isa LinesCfg
+        n = length(geom.lines)
+        n <= MAX_LINES || error("at most $MAX_LINES lines")
+        flat = zeros(4MAX_LINES)
+        for (k, l) in enumerate(geom.lines)
+            flat[4k-3:4k] .= (l.p1[1], l.p1[2], l.p2[1], l.p2[2])
+        end
+        bb = geom.bbox
+        hb = isnothing(bb) ? 0 : 1
+        b = isnothing(bb) ? (0.0, 0.0, 0.0, 0.0) : (bb.length, bb.height, bb.bottom_left[1], bb.bottom_left[2])
+        return CSpace(wcode, GEOM_LINES, 0, 0, 0, 0, 0, 0, 0, n, hb, Tuple(flat), b..., pk, pm, pp)
+    end
+    error("unsupported geometry $(typeof(geom))")
+end
+
+function cspaces(space_cfg)
+    w, g = space_cfg.wall_type, space_cfg.geometry_cfg
+    pairs = w isa ManyWalls ? collect(zip(w.list, g.list)) : [(w, g)]
+    length(pairs) <= MAX_SPACES || error("at most $MAX_SPACES (wall, geometry) entries")
+    sp = [cspace(a, b) for (a, b) in pairs]
+    while length(sp) < MAX_SPACES
+        push!(sp, zspace())
+    end
+    return Tuple(sp), Int32(length(pairs))
+end
+
+function cdynamic(cfg)
+    z = 0.0
+    cfg isa HarmTruncCfg && return CDynamicCfg(DYN_HARM_TRUNC, 0, cfg.k_rep, cfg.k_atr, cfg.dist_eq,
+                                               cfg.dist_max, z, z, z, 1.0, z, z, z, z, z, z)
+    cfg isa LenJonesCfg && return CDynamicCfg(DYN_LEN_JONES, 0, z, z, z, z, cfg.sigma, cfg.epsilon,
+                                              z, 1.0, z, z, z, z, z, z)
+    cfg isa SzaboCfg && return CDynamicCfg(DYN_SZABO, 0, cfg.k_rep, z, z, z, z, z, cfg.vo, cfg.mobility,
+                                           cfg.relax_time, cfg.k_adh, cfg.r_eq, cfg.r_max, cfg.rot_diff, z)
+    cfg isa RunTumbleCfg && return CDynamicCfg(DYN_RUN_TUMBLE, 0, z, z, z, z, cfg.sigma, cfg.epsilon,
+                                               cfg.vo, 1.0, z, z, z, z, z, cfg.tumble_rate)
+    error("unsupported dynamic config $(typeof(cfg)) (rings: use the Python host API or extend this shim)")
+end
+
+const ZRINGS = CRingsCfg(0, 0, 0, 0, ntuple(_ -> Int32(0), MAX_TYPES), ntuple(_ -> ntuple(_ -> 0.0, MAX_TYPES), 9)...,
+                         ntuple(_ -> 0.0, 4 * MAX_TYPES * MAX_TYPES))
+
+function step_kind(system)
+    cfg = system.dynamic_cfg
+    cfg isa SzaboCfg && return STEP_SZABO
+    cfg isa RunTumbleCfg && return STEP_RTP
+    return STEP_NEWTON
+end
+
+function replica_params(system, kind=step_kind(system))
+    st = system.state
+    sp, nsp = cspaces(system.space_cfg)
+    cc = system.int_cfg.chunks_cfg
+    cols, rows = has_chunks(system.int_cfg) ? (Int32(cc.num_cols), Int32(cc.num_rows)) : (Int32(0), Int32(0))
+    sk = st isa SecondLawState ? STATE_SECOND_LAW : STATE_SELF_PROPELLED
+    CReplicaParams(length(st.pos), sk, kind, nsp, cols, rows, 0, system.int_cfg.dt, sp,
+                   cdynamic(system.dynamic_cfg), ZRINGS)
+end
+
+# ---- handles -------------------------------------------------------------------
+mutable struct Handle
+    ptr::Ptr{Cvoid}
+end
+
+const HANDLES = IdDict{Any, Handle}()
+
+function check(st, what, h=C_NULL)
+    st == MAVI_OK && return
+    msg = unsafe_string(ccall((:mavi_status_string, libmavi), Cstring, (Cint,), st))
+    if h != C_NULL
+        buf = zeros(UInt8, 512)
+        ccall((:mavi_last_error, libmavi), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int32), h, buf, 512)
+        msg *= ": " * unsafe_string(pointer(buf))
+    end
+    # the reference raises BoundsError / throws on the same conditions
+    error("$what: $msg")
+end
+
+function handle!(system)
+    haskey(HANDLES, system) && return HANDLES[system].ptr
+    dev = system.int_cfg.device
+    opt = COptions(dev.precision == :mixed ? PREC_MIXED : PREC_FP64, NOISE_DEVICE, dev.seed,
+                   dev.device, 1, 0, 0)
+    params = Ref(replica_params(system))
+    st = system.state
+    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
+    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve st begin
+        check(ccall((:mavi_create, libmavi), Cint,
+                    (Ref{COptions}, Int32, Ref{CReplicaParams}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                     Ptr{Int32}, Ref{Ptr{Cvoid}}),
+                    opt, 1, params, pointer(st.pos), vel, pol, C_NULL, out), "mavi_create")
+    end
+    h = Handle(out[])
+    finalizer(x -> ccall((:mavi_destroy, libmavi), Cint, (Ptr{Cvoid},), x.ptr), h)
+    HANDLES[system] = h
+    return h.ptr
+end
+
+"Copy the GPU state and the time back into `system` (user particle order)."
+function sync!(system)
+    h = handle!(system)
+    st = system.state
+    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
+    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    GC.@preserve st check(ccall((:mavi_download_state, libmavi), Cint,
+                                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                                h, pointer(st.pos), vel, pol), "mavi_download_state", h)
+    n, t = Ref{Int64}(0), Ref{Float64}(0)
+    check(ccall((:mavi_get_time, libmavi), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Float64}), h, n, t),
+          "mavi_get_time", h)
+    system.time_info.num_steps = n[]
+    system.time_info.time = t[]
+    return system
+end
+
+"Push `system.state` to the GPU (after the caller edited it on the host)."
+function upload!(system)
+    h = handle!(system)
+    st = system.state
+    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
+    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    GC.@preserve st check(ccall((:mavi_upload_state, libmavi), Cint,
+                                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                                h, pointer(st.pos), vel, pol), "mavi_upload_state", h)
+end
+
+"Advance `num_steps` steps on the GPU and copy the state back once."
+function gpu_run!(system, num_steps::Integer)
+    h = handle!(system)
+    check(ccall((:mavi_step, libmavi), Cint, (Ptr{Cvoid}, Int64), h, num_steps), "mavi_step", h)
+    sync!(system)
+end
+
+"""
+One-step GPU step function, the value `get_step_function` returns for a
+`CUDADevice` system. It keeps `system.state` current after every step, which
+costs a device-to-host copy per step; `gpu_run!` steps in bulk.
+"""
+gpu_step!(system) = gpu_run!(system, 1)
+
+"Forces of the current state (`calc_forces!` + optionally `calc_walls_forces!`)."
+function calc_forces(system; include_walls=false)
+    h = handle!(system)
+    f = Vector{SVector{2, Float64}}(undef, length(system.state.pos))
+    check(ccall((:mavi_calc_forces, libmavi), Cint, (Ptr{Cvoid}, Int32, Ptr{Cvoid}),
+                h, include_walls ? 1 : 0, f), "mavi_calc_forces", h)
+    return f
+end
+
+# ---- the hook into Mavi.jl -------------------------------------------------------
+# get_step_function(::StandardSys, system) (src/integration.jl:539-548) dispatches on
+# the dynamic config; a CUDA device mode takes precedence.
+function Mavi.Integration.get_step_function(t::Mavi.Systems.StandardSys, system::Mavi.Systems.System{
+        T, ND, NT, S, W, G, D, <:Mavi.Configs.IntCfg{<:Number, <:Any, CUDADevice}}) where {T, ND, NT, S, W, G, D}
+    return gpu_step!
+end
+
+end # module

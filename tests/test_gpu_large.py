@@ -1,0 +1,101 @@
+"""Parity at the benchmark sizes, through size-independent properties.
+
+At 262,144 and 4,194,304 particles the oracle still finishes in seconds for a
+force evaluation and a chunk rebuild, so these tests compare chunk sets
+(bit-exact) and forces (FP64 1e-12, mixed 1e-5 of the RMS force) on the full
+workloads after the GPU has advanced them, plus conservation laws that hold at
+any size: the pair sum of a periodic system is zero (Newton's third law)."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_force_err
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 1
+
+
+def chunks_equal(a, b):
+    ca, ma = a
+    cb, mb = b
+    return np.array_equal(ca, cb) and np.array_equal(ma, mb)
+
+
+@pytest.fixture(scope="module")
+def wl(mg):
+    from mavi_gb300 import workloads
+    return workloads
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lj_4194304_chunks_forces_momentum(mg, orc, wl, precision):
+    s, step = wl.lj_4194304(precision=precision)
+    mg.run_system(s, num_steps=20, step_func=step)
+    assert s.time_info.num_steps == 20
+    ref = orc.from_system(s, nthreads=NT, step_kind=step.kind)
+    assert chunks_equal(s.chunks(), ref.chunks())
+    f = s.calc_forces()
+    fr = ref.forces(orc.THREADED)
+    err = rel_force_err(f, fr)
+    assert err < (1e-12 if precision == "fp64" else 1e-5), err
+    # periodic LJ: pair forces cancel in the sum
+    net = np.linalg.norm(f.sum(axis=0)) / np.abs(f).sum()
+    assert net < (1e-12 if precision == "fp64" else 1e-6), net
+    ref.close()
+    s.close()
+
+
+def test_harm_262144_fp64_trajectory_and_mixed_forces(mg, orc, wl):
+    s, step = wl.harm_262144(precision="fp64")
+    ref = orc.from_system(s, nthreads=NT, step_kind=step.kind)
+    mg.run_system(s, num_steps=50, step_func=step)
+    ref.step(50, orc.THREADED)
+    p = ref.state()[0]
+    d = s.state.pos - p
+    L = s.space_cfg.geometry_cfg.length
+    d -= L * np.round(d / L)        # a particle may sit on the other side of a periodic seam
+    assert np.max(np.abs(d)) < 1e-9
+    ref.set_state(s.state.pos)
+    assert chunks_equal(s.chunks(), ref.chunks())
+    # mixed form on the same relaxed state
+    m = wl.harm_system(s.state.pos, L, "mixed")
+    err = rel_force_err(m.calc_forces(), ref.forces(orc.THREADED))
+    assert err < 1e-5, err
+    mg.run_system(m, num_steps=100, step_func=step)
+    ref.set_state(m.state.pos)
+    assert chunks_equal(m.chunks(), ref.chunks())
+    for x in (s, m):
+        x.close()
+    ref.close()
+
+
+def test_lj_batch_replicas_chunks_and_forces(mg, orc, wl):
+    systems, step = wl.lj_batch(num_replicas=24, precision="mixed", n_max=20000,
+                                quadrants=("rigid_rect", "periodic_rect", "rigid_circle"))
+    b = mg.SystemBatch(systems, step)
+    b.run(100)
+    forces = b.calc_forces()
+    for k, s in enumerate(systems):
+        ref = orc.from_system(s, nthreads=NT, step_kind=step.kind)
+        assert chunks_equal(b.handle.chunks(k), ref.chunks()), k
+        err = rel_force_err(forces[k], ref.forces(orc.THREADED))
+        assert err < 1e-5, (k, err)
+        ref.close()
+    b.close()
+
+
+def test_rings_batch_device_noise_runs_and_chunks(mg, orc, wl):
+    systems, _ = wl.rings_batch(num_replicas=6, rings_min=50, rings_max=300, precision="mixed")
+    b = mg.SystemBatch(systems)
+    b.run(200)
+    for k, s in enumerate(systems):
+        assert np.all(np.isfinite(s.state.rings_pos))
+        ref = orc.from_system(s, nthreads=NT)
+        assert chunks_equal(b.handle.chunks(k), ref.chunks()), k
+        ref.forces(orc.THREADED)          # the ring areas are formed with the forces
+        areas = ref.areas(s.state.num_rings)
+        assert np.all(areas > 0)
+        ref.close()
+    b.close()
