@@ -301,6 +301,34 @@ int mavi_last_error(MaviSystem* sys, char* buf, int32_t len);
  * counterpart. */
 int mavi_fma_peak(int32_t precision, int32_t device, double* flops_per_s);
 
+/* Chunk lists of one replica's positions that the caller already holds on the
+ * current CUDA device, built WITHOUT allocating device memory. No counterpart
+ * in the reference: it serves callers that cannot let a library allocate — a
+ * host that owns all device memory through its own pool or budget, or one
+ * that must avoid the device-wide synchronisation of cudaMalloc/cudaFree —
+ * and need update_chunks! (src/chunks.jl:120-161) without a handle
+ * (mavi_create allocates).
+ *   params   : the replica (geometry, chunk_cols/chunk_rows, dynamic config
+ *              for the particle radius and the capacity); chunks required.
+ *   pos_dev  : device, 2*n doubles (interleaved x, y), 16-byte aligned.
+ *   start_dev: device, rows*cols + 1 int32 written: CSR offsets over chunks
+ *              in column-major order (chunk = col*rows + row), 16-byte aligned.
+ *   ids_dev  : device, n int32 written: 0-based particle ids chunk by chunk,
+ *              ascending inside a chunk — the reference's chunk_particles
+ *              lists (mavi_get_chunks gives the same lists).
+ *   stream   : cudaStream_t (NULL = legacy default stream); the call waits for
+ *              it to read the status back.
+ *   msg      : optional buffer (msg_len bytes) for the reason of a failure.
+ * Scratch is one fixed device array inside the library: at most 1,048,576
+ * chunks and a chunk capacity of at most 1024; larger requests return
+ * MAVI_ERR_INVALID_ARG with the limit in msg. The first call on a device
+ * locates that array (set-up): make it before any stream capture. Every call
+ * clears the scratch it uses. Calls on one device share the scratch, so calls
+ * that overlap in time race: serialise them per device. */
+int mavi_chunk_lists_noalloc(const MaviReplicaParams* params, const double* pos_dev, int64_t n,
+                             int32_t* start_dev, int32_t* ids_dev, void* stream,
+                             char* msg, int32_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -184,6 +184,8 @@ SIGNATURES = {
     "mavi_profile_read": (C.c_int, [_vp, C.POINTER(MaviProfile)]),
     "mavi_last_error": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "mavi_fma_peak": (C.c_int, [C.c_int32, C.c_int32, _dp]),
+    "mavi_chunk_lists_noalloc": (C.c_int, [C.POINTER(MaviReplicaParams), _vp, C.c_int64, _vp, _vp, _vp,
+                                           C.c_char_p, C.c_int32]),
 }
 
 PACKAGE_DIR = pathlib.Path(__file__).resolve().parent

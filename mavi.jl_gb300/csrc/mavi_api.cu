@@ -111,6 +111,21 @@ static void bbox_of(const MaviReplicaParams& p, double& len, double& h, double& 
     }
 }
 
+// Chunk grid of one replica with the same arithmetic as mavi_create (bounding
+// box, chunk sides, capacity src/chunks.jl:32-34); used by the
+// allocation-free chunk-list entry point (mavi_noalloc.cu).
+__attribute__((visibility("hidden"))) void replica_chunk_grid(const MaviReplicaParams& p, DevRep& R) {
+    R.radius = particle_radius_of(p);
+    bbox_of(p, R.bb_len, R.bb_h, R.bb_blx, R.bb_bly);
+    R.has_chunks = 1;
+    R.rows = p.chunk_rows;
+    R.cols = p.chunk_cols;
+    R.chunk_l = R.bb_len / R.cols;
+    R.chunk_h = R.bb_h / R.rows;
+    double nc = (std::ceil(0.5 * R.chunk_l / R.radius) + 1) * (std::ceil(0.5 * R.chunk_h / R.radius) + 1);
+    R.cap = (int32_t)std::ceil(nc * 2);
+}
+
 // Real particles of a replica (rings: FixRingsIds p_ids, src/rings/states.jl:46-62).
 static int64_t active_count(const MaviReplicaParams& p, const int32_t* types) {
     if (p.state_kind != MAVI_STATE_RINGS) return p.num_particles;
