@@ -132,26 +132,36 @@ def time_form(mg, system, step_func, K, W, flush, torch):
     h = system.handle if step_func is None else system._ensure(step_func.kind)
     lib, hd = h.lib, h.handle
     h.check(lib.mavi_step(hd, W), "warm-up")
-    h.check(lib.mavi_profile_enable(hd, 1), "profile")
-    h.check(lib.mavi_step(hd, 1), "profiled warm-up")          # captures the profiled graph
-    h.check(lib.mavi_profile_enable(hd, 1), "profile reset")
-    torch.cuda.synchronize()
-    step_ms = []
-    for _ in range(K):
-        flush()
+
+    def timed(mode, k):
+        # mode 2: one event pair around each step's graph (nothing between its
+        # kernels); mode 1: event pairs around every kernel group as well
+        h.check(lib.mavi_profile_enable(hd, mode), "profile")
+        h.check(lib.mavi_step(hd, 1), "profiled warm-up")      # captures the graph of this mode
+        h.check(lib.mavi_profile_enable(hd, mode), "profile reset")
         torch.cuda.synchronize()
-        h.check(lib.mavi_step(hd, 1), "timed step")
+        ms = []
+        for _ in range(k):
+            flush()
+            torch.cuda.synchronize()
+            h.check(lib.mavi_step(hd, 1), "timed step")
+            p = abi.MaviProfile()
+            lib.mavi_profile_read(hd, C.byref(p))
+            ms.append(p.last_step_ms)
+        torch.cuda.synchronize()
         p = abi.MaviProfile()
         lib.mavi_profile_read(hd, C.byref(p))
-        step_ms.append(p.last_step_ms)
-    torch.cuda.synchronize()
-    p = abi.MaviProfile()
-    lib.mavi_profile_read(hd, C.byref(p))
+        return ms, p
+
+    step_ms, _ = timed(2, K)
+    kb = min(K, 100)
+    _, p = timed(1, kb)
     h.check(lib.mavi_profile_enable(hd, 0), "profile off")
-    kinds = {abi.MAVI_KERNEL_NAMES[k]: {"ms": p.ms[k], "launches": int(p.launches[k])}
+    kinds = {abi.MAVI_KERNEL_NAMES[k]: {"ms": p.ms[k] * K / kb, "launches": int(p.launches[k]) * K // kb}
              for k in range(abi.MAVI_NUM_KERNEL_KINDS) if p.launches[k]}
     return {"total_ms": float(sum(step_ms)), "step_ms": step_ms, "kinds": kinds,
-            "launches_per_step": launches_per_step(h.step_kind, abi)}
+            "launches_per_step": launches_per_step(h.step_kind, abi),
+            "kernel_breakdown_steps": kb}
 
 
 def e2e_form(mg, system, step_func, K, torch):

@@ -91,7 +91,8 @@ extern "C" {
 
 /* Arithmetic of the pair loop. FP64: every operation in double (the drop-in).
  * MIXED: positions stay FP64 for update, wrap and binning; the pair loop runs in
- * FP32 on chunk-centre-relative offsets with compensated FP32 accumulation. */
+ * FP32 instructions on exact integer chunk-centre-relative offsets (Lennard-Jones
+ * and WCA terms in double-float FP32 arithmetic, compensated accumulation). */
 #define MAVI_PREC_FP64  0
 #define MAVI_PREC_MIXED 1
 
@@ -289,6 +290,9 @@ int mavi_energies(MaviSystem* sys, int32_t pe_mode, double* ke, double* pe);
 int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
 
 int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
+/* Device-time profiling (and reset of the accumulated profile). on: 0 off,
+ * 1 per kernel kind and whole step (an event pair around every launch group),
+ * 2 whole step only (one event pair per step, nothing between the kernels). */
 int mavi_profile_enable(MaviSystem* sys, int32_t on);
 int mavi_profile_read(MaviSystem* sys, MaviProfile* prof);
 

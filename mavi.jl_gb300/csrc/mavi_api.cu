@@ -296,6 +296,17 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
                 (sp.wall == MAVI_WALL_RIGID || sp.wall == MAVI_WALL_PERIODIC) && sp.length == R.bb_len &&
                 sp.height == R.bb_h && sp.bl_x == R.bb_blx && sp.bl_y == R.bb_bly;
     R.walls_edge_only = edge_only ? 1 : 0;
+    if (p.dyn.kind == MAVI_DYN_LEN_JONES || p.dyn.kind == MAVI_DYN_RUN_TUMBLE) {
+        // 2^k ~ (sigma/u)^2 so that the scaled d^2 is O(1) at contact
+        int k = (int)std::lround(std::log2(p.dyn.sigma * p.dyn.sigma / (u * u)));
+        double g = std::ldexp(u * u, k);
+        double ad = R.pd[0] * u * std::pow(g, -7.0), bd = R.pd[1] * u * std::pow(g, -4.0);
+        R.lj_sk = (float)std::ldexp(1.0, -k);
+        R.lj_ah = (float)ad;
+        R.lj_al = (float)(ad - (double)R.lj_ah);
+        R.lj_bh = (float)bd;
+        R.lj_bl = (float)(bd - (double)R.lj_bh);
+    }
 }
 
 // Fixed-point pair constants (units of the replica) per (type, type).
@@ -372,7 +383,7 @@ static void drop_graph(MaviSystem* s) {
 // leaves behind). With profiling on, the event records are captured too and
 // replayed with the graph.
 static int ensure_graph(MaviSystem* s) {
-    if (s->graph_exec && s->graph_profiled == s->profiling) return MAVI_OK;
+    if (s->graph_exec && s->graph_profile_mode == s->profile_mode) return MAVI_OK;
     drop_graph(s);
     for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
     CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
@@ -387,7 +398,7 @@ static int ensure_graph(MaviSystem* s) {
     }
     s->graph_step_used = s->ev.step_used;
     s->ev.step_used = 0;
-    s->graph_profiled = s->profiling;
+    s->graph_profile_mode = s->profile_mode;
     return MAVI_OK;
 }
 
@@ -914,7 +925,9 @@ int mavi_get_stats(MaviSystem* s, MaviStats* st) {
 
 int mavi_profile_enable(MaviSystem* s, int32_t on) {
     if (!s) return MAVI_ERR_INVALID_ARG;
+    if (on < 0 || on > 2) return MAVI_ERR_INVALID_ARG;
     s->profiling = on != 0;
+    s->profile_mode = on;
     s->prof = MaviProfile{};
     for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
     return MAVI_OK;

@@ -68,6 +68,11 @@ struct DevRep {
     float mdt_f;
     int32_t mi_small;      // grid too small to skip the minimum image for unwrapped neighbours
     int32_t walls_edge_only; // every wall acts on the bounding rectangle only
+    // mixed-form Lennard-Jones / WCA in double-float: d^2 (units^2) scaled by
+    // lj_sk = 2^-k to O(1); (ah + al) = 48 eps sigma^12 u g^-7 and
+    // (bh + bl) = 24 eps sigma^6 u g^-4 with g = 2^k u^2
+    float lj_sk, lj_ah, lj_al, lj_bh, lj_bl;
+    int32_t _pad2;
 };
 
 // ---------------------------------------------------------------------------

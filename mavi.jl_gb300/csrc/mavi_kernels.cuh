@@ -438,15 +438,6 @@ __device__ __forceinline__ void pair_fixed(const DevRep& R, const FixPair& fp, i
     fy = 0.f;
     const float dxf = (float)dxi, dyf = (float)dyi;
     const float d2f = fmaf(dxf, dxf, dyf * dyf);
-    if constexpr (DYN == MAVI_DYN_LEN_JONES) {
-        float r2 = d2f * R.u2_f;
-        float ir2 = __frcp_rn(r2);
-        float ir6 = ir2 * ir2 * ir2;
-        float sc = ir6 * ir2 * (R.pf[0] * ir6 - R.pf[1]) * R.u_f;
-        fx = sc * dxf;
-        fy = sc * dyf;
-        return;
-    }
     if (d2f > fp.cut2_hi) return;
     const unsigned long long d2 = (unsigned long long)((long long)dxi * dxi) + (unsigned long long)((long long)dyi * dyi);
     if (d2f >= fp.cut2_lo && d2 > fp.cut2) return;
@@ -467,14 +458,61 @@ __device__ __forceinline__ void pair_fixed(const DevRep& R, const FixPair& fp, i
         const float sc = __fdividef(-fm * i64_to_f32(D) * R.u2_f, d + fp.eq);
         fx = sc * dxf;
         fy = sc * dyf;
-    } else {  // RunTumble (WCA) inside its cutoff
-        float r2 = d2f * R.u2_f;
-        float ir2 = __frcp_rn(r2);
-        float ir6 = ir2 * ir2 * ir2;
-        float sc = ir6 * ir2 * (R.pf[0] * ir6 - R.pf[1]) * R.u_f;
-        fx = sc * dxf;
-        fy = sc * dyf;
     }
+}
+
+// Whether a pair lies inside the cutoff of fp (FP32 test, exact int64 test
+// inside the +-1e-6 band).
+__device__ __forceinline__ bool inside_cutoff(const FixPair& fp, int32_t dxi, int32_t dyi) {
+    const float dxf = (float)dxi, dyf = (float)dyi;
+    const float d2f = fmaf(dxf, dxf, dyf * dyf);
+    if (d2f > fp.cut2_hi) return false;
+    if (d2f < fp.cut2_lo) return true;
+    const unsigned long long d2 = (unsigned long long)((long long)dxi * dxi) + (unsigned long long)((long long)dyi * dyi);
+    return d2 <= fp.cut2;
+}
+
+// Lennard-Jones force (src/configs.jl:380-397) of the exact integer
+// displacement (dxi, dyi), in double-float arithmetic: every value carries a
+// float high part and the rounding error of the operation that made it
+// (error-free products by fmaf, two-sums), so the result (fxh + fxl,
+// fyh + fyl) keeps ~1e-12 relative accuracy with FP32 instructions only. A
+// single FP32 evaluation loses ~1e-6 per pair (the r^-14 term amplifies the
+// rounding of d^2 sevenfold), which near-cancelling pair sums of a dense
+// Lennard-Jones state turn into force errors above 1e-5 of the RMS force.
+//   d^2 = S + E (S = fl(dx^2 + dy^2), dx = xh + xl exactly)
+//   h + l = d^2 2^-k, t = 1/h, 1/(h + l) = t (1 + e), e = 1 - (h + l) t
+//   f/d = (ah + al) (h+l)^-7 - (bh + bl) (h+l)^-4 = t^4 (A t^3 - B) (1 + O(e))
+// _rn intrinsics keep the compiler from fusing the products the error terms
+// are taken of.
+__device__ __forceinline__ void lj_pair_df(const DevRep& R, int32_t dxi, int32_t dyi, float& fxh, float& fxl,
+                                           float& fyh, float& fyl) {
+    const float xh = (float)dxi, yh = (float)dyi;
+    const float xl = (float)(dxi - __float2int_rz(xh)), yl = (float)(dyi - __float2int_rz(yh));
+    const float p1 = __fmul_rn(xh, xh), e1 = fmaf(xh, xh, -p1);
+    const float p2 = __fmul_rn(yh, yh), e2 = fmaf(yh, yh, -p2);
+    const float S = __fadd_rn(p1, p2);
+    const float sv = __fsub_rn(S, p1);
+    const float E = __fadd_rn(__fsub_rn(p1, __fsub_rn(S, sv)), __fsub_rn(p2, sv)) + e1 + e2 +
+                    2.0f * fmaf(xh, xl, yh * yl);
+    const float h = __fmul_rn(S, R.lj_sk), l = E * R.lj_sk;   // power-of-two scaling: exact
+    const float t = __frcp_rn(h);
+    const float e = fmaf(-h, t, 1.0f) - l * t;
+    const float t2 = __fmul_rn(t, t), t2e = fmaf(t, t, -t2);
+    const float t3 = __fmul_rn(t2, t), t3e = fmaf(t2, t, -t3) + t2e * t;
+    const float a = __fmul_rn(R.lj_ah, t3);
+    const float ae = fmaf(R.lj_ah, t3, -a) + fmaf(R.lj_ah, t3e, R.lj_al * t3);
+    const float b = __fsub_rn(a, R.lj_bh);                      // two-sum a + (-bh)
+    const float bv = __fsub_rn(b, a);
+    const float be = __fadd_rn(__fsub_rn(a, __fsub_rn(b, bv)), __fsub_rn(-R.lj_bh, bv)) + ae - R.lj_bl;
+    const float t4 = __fmul_rn(t2, t2), t4e = fmaf(t2, t2, -t4) + 2.0f * t2 * t2e;
+    const float sh = __fmul_rn(t4, b);
+    float sl = fmaf(t4, b, -sh) + fmaf(t4, be, t4e * b);
+    sl = fmaf(e * t4, 7.0f * a - 4.0f * R.lj_bh, sl);         // first order in e
+    fxh = __fmul_rn(sh, xh);
+    fxl = fmaf(sh, xh, -fxh) + fmaf(sh, xl, sl * xh);
+    fyh = __fmul_rn(sh, yh);
+    fyl = fmaf(sh, yh, -fyh) + fmaf(sh, yl, sl * yh);
 }
 
 // Force accumulators. Mixed form: FP32, Kahan-compensated for Lennard-Jones
@@ -498,6 +536,21 @@ template <int DYN> struct Acc<kPrecMixed, DYN> {
         } else {
             x += fx;
             y += fy;
+        }
+    }
+    // a term given as high + low parts (double-float pair laws): the low part
+    // goes into the compensation
+    __device__ __forceinline__ void add2(float fxh, float fxl, float fyh, float fyl) {
+        if constexpr (DYN == MAVI_DYN_LEN_JONES) {
+            float yx = fxh - cx, tx = x + yx;
+            cx = ((tx - x) - yx) - fxl;
+            x = tx;
+            float yy = fyh - cy, ty = y + yy;
+            cy = ((ty - y) - yy) - fyl;
+            y = ty;
+        } else {
+            x += fxh + fxl;
+            y += fyh + fyl;
         }
     }
     __device__ __forceinline__ float gx() const { return x - cx; }
@@ -565,6 +618,15 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
     if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
         if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
         if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
+    }
+    if constexpr (DYN == MAVI_DYN_LEN_JONES || DYN == MAVI_DYN_RUN_TUMBLE) {
+        if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
+            if (!inside_cutoff(me.fp0, dxi, dyi)) return;
+        }
+        float fxh, fxl, fyh, fyl;
+        lj_pair_df(R, dxi, dyi, fxh, fxl, fyh, fyl);
+        acc.add2(fxh, fxl, fyh, fyl);
+        return;
     }
     float fx, fy;
     if constexpr (DYN == MAVI_DYN_RINGS) {

@@ -52,7 +52,8 @@ struct MaviSystem {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     bool profiling = false;
-    bool graph_profiled = false;
+    int profile_mode = 0;          // 0 off, 1 per kernel kind + whole step, 2 whole step only
+    int graph_profile_mode = 0;    // profile_mode the captured graph was recorded with
     int graph_ev_used[MAVI_NUM_KERNEL_KINDS] = {0};
     int graph_step_used = 0;
     ProfEvents ev{};
@@ -99,12 +100,12 @@ inline cudaError_t dalloc(MaviSystem* s, T** p, size_t count) {
 inline unsigned nblocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
 
 inline void record_begin(MaviSystem* s, int kind) {
-    if (!s->profiling) return;
+    if (s->profile_mode != 1) return;
     int u = s->ev.used[kind];
     if (u < 4) cudaEventRecordWithFlags(s->ev.a[kind][u], s->stream, cudaEventRecordExternal);
 }
 inline void record_end(MaviSystem* s, int kind) {
-    if (!s->profiling) return;
+    if (s->profile_mode != 1) return;
     int u = s->ev.used[kind];
     if (u < 4) {
         cudaEventRecordWithFlags(s->ev.b[kind][u], s->stream, cudaEventRecordExternal);

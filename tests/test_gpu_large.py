@@ -58,6 +58,7 @@ def test_harm_262144_fp64_trajectory_and_mixed_forces(mg, orc, wl):
     d -= L * np.round(d / L)        # a particle may sit on the other side of a periodic seam
     assert np.max(np.abs(d)) < 1e-9
     ref.set_state(s.state.pos)
+    ref.update_chunks()
     assert chunks_equal(s.chunks(), ref.chunks())
     # mixed form on the same relaxed state
     m = wl.harm_system(s.state.pos, L, "mixed")
@@ -65,6 +66,7 @@ def test_harm_262144_fp64_trajectory_and_mixed_forces(mg, orc, wl):
     assert err < 1e-5, err
     mg.run_system(m, num_steps=100, step_func=step)
     ref.set_state(m.state.pos)
+    ref.update_chunks()
     assert chunks_equal(m.chunks(), ref.chunks())
     for x in (s, m):
         x.close()

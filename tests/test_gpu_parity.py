@@ -51,6 +51,7 @@ def test_lj_trajectory_periodic_chunks_bit_exact_after_steps(mg, orc):
         mg.run_system(s, num_steps=50)
         ref.step(50)
         ref.set_state(s.state.pos, s.state.vel)   # same FP64 state on both sides
+        ref.update_chunks()
         assert chunks_equal(s, ref)
     s.close()
 
@@ -282,3 +283,24 @@ def test_staged_gather_equals_global_gather_bitwise(mg, precision):
         l.append(s.state.pos.copy())
         s.close()
     assert np.array_equal(l[0], l[1])
+
+
+def test_energy_drift_mixed_matches_fp64(mg):
+    """Lennard-Jones gas (1024 particles, rigid box, dt = 1e-3, 2000 steps):
+    the total energy of the mixed form follows the FP64 form's (same drift)."""
+    series = {}
+    for precision in ("fp64", "mixed"):
+        s = lj_grid(mg, 32, 32, wall="rigid", chunks=(17, 17), precision=precision)
+        e = []
+        for _ in range(10):
+            mg.run_system(s, num_steps=200)
+            ke, pe = s.energies()
+            e.append(ke + pe)
+        series[precision] = np.array(e)
+        s.close()
+    e64, emx = series["fp64"], series["mixed"]
+    scale = np.abs(e64).max()
+    drift64 = abs(e64[-1] - e64[0]) / scale
+    driftmx = abs(emx[-1] - emx[0]) / scale
+    assert np.max(np.abs(emx - e64)) / scale < 1e-6
+    assert abs(driftmx - drift64) < 1e-6
