@@ -115,7 +115,7 @@ class Clocks:
 def launches_per_step(step_kind, abi):
     rebin = 3   # scan, scatter, deterministic per-chunk order + permutation
     body = {abi.MAVI_STEP_NEWTON: 2, abi.MAVI_STEP_OVERDAMPED: 1, abi.MAVI_STEP_SZABO: 1, abi.MAVI_STEP_RTP: 1,
-            abi.MAVI_STEP_RINGS: 3}[step_kind]
+            abi.MAVI_STEP_RINGS: 4}[step_kind]   # rings: pair pass, ring terms + update, polarisation, histogram
     return rebin + body
 
 
@@ -126,10 +126,65 @@ def measured_peaks():
         return {}
 
 
-def time_form(mg, system, step_func, K, W, flush, torch):
-    """Device-timed steps of one system; returns a dict of measurements."""
+class Runner:
+    """One workload behind one handle: a single System, or a list of systems
+    advanced together as a SystemBatch (replicas in the same launches)."""
+
+    def __init__(self, mg, obj, step):
+        self.mg = mg
+        self.step = step
+        if isinstance(obj, (list, tuple)):
+            self.systems = list(obj)
+            self.batch = mg.SystemBatch(self.systems, step)
+            self.handle = self.batch.handle
+        else:
+            self.systems = [obj]
+            self.batch = None
+            self.handle = obj._ensure(step.kind if step is not None else None)
+        self.kind = self.handle.step_kind
+        self.num_slots = int(sum(s.num_slots for s in self.systems))
+
+    @property
+    def first(self):
+        return self.systems[0]
+
+    def forces(self):
+        return self.handle.forces(False)
+
+    def stats(self):
+        return self.handle.stats()
+
+    def host_state(self):
+        """Concatenated host arrays in the layout of mavi_create."""
+        st = [s.state for s in self.systems]
+        pos = np.concatenate([x.pos.reshape(-1) for x in st])
+        vel = None
+        if st[0].kind == self.mg.abi.MAVI_STATE_SECOND_LAW and st[0].vel is not None:
+            vel = np.concatenate([x.vel.reshape(-1) for x in st])
+        pol = None
+        if st[0].pol_array() is not None:
+            pol = np.concatenate([x.pol_array() for x in st])
+        return pos, vel, pol
+
+    def oracle_forces(self, orc, nthreads):
+        out = []
+        for s in self.systems:
+            o = orc.from_system(s, nthreads=nthreads, step_kind=self.kind)
+            out.append(o.forces(orc.THREADED if nthreads > 1 else orc.SEQUENTIAL))
+            o.close()
+        return np.concatenate(out)
+
+    def close(self):
+        if self.batch is not None:
+            self.batch.close()
+        else:
+            self.systems[0].close()
+
+
+def time_form(mg, runner, K, W, flush, torch):
+    """Device-timed steps of one workload; returns a dict of measurements."""
     abi = mg.abi
-    h = system.handle if step_func is None else system._ensure(step_func.kind)
+    h = runner.handle
     lib, hd = h.lib, h.handle
     h.check(lib.mavi_step(hd, W), "warm-up")
 
@@ -164,32 +219,31 @@ def time_form(mg, system, step_func, K, W, flush, torch):
             "kernel_breakdown_steps": kb}
 
 
-def e2e_form(mg, system, step_func, K, torch):
+def e2e_form(mg, runner, K, torch):
     """Through the C ABI with pinned host buffers: upload -> 1 step -> download."""
-    h = system._ensure(step_func.kind)
+    h = runner.handle
     lib, hd = h.lib, h.handle
-    n = system.num_slots
-    pos_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
-    pos_h.copy_(torch.from_numpy(system.state.pos))
-    has_vel = system.state.kind == mg.abi.MAVI_STATE_SECOND_LAW and system.state.vel is not None
-    vel_h = None
-    if has_vel:
-        vel_h = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
-        vel_h.copy_(torch.from_numpy(system.state.vel))
     dp = C.POINTER(C.c_double)
-    pp = C.cast(pos_h.data_ptr(), dp)
-    vp = C.cast(vel_h.data_ptr(), dp) if vel_h is not None else None
-    bi = pos_h.numel() * 8 + (vel_h.numel() * 8 if vel_h is not None else 0)
+    bufs = []
+    for a in runner.host_state():
+        if a is None:
+            bufs.append((None, None))
+            continue
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        t.copy_(torch.from_numpy(np.ascontiguousarray(a)))
+        bufs.append((t, C.cast(t.data_ptr(), dp)))
+    (pt, pp), (vt, vp), (qt, qp) = bufs
+    bi = sum(t.numel() * 8 for t, _ in bufs if t is not None)
     bo = bi
     for _ in range(3):
-        h.check(lib.mavi_upload_state(hd, pp, vp, None), "upload")
+        h.check(lib.mavi_upload_state(hd, pp, vp, qp), "upload")
         h.check(lib.mavi_step(hd, 1), "step")
-        h.check(lib.mavi_download_state(hd, pp, vp, None), "download")
+        h.check(lib.mavi_download_state(hd, pp, vp, qp), "download")
     t0 = time.perf_counter()
     for _ in range(K):
-        h.check(lib.mavi_upload_state(hd, pp, vp, None), "upload")
+        h.check(lib.mavi_upload_state(hd, pp, vp, qp), "upload")
         h.check(lib.mavi_step(hd, 1), "step")
-        h.check(lib.mavi_download_state(hd, pp, vp, None), "download")
+        h.check(lib.mavi_download_state(hd, pp, vp, qp), "download")
     dt = time.perf_counter() - t0
     return {"seconds": dt, "h2d": bi, "d2h": bo}
 
@@ -211,10 +265,10 @@ def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
         # final pass: r x, (v), uid, rep, cell, (off); w x, (v), uid, rep, cell, rank, (off)
         return (16 + vel + 4 + 4 + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
     if kind == "bin_sort":
-        # r src_of, cell, uid, x, (v), rep, (off); w x, (v), uid, rep, cell, slot_of, (off)
+        # r src_of, cell_at, key_of, x, (v), rep, (off); w x, (v), uid, rep, cell, slot_of, (off)
         return (4 + 4 + 4 + 16 + vel + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
     if kind == "bin_scatter":
-        return 4 + 4 + 4          # r cell, rank; w src_of
+        return 4 + 4 + 4 + 4 + 4 + 4   # r cell, rank, uid; w src_of, key_of, cell_at
     if kind == "bin_scan":
         return 0                  # per chunk, not per particle (counted in the chunk term)
     return 0
@@ -248,28 +302,87 @@ def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_pea
     return rf
 
 
-def cpu_baseline(mg, orc, system, step_func, seconds, nthreads):
-    o = orc.from_system(system, nthreads=nthreads, step_kind=step_func.kind)
+def oracle_steps(orc, o, k, mode, kind, rng):
+    """k oracle steps, drawing the step's noise on the host when it has any."""
+    cnt = o.noise_count()
+    o.step(k, mode, orc.noise_for(kind, cnt * k, rng) if cnt else None)
+
+
+def cpu_baseline(mg, orc, runner, seconds, nthreads):
+    """The reference's algorithm (oracle/, Threaded column split) on the host
+    cores: whole replicas, in order, until about `seconds` of work."""
     mode = orc.THREADED if nthreads > 1 else orc.SEQUENTIAL
-    t0 = time.perf_counter()
-    o.step(1, mode)
-    t1 = time.perf_counter() - t0
-    k = max(1, min(10000, int(seconds / max(t1, 1e-6))))
-    t0 = time.perf_counter()
-    o.step(k, mode)
-    dt = time.perf_counter() - t0
-    o.close()
-    n = system.num_slots
-    return {"value": n * k / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{k} steps of the full workload (N={n}) after 1 warm-up step, "
-                      f"oracle/mavi_oracle.c, {'Threaded column split' if nthreads > 1 else 'Sequencial'}"}
+    done = 0
+    total = 0.0
+    used = 0
+    steps = []
+    rng = np.random.default_rng(0)
+    for s in runner.systems:
+        o = orc.from_system(s, nthreads=nthreads, step_kind=runner.kind)
+        oracle_steps(orc, o, 1, mode, runner.kind, rng)                      # warm-up
+        t0 = time.perf_counter()
+        oracle_steps(orc, o, 1, mode, runner.kind, rng)
+        one = time.perf_counter() - t0
+        budget = max(seconds / max(len(runner.systems), 1), seconds - total) if used == 0 else seconds - total
+        k = max(1, min(10000, int(budget / max(one, 1e-6))))
+        noise = orc.noise_for(runner.kind, o.noise_count() * k, rng) if o.noise_count() else None
+        t0 = time.perf_counter()
+        o.step(k, mode, noise)
+        total += time.perf_counter() - t0
+        o.close()
+        done += s.num_slots * k
+        steps.append(k)
+        used += 1
+        if total >= seconds:
+            break
+    what = (f"{steps[0]} steps of the full workload (N={runner.num_slots})" if len(runner.systems) == 1 else
+            f"{used} of {len(runner.systems)} replicas, {min(steps)}..{max(steps)} steps each")
+    return {"value": done / total, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{what} after 1 warm-up step, oracle/mavi_oracle.c, "
+                      f"{'Threaded column split' if nthreads > 1 else 'Sequencial'}"}
 
 
 def build_workload(mg, name, precision):
     W = __import__("mavi_gb300.workloads", fromlist=["WORKLOADS"]).WORKLOADS
-    if name == "harm_262144":
-        return W[name](precision=precision)
-    return W[name](precision=precision)
+    obj, step = W[name](precision=precision)
+    return Runner(mg, obj, step)
+
+
+def run_reference_generic(args, mg, orc, workloads, nthreads):
+    """The reference's algorithm (oracle/) on any workload: every replica
+    advances one step per step, steps bounded to about a minute in total."""
+    from mavi_gb300.system import get_step_function
+    obj, step = workloads.WORKLOADS[args.workload](precision="fp64")
+    systems = list(obj) if isinstance(obj, (list, tuple)) else [obj]
+    kind = step.kind if step is not None else get_step_function(systems[0]).kind
+    oracles = [orc.from_system(s, nthreads=nthreads, step_kind=kind) for s in systems]
+    rng = np.random.default_rng(0)
+    for o in oracles:
+        oracle_steps(orc, o, max(args.warmup, 1), orc.THREADED, kind, rng)
+    noise = [orc.noise_for(kind, o.noise_count(), rng) if o.noise_count() else None for o in oracles]
+    n = sum(s.num_slots for s in systems)
+    k = 0
+    t0 = time.perf_counter()
+    while k < args.steps:
+        for o, z in zip(oracles, noise):   # one step of noise per replica, reused (timing only)
+            o.step(1, orc.THREADED, z)
+        k += 1
+        if time.perf_counter() - t0 > 60.0:
+            break
+    dt = time.perf_counter() - t0
+    for o in oracles:
+        o.close()
+    v = n * k / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": k,
+            "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "N": n, "replicas": len(systems)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{k} steps of every replica; the reference is Julia, absent on this "
+                                       f"machine: its algorithm restated in C (oracle/), Threaded column split"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
 
 
 def run_reference(args):
@@ -281,8 +394,7 @@ def run_reference(args):
     from mavi_gb300 import workloads
     nthreads = os.cpu_count() or 1
     if args.workload != "harm_262144":
-        print(json.dumps({"impl": "reference", "unavailable": f"reference arm runs the default workload only"}))
-        return 0
+        return run_reference_generic(args, mg, orc, workloads, nthreads)
     pos, L = workloads.harm_262144_initial()
     # same relaxation as the GPU arm, on the oracle (the reference's algorithm)
     sys_ = workloads.harm_system(pos, L, "fp64")
@@ -338,23 +450,17 @@ def main():
     def flush():
         flush_buf.fill_(1.0)
 
-    results = {}
-    for precision in ("fp64", "mixed"):
-        system, step_func = build_workload(mg, args.workload, precision)
-        results[precision] = {"system": system, "step": step_func}
+    runners = {precision: build_workload(mg, args.workload, precision) for precision in ("fp64", "mixed")}
 
     # force accuracy at the starting state (both forms and the oracle)
-    f64 = results["fp64"]["system"].calc_forces()
-    fmx = results["mixed"]["system"].calc_forces()
+    f64 = runners["fp64"].forces()
+    fmx = runners["mixed"].forces()
     err = {"mixed_vs_fp64": rel_force_err(fmx, f64)}
-    stats = results["fp64"]["system"].stats()
+    stats = runners["fp64"].stats()
     orc = None
     if rank == 0 and not args.no_cpu_baseline:
         orc = graft.load_oracle()
-        o = orc.from_system(results["fp64"]["system"], nthreads=os.cpu_count() or 1,
-                            step_kind=results["fp64"]["step"].kind)
-        fo = o.forces(orc.THREADED)
-        o.close()
+        fo = runners["fp64"].oracle_forces(orc, os.cpu_count() or 1)
         err["fp64_vs_oracle"] = rel_force_err(f64, fo)
         err["mixed_vs_oracle"] = rel_force_err(fmx, fo)
 
@@ -366,13 +472,12 @@ def main():
     clocks = Clocks(local)
     meas = {}
     for precision in ("fp64", "mixed"):
-        r = results[precision]
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
         if precision == "mixed":
             clocks.start()
-        m = time_form(mg, r["system"], r["step"], args.steps, max(args.warmup, 3), flush, torch)
+        m = time_form(mg, runners[precision], args.steps, max(args.warmup, 3), flush, torch)
         if precision == "mixed":
             clk = clocks.stop()
         torch.cuda.synchronize()
@@ -383,35 +488,39 @@ def main():
             dist.barrier()
         meas[precision] = m
 
-    e2e = e2e_form(mg, results["mixed"]["system"], results["mixed"]["step"], min(args.steps, 300), torch)
+    e2e = e2e_form(mg, runners["mixed"], min(args.steps, 300), torch)
 
-    n = results["mixed"]["system"].num_slots
+    n = runners["mixed"].num_slots
     K = args.steps
     line_forms = {}
     for precision in ("fp64", "mixed"):
         m = meas[precision]
+        r = runners[precision]
         v = world * n * K / (m["total_ms"] * 1e-3)
-        dyn_kind = abi.MaviReplicaParams()
-        results[precision]["system"].fill_params(dyn_kind, results[precision]["step"].kind)
-        st = results[precision]["system"].state
-        rf = roofline(m, n, precision, results[precision]["step"].kind, abi, peaks, stats.candidate_pairs,
-                      fma[precision], dyn_kind.dyn.kind, getattr(st, "vel", None) is not None)
+        params = abi.MaviReplicaParams()
+        r.first.fill_params(params, r.kind)
+        rf = roofline(m, n, precision, r.kind, abi, peaks, stats.candidate_pairs,
+                      fma[precision], params.dyn.kind, getattr(r.first.state, "vel", None) is not None)
         line_forms[precision] = {"value": v, "ms_per_step": m["total_ms"] / K, "roofline": rf,
                                  "kernels_ms_per_step": {k: d["ms"] / K for k, d in m["kinds"].items()},
                                  "gpu_launches": m["launches_per_step"] * K}
     cpu = None
     if rank == 0 and orc is not None:
-        cpu = cpu_baseline(mg, orc, results["fp64"]["system"], results["fp64"]["step"], args.cpu_seconds,
-                           os.cpu_count() or 1)
+        cpu = cpu_baseline(mg, orc, runners["fp64"], args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
         mx = line_forms["mixed"]
+        first = runners["mixed"].first
+        cc = first.int_cfg.chunks_cfg if hasattr(first.int_cfg, "chunks_cfg") else None
+        grid = [cc.num_rows, cc.num_cols] if cc is not None and len(runners["mixed"].systems) == 1 else None
         out = {
             "metric": METRIC, "value": mx["value"], "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": max(args.warmup, 3), "ms_per_step": mx["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair loop + f64 update",
             "data": "synthetic",
-            "config": {"workload": args.workload, "N": n, "form": "mixed",
-                       "chunks": [int(stats.total_chunks ** 0.5)] * 2, "candidate_pairs": stats.candidate_pairs,
+            "config": {"workload": args.workload, "N": n, "replicas": len(runners["mixed"].systems),
+                       "form": "mixed", "chunks": grid, "total_chunks": stats.total_chunks,
+                       "candidate_pairs": stats.candidate_pairs,
+                       "gather": {0: "staged", 1: "global", 2: "columns"}.get(runners["mixed"].stats().gather_mode),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed (256 MiB write) before every timed step"},
             "roofline": mx["roofline"],
@@ -431,8 +540,8 @@ def main():
             "fma_peak_tflops": {k: (v / 1e12 if v else None) for k, v in fma.items()},
         }
         print(json.dumps(out))
-    for precision in ("fp64", "mixed"):
-        results[precision]["system"].close()
+    for r in runners.values():
+        r.close()
     if world > 1:
         dist.destroy_process_group()
     return 0

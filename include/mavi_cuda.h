@@ -192,7 +192,10 @@ typedef struct MaviOptions {
     int32_t use_graph;       /* capture the step in a CUDA graph when nonzero      */
     int32_t block_size;      /* threads per block for particle kernels (0 = tuned) */
     int32_t gather_mode;     /* pair gather: 0 = warp-staged shared-memory window,
-                                1 = per-thread global loads (same results)          */
+                                1 = per-thread global loads chunk by chunk,
+                                2 = per-thread contiguous row ranges per column,
+                                -1 = autotuned at creation (fastest force pass);
+                                all add the same terms in the same order        */
 } MaviOptions;
 
 /* Work counters of the last force pass (for roofline accounting). */
@@ -201,7 +204,7 @@ typedef struct MaviStats {
     int64_t total_particles;
     int64_t total_chunks;
     int32_t max_chunk_count;  /* largest chunk occupancy at the last rebuild        */
-    int32_t _pad0;
+    int32_t gather_mode;      /* pair gather in use (MaviOptions.gather_mode)        */
 } MaviStats;
 
 /* Per-kernel device time accumulated while profiling is on (milliseconds). */

@@ -137,7 +137,7 @@ class MaviOptions(C.Structure):
 class MaviStats(C.Structure):
     _fields_ = [
         ("candidate_pairs", C.c_int64), ("total_particles", C.c_int64), ("total_chunks", C.c_int64),
-        ("max_chunk_count", C.c_int32), ("_pad0", C.c_int32),
+        ("max_chunk_count", C.c_int32), ("gather_mode", C.c_int32),
     ]
 
 

@@ -275,13 +275,16 @@ class CUDADevice:
     precision: "fp64" (every operation in double; the drop-in) or "mixed"
     (FP32 pair loop on chunk-centre offsets, FP64 update, wrap and binning).
     noise: "device" (Philox on the GPU, seeded) or "injected" (the caller
-    supplies each step's noise numbers)."""
+    supplies each step's noise numbers).
+    gather: pair gather — "staged" (warp window in shared memory), "global"
+    (chunk by chunk), "columns" (contiguous row ranges per column) or "auto"
+    (the fastest force pass at creation); all give identical results."""
     precision: str = "fp64"
     device: int = 0
     use_graph: bool = True
     noise: str = "device"
     seed: int = 0
-    gather: str = "staged"
+    gather: str = "auto"
 
     def options(self) -> abi.MaviOptions:
         o = abi.MaviOptions()
@@ -290,7 +293,7 @@ class CUDADevice:
         o.seed = int(self.seed) & ((1 << 64) - 1)
         o.device = int(self.device)
         o.use_graph = 1 if self.use_graph else 0
-        o.gather_mode = {"staged": 0, "global": 1}[self.gather]
+        o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2}[self.gather]
         return o
 
 

@@ -402,6 +402,43 @@ static int ensure_graph(MaviSystem* s) {
     return MAVI_OK;
 }
 
+// Pair-gather autotuner: times a force-only pass (it changes no state) with
+// each gather and keeps the fastest for the handle's lifetime; graphs are
+// captured afterwards and use it. The gathers add the same terms in the same
+// order, so the choice never changes results, only speed.
+static int autotune_gather(MaviSystem* s) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    CUDA_TRY(s, cudaEventCreate(&a));
+    CUDA_TRY(s, cudaEventCreate(&b));
+    float best = INFINITY;
+    int best_mode = 0;
+    for (int mode = 0; mode < kNumGatherModes; mode++) {
+        s->C.gather_mode = mode;
+        for (int w = 0; w < 2; w++) {
+            if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, 0);
+            else forces_only_mixed(s, 0);
+        }
+        cudaEventRecord(a, s->stream);
+        for (int r = 0; r < 5; r++) {
+            if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, 0);
+            else forces_only_mixed(s, 0);
+        }
+        cudaEventRecord(b, s->stream);
+        cudaError_t e = cudaEventSynchronize(b);
+        float ms = INFINITY;
+        if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) {
+            best = ms;
+            best_mode = mode;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    s->C.gather_mode = best_mode;
+    CUDA_TRY(s, cudaGetLastError());
+    return check_device_error(s);
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -453,7 +490,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     s->R = num_replicas;
     s->params.assign(replicas, replicas + num_replicas);
     s->prec = opt->precision;
-    if (s->prec != MAVI_PREC_FP64 && s->prec != MAVI_PREC_MIXED) {
+    if ((s->prec != MAVI_PREC_FP64 && s->prec != MAVI_PREC_MIXED) || opt->gather_mode < -1 ||
+        opt->gather_mode >= kNumGatherModes) {
         delete s;
         return MAVI_ERR_INVALID_ARG;
     }
@@ -611,11 +649,16 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     }
     ALLOC(C.uid_cur, M); ALLOC(C.uid_out, M); ALLOC(C.rep_cur, M); ALLOC(C.rep_out, M);
     ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.rank, M); ALLOC(C.src_of, M);
+    ALLOC(C.key_of, M); ALLOC(C.cell_at, M);
     ALLOC(C.slot_of, N);
     ALLOC(C.count, s->Ctot); ALLOC(C.start, s->Ctot + 1);
     ALLOC(C.tile_sum, s->ntiles);
     int32_t* ring_types_d = nullptr;
-    if (s->is_rings) { ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings); }
+    int32_t* ring_rep_d = nullptr;
+    if (s->is_rings) {
+        ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings);
+        ALLOC(ring_rep_d, s->total_rings); ALLOC(C.ring_cs, s->total_rings); ALLOC(C.ring_vc, s->total_rings);
+    }
     DevRep* reps_d = nullptr;
     MaviSpace* spaces_d = nullptr;
     MaviRingsCfg* rcfg_d = nullptr;
@@ -631,6 +674,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     if (s->noise_count > 0) { ALLOC(s->noise_cur, s->noise_count); }
 #undef ALLOC
     C.ring_types = ring_types_d;
+    C.ring_rep = ring_rep_d;
     C.reps = reps_d;
     C.spaces = spaces_d;
     C.rcfg = rcfg_d;
@@ -653,7 +697,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     }
     // identity user order over active slots
     std::vector<int32_t> uid_h(M), rep_h(M);
-    std::vector<int32_t> types_all;
+    std::vector<int32_t> types_all, ring_rep_h;
     {
         int64_t k = 0;
         const int32_t* tc = ring_types;
@@ -664,6 +708,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
                 for (int q = 0; q < p.rings.num_rings; q++) {
                     int t = tc ? tc[q] : 1;
                     types_all.push_back(t);
+                    ring_rep_h.push_back(r);
                     for (int i = 0; i < p.rings.num_particles[t - 1]; i++) {
                         uid_h[k] = (int32_t)(R.slot0 + (int64_t)q * p.rings.nmax + i);
                         rep_h[k] = r;
@@ -692,6 +737,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     if (s->is_rings) {
         CUDA_TRY(s, cudaMemcpyAsync(ring_types_d, types_all.data(), sizeof(int32_t) * s->total_rings,
                                     cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(ring_rep_d, ring_rep_h.data(), sizeof(int32_t) * s->total_rings,
+                                    cudaMemcpyHostToDevice, s->stream));
     }
     CUDA_TRY(s, cudaStreamSynchronize(s->stream));
     for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++)
@@ -707,6 +754,10 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     launch_rebin(s, false);
     rc = check_device_error(s);
     if (rc) return bail(rc);
+    if (opt->gather_mode < 0) {
+        rc = autotune_gather(s);
+        if (rc) return bail(rc);
+    }
     *out = s;
     return MAVI_OK;
 }
@@ -718,8 +769,10 @@ int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const
         CUDA_TRY(s, cudaMemcpyAsync(s->vel_user, vel, sizeof(double2) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
     if (s->has_pol && pol)
         CUDA_TRY(s, cudaMemcpyAsync(s->pol_user, pol, sizeof(double) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
-    if (s->is_rings && pol)
+    if (s->is_rings && pol) {
         CUDA_TRY(s, cudaMemcpyAsync(s->C.ring_pol, pol, sizeof(double) * s->total_rings, cudaMemcpyHostToDevice, s->stream));
+        k_ring_pol<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
+    }
     k_gather_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, (s->has_vel && vel) ? s->vel_user : nullptr,
                                                            (s->has_pol && pol) ? s->pol_user : nullptr);
     s->counts_valid = false;
@@ -920,6 +973,7 @@ int mavi_get_stats(MaviSystem* s, MaviStats* st) {
     st->total_particles = s->M;
     st->total_chunks = s->Ctot;
     st->max_chunk_count = mx;
+    st->gather_mode = s->C.gather_mode;
     return MAVI_OK;
 }
 

@@ -59,12 +59,16 @@ struct Ctx {
     int32_t *uid_cur, *uid_out, *rep_cur, *rep_out;
     int32_t *cell_cur, *cell_out, *rank;
     int32_t *count, *start, *src_of, *slot_of;
+    int32_t *key_of, *cell_at;   // per claimed slot: user id and chunk of its particle
     int32_t *tile_sum;   // chunk counts per scan tile, accumulated with the histogram
     int64_t ntiles;
     // per ring (global ring index)
     double *ring_pol;
     double *ring_area;
     const int32_t *ring_types;
+    const int32_t *ring_rep;   // replica of each ring
+    double2 *ring_cs;          // (cos, sin) of the ring's polarisation angle
+    double2 *ring_vc;          // mean particle velocity of the ring in the last update
     // descriptors
     const DevRep *reps;
     const MaviSpace *spaces;     // [replica][MAVI_MAX_SPACES]
@@ -77,7 +81,8 @@ struct Ctx {
     const double *noise;
     int32_t noise_mode;
     int32_t num_reps;
-    int32_t gather_mode;   // 0: warp-staged window in shared memory, 1: global loads
+    int32_t gather_mode;   // 0: warp-staged window in shared memory, 1: per-chunk global loads,
+                           // 2: per-column contiguous global ranges
     uint64_t seed;
 };
 
@@ -333,6 +338,8 @@ static __global__ void k_scatter(Ctx C) {
     int32_t dst = C.start[c] + C.rank[s];
     // ranks are < count[c] by construction, so dst stays inside [start[c], start[c+1])
     C.src_of[dst] = (int32_t)s;
+    C.key_of[dst] = C.uid_out[s];
+    C.cell_at[dst] = c;
 }
 
 // ===========================================================================
@@ -344,12 +351,14 @@ template <int PREC, bool HAS_VEL, bool HAS_POL>
 __global__ void k_permute(Ctx C) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= C.M) return;
+    // the scatter left each claimed slot's user id and chunk beside it, so the
+    // rank loop reads one array and the chunk range needs no gather
     int32_t sm = C.src_of[p];
-    int32_t c = C.cell_out[sm];
+    int32_t c = C.cell_at[p];
+    int32_t u = C.key_of[p];
     int32_t b = C.start[c], e = C.start[c + 1];
-    int32_t u = C.uid_out[sm];
     int32_t rank = 0;
-    for (int32_t q = b; q < e; q++) rank += (C.uid_out[C.src_of[q]] < u) ? 1 : 0;
+    for (int32_t q = b; q < e; q++) rank += (C.key_of[q] < u) ? 1 : 0;
     int32_t dst = b + rank;
     C.pos_cur[dst] = C.pos_out[sm];
     C.uid_cur[dst] = u;
@@ -645,17 +654,50 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
     acc.add(fx, fy);
 }
 
+// Pair term of a neighbour reached through a wrapped periodic stencil on a
+// space without minimum image (periodic walls on a non-rectangular geometry):
+// the reference takes the raw difference r1 - r2 there (src/integration.jl:
+// 38-52), a vector across the box. FP64 positions give it directly; the
+// mixed form forms it from the exact integer offsets and the true chunk
+// distance (shx, shy in units, int64) and evaluates the pair law in FP64
+// (such pairs are rare and far apart).
+template <int DYN>
+__device__ __forceinline__ void pair_term_raw(const Ctx& C, const DevRep& R, int32_t rep,
+                                              const Me<kPrecFP64, DYN>& me, double2 q, int32_t uq, long long,
+                                              long long, Acc<kPrecFP64, DYN>& acc) {
+    pair_term<DYN>(C, R, rep, me, q, uq, 0, 0, false, acc);
+}
+
+template <int DYN>
+__device__ __forceinline__ void pair_term_raw(const Ctx& C, const DevRep& R, int32_t rep,
+                                              const Me<kPrecMixed, DYN>& me, int2 oj, int32_t uq, long long shx,
+                                              long long shy, Acc<kPrecMixed, DYN>& acc) {
+    const double dx = (double)((long long)me.p.x - oj.x + shx) / R.inv_u;
+    const double dy = (double)((long long)me.p.y - oj.y + shy) / R.inv_u;
+    const double d2 = dx * dx + dy * dy;
+    double sc;
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        RingInfo o = ring_info(C, R, uq);
+        sc = rings_pair_scalar_d(C.rcfg[rep], me.ri.type, o.type, o.ring == me.ri.ring, me.ri.p, o.p, me.n_ring, d2);
+    } else {
+        sc = pair_scalar<DYN, double>(R.pd, d2);
+    }
+    acc.add((float)(sc * dx), (float)(sc * dy));
+}
+
 // Global-memory gather of one lane (also the all-pairs mode without chunks).
 template <int PREC, int DYN>
 __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
                                               const typename PartOf<PREC>::T* __restrict__ P,
                                               const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc) {
-    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
+    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi, bool raw = false,
+                     long long rshx = 0, long long rshy = 0) {
         for (int32_t j = b; j < e; j++) {
             if (j == (int32_t)s) continue;
             int32_t uq = 0;
             if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
-            pair_term<DYN>(C, R, rep, me, P[j], uq, shx, shy, mi, acc);
+            if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, rshy, acc);
+            else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, shy, mi, acc);
         }
     };
     if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224)
@@ -683,7 +725,73 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
             int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
             // centre of the neighbour chunk relative to ours, in units:
             // x grows with the column, y decreases with the row
-            visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small));
+            const bool raw = wr && !R.min_image;
+            visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small), raw,
+                  -(long long)(ncol - col) * R.sx_u, (long long)(nrow - row) * R.sy_u);
+        }
+    }
+}
+
+// Column-range gather of one lane: in each of the three neighbouring chunk
+// columns the rows row-1..row+1 are consecutive chunks, hence one contiguous
+// particle range (unless the stencil wraps around the column or is clipped),
+// read directly from global memory (neighbouring lanes read overlapping
+// ranges, so the loads hit L1). Same terms in the same order as the other
+// gathers, so the sums agree bitwise; suits sparse grids (about one particle
+// per chunk), where staging a window costs more than it saves.
+template <int PREC, int DYN>
+__device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
+                                               const typename PartOf<PREC>::T* __restrict__ P,
+                                               const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc) {
+    const int32_t lc = (int32_t)(cell - R.c0);
+    const int32_t col = lc / R.rows, row = lc - col * R.rows;
+    const bool rows_inside = row >= 1 && row + 1 < R.rows;
+#pragma unroll 1
+    for (int dc = -1; dc <= 1; dc++) {
+        int ncol = col + dc;
+        bool cw = false;
+        if (R.periodic) {
+            if (ncol < 0) { ncol += R.cols; cw = true; }
+            else if (ncol >= R.cols) { ncol -= R.cols; cw = true; }
+        } else if (ncol < 0 || ncol >= R.cols) continue;
+        const bool mi_c = R.min_image && (cw || R.mi_small);
+        const int32_t shx = -dc * R.sx_i;
+        const long long rshx = -(long long)(ncol - col) * R.sx_u;
+        const int64_t cb = R.c0 + (int64_t)ncol * R.rows;
+        if (rows_inside) {
+            const int32_t g0 = C.start[cb + row - 1], g1 = C.start[cb + row];
+            const int32_t g2 = C.start[cb + row + 1], g3 = C.start[cb + row + 2];
+            const int32_t self = (dc == 0) ? (int32_t)s : -1;
+            const bool raw = cw && !R.min_image;
+#pragma unroll 2
+            for (int32_t j = g0; j < g3; j++) {
+                if (j == self) continue;
+                const int dr = j < g1 ? -1 : (j < g2 ? 0 : 1);
+                int32_t uq = 0;
+                if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
+                if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)dr * R.sy_u, acc);
+                else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi_c, acc);
+            }
+        } else {
+#pragma unroll 1
+            for (int dr = -1; dr <= 1; dr++) {
+                int nrow = row + dr;
+                bool rw = false;
+                if (R.periodic) {
+                    if (nrow < 0) { nrow += R.rows; rw = true; }
+                    else if (nrow >= R.rows) { nrow -= R.rows; rw = true; }
+                } else if (nrow < 0 || nrow >= R.rows) continue;
+                const int32_t b = C.start[cb + nrow], e = C.start[cb + nrow + 1];
+                const bool mi = mi_c || (R.min_image && rw);
+                const bool raw = (cw || rw) && !R.min_image;
+                for (int32_t j = b; j < e; j++) {
+                    if (j == (int32_t)s) continue;
+                    int32_t uq = 0;
+                    if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
+                    if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)(nrow - row) * R.sy_u, acc);
+                    else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi, acc);
+                }
+            }
         }
     }
 }
@@ -699,6 +807,7 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
 // table. Windows that do not fit fall back to the global gather (same terms
 // in the same order, bitwise-identical sums).
 // ---------------------------------------------------------------------------
+constexpr int kNumGatherModes = 3; // staged window, per-chunk global, per-column global
 constexpr int kStageParts = 256;   // staged particles per window
 constexpr int kPassThreads = 128;
 constexpr int kPassWarps = kPassThreads / 32;
@@ -740,7 +849,10 @@ __device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s,
     unsigned vmask = __ballot_sync(full, valid);
     int first = vmask ? __ffs(vmask) - 1 : 0;
     int32_t rep0 = __shfl_sync(full, rep, first);
-    bool uniform = __all_sync(full, !valid || rep == rep0);
+    // windows are replica-uniform; the mixed form stages no window whose
+    // stencil may wrap without minimum image (raw displacements, see above)
+    const bool stageable = PREC == kPrecFP64 || !(R.periodic && !R.min_image);
+    bool uniform = __all_sync(full, !valid || (rep == rep0 && stageable));
     Me<PREC, DYN> me;
     if (valid) me = make_me<PREC, DYN>(C, R, rep, s, P);
     int32_t col = 0, row = 0;
@@ -889,7 +1001,10 @@ __device__ __forceinline__ void gather_warp(const Ctx& C, bool valid, int64_t s,
         __syncwarp();
         pending &= ~amask;
     }
-    if (valid && (!want || !uniform || C.gather_mode != 0)) gather_global<PREC, DYN>(C, R, rep, s, cell, P, me, acc);
+    if (valid && (!want || !uniform || C.gather_mode != 0)) {
+        if (want && C.gather_mode == 2) gather_columns<PREC, DYN>(C, R, rep, s, cell, P, me, acc);
+        else gather_global<PREC, DYN>(C, R, rep, s, cell, P, me, acc);
+    }
 }
 
 // ===========================================================================
@@ -929,7 +1044,17 @@ static __device__ __forceinline__ void add_wall_forces(const Ctx& C, int32_t rep
         if (sp.wall != MAVI_WALL_POTENTIAL) continue;
         if (sp.geometry == MAVI_GEOM_CIRCLE) {   // signed_pos (src/configs.jl:154-163)
             double drx = x - sp.cx, dry = y - sp.cy;
-            double dist = sqrt(drx * drx + dry * dry);
+            double r2 = drx * drx + dry * dry;
+            if (sp.pot_kind == MAVI_DYN_HARM_TRUNC && sp.pot_mode != MAVI_POTMODE_OUTSIDE) {
+                // the truncated potential acts only where |dist - radius| <= dist_max
+                // (inside and repulsion modes): skip the rest without the sqrt,
+                // with a relative margin far above the rounding of dist
+                const double dmax = sp.pot_params[3];
+                const double lo = sp.radius - dmax, hi = sp.radius + dmax;
+                if (lo > 0 && r2 < lo * lo * (1.0 - 1e-9)) continue;
+                if (sp.pot_mode == MAVI_POTMODE_REPULSION && r2 > hi * hi * (1.0 + 1e-9)) continue;
+            }
+            double dist = sqrt(r2);
             double hx = drx / dist, hy = dry / dist;
             drx = drx - hx * sp.radius;
             dry = dry - hy * sp.radius;
@@ -1199,13 +1324,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t g = (int64_t)blockIdx.x * kRingWarps + w;
     if (g >= total_rings) return;   // whole warp exits together
-    // replica of ring g: binary search over ring offsets
-    int lo = 0, hi = C.num_reps - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (C.reps[mid].ring0 <= g) lo = mid; else hi = mid - 1;
-    }
-    const int32_t rep = lo;
+    const int32_t rep = C.ring_rep[g];
     const DevRep& R = C.reps[rep];
     const MaviRingsCfg& rc = C.rcfg[rep];
     const int32_t rl = (int32_t)(g - R.ring0);
@@ -1260,53 +1379,18 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
     const double a0 = n * rc.l_spring[t] / rc.p0[t];
     const double fmod_area = rc.k_area[t] * (area - a0 * a0);
     const double kb = rc.k_bend[t];
-    // overdamped active update parameters
-    const double theta = C.ring_pol[g];
-    double ps, pc;
-    sincos(theta, &ps, &pc);
+    // overdamped active update parameters; (cos, sin) of the polarisation
+    // come from k_ring_pol (one thread per ring, not one warp)
+    double pc = 0.0, ps = 0.0;
+    if (do_update) {
+        const double2 cs = C.ring_cs[g];
+        pc = cs.x;
+        ps = cs.y;
+    }
     const double vo = rc.vo[t], mu = rc.mobility[t], dt = R.dt;
     double vcx = 0, vcy = 0;
-    for (int p = lane; p < n; p += 32) {
-        int pm = p == 0 ? n - 1 : p - 1, pp = p == n - 1 ? 0 : p + 1;
-        double2 xc = P[p], xm = P[pm], xp = P[pp];
-        double fx = 0, fy = 0;
-        // springs: f = -k (d - l) dr/d on (p, p+1) with dr = x_p - x_{p+1};
-        // particle p is the first end of spring p and the second of spring p-1
-        {
-            double2 d = diff(xc, xp);
-            double dist = sqrt(d.x * d.x + d.y * d.y);
-            double sc = -k_s * (dist - l_s) / dist;
-            fx += sc * d.x; fy += sc * d.y;
-            double2 e = diff(xm, xc);
-            double de = sqrt(e.x * e.x + e.y * e.y);
-            double se = -k_s * (de - l_s) / de;
-            fx -= se * e.x; fy -= se * e.y;
-        }
-        // area: F_p -= k_area (A - A0) * (dr.y, -dr.x)/2, dr = x_{p+1} - x_{p-1}
-        {
-            double2 d = diff(xp, xm);
-            fx -= fmod_area * (d.y / 2);
-            fy -= fmod_area * (-d.x / 2);
-        }
-        if (kb != 0.0) {
-            // bending: E = kb sum_i (1 - cos theta_i); contributions of the
-            // angles at p-1, p and p+1.
-            int pmm = pm == 0 ? n - 1 : pm - 1, ppp = pp == n - 1 ? 0 : pp + 1;
-            double2 xmm = P[pmm], xpp = P[ppp];
-            auto dcos = [&](double2 a, double2 b, double2& dca, double2& dcb) {
-                double la = sqrt(a.x * a.x + a.y * a.y), lb = sqrt(b.x * b.x + b.y * b.y);
-                double c = (a.x * b.x + a.y * b.y) / (la * lb);
-                dca = make_double2(b.x / (la * lb) - c * a.x / (la * la), b.y / (la * lb) - c * a.y / (la * la));
-                dcb = make_double2(a.x / (la * lb) - c * b.x / (lb * lb), a.y / (la * lb) - c * b.y / (lb * lb));
-            };
-            double2 dca, dcb;
-            dcos(diff(xc, xm), diff(xp, xc), dca, dcb);       // angle at p
-            fx += kb * (dca.x - dcb.x); fy += kb * (dca.y - dcb.y);
-            dcos(diff(xp, xc), diff(xpp, xp), dca, dcb);      // angle at p+1: p is its "i-1"
-            fx += -kb * dca.x; fy += -kb * dca.y;
-            dcos(diff(xm, xmm), diff(xc, xm), dca, dcb);      // angle at p-1: p is its "i+1"
-            fx += kb * dcb.x; fy += kb * dcb.y;
-        }
+    // pair + wall forces, then the overdamped active update of particle p
+    auto finish = [&](int p, double2 xc, double fx, double fy) {
         int32_t s = S[p];
         if constexpr (PREC == kPrecFP64) { double2 f = C.fd[s]; fx += f.x; fy += f.y; }
         else { float2 f = C.ff[s]; fx += f.x; fy += f.y; }
@@ -1314,7 +1398,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         if (!do_update) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
             else C.ff[s] = make_float2((float)fx, (float)fy);
-            continue;
+            return;
         }
         double vx = __dadd_rn(__dmul_rn(vo, pc), __dmul_rn(mu, fx));
         double vy = __dadd_rn(__dmul_rn(vo, ps), __dmul_rn(mu, fy));
@@ -1326,6 +1410,95 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         C.pos_out[s] = make_double2(x, y);
         C.uid_out[s] = C.uid_cur[s];
         C.rep_out[s] = rep;
+    };
+    if (n <= 32) {
+        // One particle per lane; neighbours' bond data by shuffles. Each bond
+        // length and its inverse are formed once (one sqrt and one division
+        // per particle), and the bending gradients use the inverse lengths.
+        // The mixed form evaluates these ring-internal terms in FP32 on FP64
+        // differences; the FP64 form in double.
+        using T = typename std::conditional<PREC == kPrecFP64, double, float>::type;
+        const unsigned full = 0xffffffffu;
+        const bool act = lane < n;
+        const int p = act ? lane : 0;
+        const int pp = p == n - 1 ? 0 : p + 1, pm = p == 0 ? n - 1 : p - 1;
+        const double2 xc = P[p], xp = P[pp], xm = P[pm];
+        const double2 bd = diff(xp, xc);                       // bond p: x_{p+1} - x_p
+        const T bx = (T)bd.x, by = (T)bd.y;
+        const T L = sqrt(bx * bx + by * by);
+        const T inv = T(1) / L;
+        const T bmx = __shfl_sync(full, bx, pm), bmy = __shfl_sync(full, by, pm);   // bond p-1
+        const T Lm = __shfl_sync(full, L, pm), invm = __shfl_sync(full, inv, pm);
+        const T ks = (T)k_s, ls = (T)l_s;
+        // springs (p, p+1) and (p-1, p)
+        const T sp = ks * (L - ls) * inv, sm = ks * (Lm - ls) * invm;
+        T fx = sp * bx - sm * bmx;
+        T fy = sp * by - sm * bmy;
+        // area: F_p -= k_area (A - A0) * (dr.y, -dr.x)/2, dr = x_{p+1} - x_{p-1}
+        {
+            const double2 d = diff(xp, xm);
+            const T fa = (T)fmod_area;
+            fx -= fa * (T)(d.y / 2);
+            fy -= fa * (T)(-d.x / 2);
+        }
+        // bending: angle at p between a = bond p-1 and b = bond p,
+        // c = a.b/(|a||b|); dc/da = b/(|a||b|) - c a/|a|^2, dc/db = a/(|a||b|) - c b/|b|^2
+        const T kbt = (T)kb;
+        const T iab = invm * inv;
+        const T c = (bmx * bx + bmy * by) * iab;
+        const T dcax = bx * iab - c * bmx * (invm * invm), dcay = by * iab - c * bmy * (invm * invm);
+        const T dcbx = bmx * iab - c * bx * (inv * inv), dcby = bmy * iab - c * by * (inv * inv);
+        const T nax = __shfl_sync(full, dcax, pp), nay = __shfl_sync(full, dcay, pp);   // angle at p+1
+        const T pbx = __shfl_sync(full, dcbx, pm), pby = __shfl_sync(full, dcby, pm);   // angle at p-1
+        if (kb != 0.0) {
+            fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
+            fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
+        }
+        if (act) finish(p, xc, (double)fx, (double)fy);
+    } else {
+        for (int p = lane; p < n; p += 32) {
+            int pm = p == 0 ? n - 1 : p - 1, pp = p == n - 1 ? 0 : p + 1;
+            double2 xc = P[p], xm = P[pm], xp = P[pp];
+            double fx = 0, fy = 0;
+            // springs: f = -k (d - l) dr/d on (p, p+1) with dr = x_p - x_{p+1};
+            // particle p is the first end of spring p and the second of spring p-1
+            {
+                double2 d = diff(xc, xp);
+                double dist = sqrt(d.x * d.x + d.y * d.y);
+                double sc = -k_s * (dist - l_s) / dist;
+                fx += sc * d.x; fy += sc * d.y;
+                double2 e = diff(xm, xc);
+                double de = sqrt(e.x * e.x + e.y * e.y);
+                double se = -k_s * (de - l_s) / de;
+                fx -= se * e.x; fy -= se * e.y;
+            }
+            // area: F_p -= k_area (A - A0) * (dr.y, -dr.x)/2, dr = x_{p+1} - x_{p-1}
+            {
+                double2 d = diff(xp, xm);
+                fx -= fmod_area * (d.y / 2);
+                fy -= fmod_area * (-d.x / 2);
+            }
+            if (kb != 0.0) {
+                // bending: E = kb sum_i (1 - cos theta_i); contributions of the
+                // angles at p-1, p and p+1.
+                int pmm = pm == 0 ? n - 1 : pm - 1, ppp = pp == n - 1 ? 0 : pp + 1;
+                double2 xmm = P[pmm], xpp = P[ppp];
+                auto dcos = [&](double2 a, double2 b, double2& dca, double2& dcb) {
+                    double la = sqrt(a.x * a.x + a.y * a.y), lb = sqrt(b.x * b.x + b.y * b.y);
+                    double c = (a.x * b.x + a.y * b.y) / (la * lb);
+                    dca = make_double2(b.x / (la * lb) - c * a.x / (la * la), b.y / (la * lb) - c * a.y / (la * la));
+                    dcb = make_double2(a.x / (la * lb) - c * b.x / (lb * lb), a.y / (la * lb) - c * b.y / (lb * lb));
+                };
+                double2 dca, dcb;
+                dcos(diff(xc, xm), diff(xp, xc), dca, dcb);       // angle at p
+                fx += kb * (dca.x - dcb.x); fy += kb * (dca.y - dcb.y);
+                dcos(diff(xp, xc), diff(xpp, xp), dca, dcb);      // angle at p+1: p is its "i-1"
+                fx += -kb * dca.x; fy += -kb * dca.y;
+                dcos(diff(xm, xmm), diff(xc, xm), dca, dcb);      // angle at p-1: p is its "i+1"
+                fx += kb * dcb.x; fy += kb * dcb.y;
+            }
+            finish(p, xc, fx, fy);
+        }
     }
     if (!do_update) return;
 #pragma unroll
@@ -1333,26 +1506,45 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         vcx += __shfl_xor_sync(0xffffffffu, vcx, o);
         vcy += __shfl_xor_sync(0xffffffffu, vcy, o);
     }
-    if (lane == 0) {
-        vcx /= n;
-        vcy /= n;
-        double speed = sqrt(vcx * vcx + vcy * vcy);
-        double cr = 0.0;
-        if (speed != 0) {
-            cr = (pc * vcy - ps * vcx) / speed;
-            if (fabs(cr) > 1) cr = jsign(cr);
-        }
-        double nz;
-        if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + rl];
-        else nz = philox_normal(C.seed, (uint64_t)g, (uint64_t)(C.d_step[0] - 1));
-        double d_theta = 1 / rc.relax_time[t] * asin(cr) * dt + sqrt(2 * rc.rot_diff[t] * dt) * nz;
-        C.ring_pol[g] = theta + d_theta;
-    }
+    if (lane == 0) C.ring_vc[g] = make_double2(vcx / n, vcy / n);
 }
 
 // ===========================================================================
 // user-order staging <-> sorted state
 // ===========================================================================
+// Polarisation of each ring (src/rings/integration.jl:340-351), one thread
+// per ring: theta += asin(p x v_mean / |v_mean|) / tau dt + sqrt(2 D dt) xi,
+// then (cos, sin) of the new angle for the next step. With update == 0 it
+// only refreshes (cos, sin) (after an upload).
+static __global__ void k_ring_pol(Ctx C, int64_t total_rings, int32_t update) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total_rings) return;
+    double theta = C.ring_pol[g];
+    if (update) {
+        const int32_t rep = C.ring_rep[g];
+        const DevRep& R = C.reps[rep];
+        const MaviRingsCfg& rc = C.rcfg[rep];
+        const int t = C.ring_types[g] - 1;
+        const double2 vc = C.ring_vc[g], cs = C.ring_cs[g];
+        const double dt = R.dt;
+        const double speed = sqrt(vc.x * vc.x + vc.y * vc.y);
+        double cr = 0.0;
+        if (speed != 0) {
+            cr = (cs.x * vc.y - cs.y * vc.x) / speed;
+            if (fabs(cr) > 1) cr = jsign(cr);
+        }
+        double nz;
+        if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (g - R.ring0)];
+        else nz = philox_normal(C.seed, (uint64_t)g, (uint64_t)(C.d_step[0] - 1));
+        const double d_theta = 1 / rc.relax_time[t] * asin(cr) * dt + sqrt(2 * rc.rot_diff[t] * dt) * nz;
+        theta = theta + d_theta;
+        C.ring_pol[g] = theta;
+    }
+    double sn, cn;
+    sincos(theta, &sn, &cn);
+    C.ring_cs[g] = make_double2(cn, sn);
+}
+
 static __global__ void k_gather_user(Ctx C, const double2* __restrict__ pos_user, const double2* __restrict__ vel_user,
                               const double* __restrict__ pol_user) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -33,6 +33,7 @@ template <int PREC>
 void rings_terms(MaviSystem* s, int do_update) {
     unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
     k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update);
+    if (do_update) k_ring_pol<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
 }
 
 // The passes of one step after the chunk rebuild.

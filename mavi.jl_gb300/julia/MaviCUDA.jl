@@ -203,7 +203,7 @@ function handle!(system)
     haskey(HANDLES, system) && return HANDLES[system].ptr
     dev = system.int_cfg.device
     opt = COptions(dev.precision == :mixed ? PREC_MIXED : PREC_FP64, NOISE_DEVICE, dev.seed,
-                   dev.device, 1, 0, 0)
+                   dev.device, 1, 0, -1)   # gather: autotuned
     params = Ref(replica_params(system))
     st = system.state
     vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)

@@ -147,6 +147,11 @@ class OracleSystem:
         return int(self.lib.oracle_noise_count(self.h))
 
     def step(self, nsteps: int = 1, mode=SEQUENTIAL, noise=None):
+        """Advance nsteps; steps that draw random numbers (Szabo, RTP, rings)
+        take them from `noise` (nsteps * noise_count() numbers, step-major)."""
+        need = self.noise_count() * int(nsteps)
+        if need and (noise is None or np.size(noise) < need):
+            raise ValueError(f"this step consumes {self.noise_count()} noise numbers per step: pass {need}")
         noise = None if noise is None else np.ascontiguousarray(noise, dtype=np.float64).reshape(-1)
         st = self.lib.oracle_step(self.h, int(nsteps), mode, _dp(noise))
         self._ck(st, "step")
@@ -198,6 +203,12 @@ def struct_sizes():
     names = ["MaviSpace", "MaviRingsCfg", "MaviDynamicCfg", "MaviReplicaParams", "MaviOptions", "MaviStats",
              "MaviProfile"]
     return {names[k]: out[k] for k in range(n)}
+
+
+def noise_for(kind: int, count: int, rng) -> np.ndarray:
+    """Noise numbers of one step: RTP draws uniforms, Szabo and rings normals."""
+    from mavi_gb300 import abi
+    return rng.random(count) if kind == abi.MAVI_STEP_RTP else rng.standard_normal(count)
 
 
 def from_system(system, nthreads: int = 1, step_kind=None) -> OracleSystem:

@@ -263,26 +263,31 @@ def test_mixed_force_error_relaxed_packing(mg, orc):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_staged_gather_equals_global_gather_bitwise(mg, precision):
-    """The warp-staged shared-memory gather and the per-thread global gather
-    sum the same terms in the same order."""
+    """The warp-staged shared-memory gather, the per-chunk global gather, the
+    per-column gather and the autotuned choice sum the same terms in the same
+    order."""
     out = []
-    for gather in ("staged", "global"):
+    for gather in ("staged", "global", "columns", "auto"):
         s = soft_disks(mg, 8192, precision=precision)
         s.int_cfg.device.gather = gather
         f = s.calc_forces()
         mg.run_system(s, num_steps=20, step_func=mg.overdamped_step)
         out.append((f, s.state.pos.copy()))
         s.close()
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1])
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0])
+        assert np.array_equal(out[0][1], o[1])
     l = []
-    for gather in ("staged", "global"):
+    for gather in ("staged", "global", "columns", "auto"):
         s = lj_grid(mg, 40, 40, wall="periodic", precision=precision)
         s.int_cfg.device.gather = gather
         mg.run_system(s, num_steps=20)
         l.append(s.state.pos.copy())
+        if gather == "auto":
+            assert s.stats().gather_mode in (0, 1, 2)
         s.close()
-    assert np.array_equal(l[0], l[1])
+    for x in l[1:]:
+        assert np.array_equal(l[0], x)
 
 
 def test_energy_drift_mixed_matches_fp64(mg):
@@ -304,3 +309,21 @@ def test_energy_drift_mixed_matches_fp64(mg):
     driftmx = abs(emx[-1] - emx[0]) / scale
     assert np.max(np.abs(emx - e64)) / scale < 1e-6
     assert abs(driftmx - drift64) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_periodic_circle_raw_displacement(mg, orc, precision):
+    """Periodic walls on a circle: the stencil wraps but the reference takes
+    the raw difference r1 - r2 (no minimum image) for wrapped neighbours."""
+    from mavi_gb300 import workloads
+    systems, step = workloads.lj_batch(num_replicas=2, precision=precision, n_min=1500, n_max=3000,
+                                       quadrants=("periodic_circle",))
+    b = mg.SystemBatch(systems, step)
+    forces = b.calc_forces()
+    for k, s in enumerate(systems):
+        ref = orc.from_system(s, step_kind=step.kind)
+        err = rel_force_err(forces[k], ref.forces())
+        assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), (k, err)
+        ref.close()
+    b.run(50)
+    b.close()
