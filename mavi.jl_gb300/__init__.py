@@ -20,6 +20,10 @@ from .system import (
 from .init_states import fixed_speed_vel, maxwell_vel, random_vel, rectangular_grid
 from . import rings
 from . import replicas
+from . import experiments
+from .experiments import (
+    CheckpointCfg, DelayedCfg, Experiment, ExperimentCfg, ManyColsCfg, load_experiment, run_experiment,
+)
 from .replicas import my_replicas, shard_replicas
 
 __all__ = [n for n in dir() if not n.startswith("_")]

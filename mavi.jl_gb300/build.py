@@ -29,7 +29,8 @@ def nvcc() -> str:
 
 def _compile(src: str, verbose: bool) -> pathlib.Path:
     out = OBJ / (pathlib.Path(src).stem + ".o")
-    cmd = [nvcc(), *FLAGS, *ARCH, "-c", str(CSRC / src), "-o", str(out)]
+    extra = os.environ.get("MAVI_NVCC_FLAGS", "").split()   # tuning defines, e.g. -DMAVI_PASS_BLOCKS_MIXED=6
+    cmd = [nvcc(), *FLAGS, *extra, *ARCH, "-c", str(CSRC / src), "-o", str(out)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -20,8 +20,8 @@ static void launch_count(MaviSystem* s) {
     record_begin(s, MAVI_KERNEL_BIN_COUNT);
     cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
     cudaMemsetAsync(s->C.tile_sum, 0, sizeof(int32_t) * s->ntiles, s->stream);
-    if (s->prec == MAVI_PREC_FP64) count_fp64(s, 0);
-    else count_mixed(s, 0);
+    if (s->prec == MAVI_PREC_FP64) count_fp64(s, 2);
+    else count_mixed(s, 2);
     record_end(s, MAVI_KERNEL_BIN_COUNT);
 }
 
@@ -650,6 +650,9 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     ALLOC(C.uid_cur, M); ALLOC(C.uid_out, M); ALLOC(C.rep_cur, M); ALLOC(C.rep_out, M);
     ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.rank, M); ALLOC(C.src_of, M);
     ALLOC(C.key_of, M); ALLOC(C.cell_at, M);
+    // no chunk guess before the first histogram
+    if (cudaMemset(C.cell_out, 0xff, sizeof(int32_t) * M) != cudaSuccess)
+        return bail(fail(s, MAVI_ERR_CUDA, "cudaMemset failed for cell_out"));
     ALLOC(C.slot_of, N);
     ALLOC(C.count, s->Ctot); ALLOC(C.start, s->Ctot + 1);
     ALLOC(C.tile_sum, s->ntiles);
@@ -659,11 +662,22 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings);
         ALLOC(ring_rep_d, s->total_rings); ALLOC(C.ring_cs, s->total_rings); ALLOC(C.ring_vc, s->total_rings);
     }
+    // chunk-centre tables (units of u) for the fast binning check
+    std::vector<double> cxu_h, cyu_h;
+    for (int r = 0; r < s->R; r++) {
+        DevRep& R = s->reps_h[r];
+        R.ccol0 = (int64_t)cxu_h.size();
+        R.crow0 = (int64_t)cyu_h.size();
+        for (int c = 0; c < R.cols; c++) cxu_h.push_back(std::fma((double)c, R.chunk_l, R.cx0) * R.inv_u);
+        for (int q = 0; q < R.rows; q++) cyu_h.push_back(std::fma(-(double)q, R.chunk_h, R.cy0) * R.inv_u);
+    }
+    double *cxu_d = nullptr, *cyu_d = nullptr;
     DevRep* reps_d = nullptr;
     MaviSpace* spaces_d = nullptr;
     MaviRingsCfg* rcfg_d = nullptr;
     FixPair* fix_d = nullptr;
     ALLOC(reps_d, s->R); ALLOC(spaces_d, (int64_t)s->R * MAVI_MAX_SPACES); ALLOC(rcfg_d, s->R);
+    ALLOC(cxu_d, (int64_t)cxu_h.size()); ALLOC(cyu_d, (int64_t)cyu_h.size());
     ALLOC(fix_d, (int64_t)s->R * MAVI_MAX_TYPES * MAVI_MAX_TYPES);
     ALLOC(C.err, 1); ALLOC(C.d_step, 1);
     ALLOC(s->pos_user, N); ALLOC(s->f_user, N);
@@ -676,6 +690,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     C.ring_types = ring_types_d;
     C.ring_rep = ring_rep_d;
     C.reps = reps_d;
+    C.cxu = cxu_d;
+    C.cyu = cyu_d;
     C.spaces = spaces_d;
     C.rcfg = rcfg_d;
     C.fix = fix_d;
@@ -726,6 +742,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         }
     }
     CUDA_TRY(s, cudaMemcpyAsync(reps_d, s->reps_h.data(), sizeof(DevRep) * s->R, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(cxu_d, cxu_h.data(), sizeof(double) * cxu_h.size(), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(cyu_d, cyu_h.data(), sizeof(double) * cyu_h.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(spaces_d, spaces_h.data(), sizeof(MaviSpace) * spaces_h.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(rcfg_d, rcfg_h.data(), sizeof(MaviRingsCfg) * s->R, cudaMemcpyHostToDevice, s->stream));
     std::vector<FixPair> fix_h((size_t)s->R * MAVI_MAX_TYPES * MAVI_MAX_TYPES);

@@ -64,6 +64,7 @@ struct DevRep {
     int32_t half_bx_i, half_by_i;
     int32_t half_sx_i, half_sy_i;  // half chunk in units
     double cx0, cy0;       // centre of chunk (row 0, col 0)
+    int64_t ccol0, crow0;  // first entry of this replica in the chunk-centre tables
     double mdt;            // mobility * dt
     float mdt_f;
     int32_t mi_small;      // grid too small to skip the minimum image for unwrapped neighbours

@@ -67,6 +67,7 @@ struct Ctx {
     double *ring_area;
     const int32_t *ring_types;
     const int32_t *ring_rep;   // replica of each ring
+    const double *cxu, *cyu;   // chunk-centre x per column, y per row, in units of u
     double2 *ring_cs;          // (cos, sin) of the ring's polarisation angle
     double2 *ring_vc;          // mean particle velocity of the ring in the last update
     // descriptors
@@ -228,10 +229,10 @@ __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64
     if (!R.has_chunks) return -1;
     int32_t lc = (int32_t)(cell - R.c0);
     int32_t col = lc / R.rows, row = lc - col * R.rows;
-    double cx = fma((double)col, R.chunk_l, R.cx0);
-    double cy = fma(-(double)row, R.chunk_h, R.cy0);
-    int32_t ix = __double2int_rn((x - cx) * R.inv_u);
-    int32_t iy = __double2int_rn((y - cy) * R.inv_u);
+    // chunk centres in units come from per-column / per-row tables: one FP64
+    // FMA and one conversion per coordinate (the FP64 pipe is the scarce one)
+    int32_t ix = __double2int_rn(fma(x, R.inv_u, -C.cxu[R.ccol0 + col]));
+    int32_t iy = __double2int_rn(fma(y, R.inv_u, -C.cyu[R.crow0 + row]));
     if (abs(ix) < R.half_sx_i - 1 && abs(iy) < R.half_sy_i - 1) {
         if constexpr (PREC == kPrecMixed) C.off_out[s] = make_int2(ix, iy);
         return cell;
@@ -240,7 +241,9 @@ __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64
 }
 
 // Standalone histogram of the *_out state (upload, explicit update_chunks!,
-// the rings step). With use_guess the current chunk of the slot is the guess.
+// the rings step). The guess of the exact binning: use_guess 1 = the slot's
+// chunk in the *_cur order (rings step), 2 = the chunk the slot's particle
+// had at the last histogram (after an upload; -1 before the first one).
 template <int PREC>
 __global__ void k_count(Ctx C, int32_t use_guess) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,7 +253,8 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
     if (valid) {
         const DevRep& R = C.reps[C.rep_out[s]];
         double2 p = C.pos_out[s];
-        cell = bin_final<PREC>(C, R, s, p.x, p.y, use_guess ? (int64_t)C.cell_cur[s] : -1);
+        const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
+        cell = bin_final<PREC>(C, R, s, p.x, p.y, guess);
         cap = R.has_chunks ? R.cap : (1 << 30);
     }
     count_into_chunk(C, valid, s, cell, cap);
@@ -746,6 +750,51 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
     const int32_t lc = (int32_t)(cell - R.c0);
     const int32_t col = lc / R.rows, row = lc - col * R.rows;
     const bool rows_inside = row >= 1 && row + 1 < R.rows;
+    if (rows_inside) {
+        // all twelve chunk boundaries first (independent loads in flight
+        // together), then the three ranges
+        int32_t g[3][4];
+        int32_t ncl[3];
+        bool cws[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            int ncol = col + k - 1;
+            bool cw = false, ok = true;
+            if (R.periodic) {
+                if (ncol < 0) { ncol += R.cols; cw = true; }
+                else if (ncol >= R.cols) { ncol -= R.cols; cw = true; }
+            } else {
+                ok = ncol >= 0 && ncol < R.cols;
+            }
+            const int64_t cb = R.c0 + (int64_t)(ok ? ncol : col) * R.rows;
+#pragma unroll
+            for (int q = 0; q < 4; q++) g[k][q] = C.start[cb + row - 1 + q];
+            if (!ok) { g[k][0] = 0; g[k][3] = 0; }
+            ncl[k] = ncol;
+            cws[k] = cw;
+        }
+#pragma unroll 1
+        for (int k = 0; k < 3; k++) {
+            const int dc = k - 1;
+            const bool cw = cws[k];
+            const bool mi_c = R.min_image && (cw || R.mi_small);
+            const int32_t shx = -dc * R.sx_i;
+            const long long rshx = -(long long)(ncl[k] - col) * R.sx_u;
+            const int32_t g0 = g[k][0], g1 = g[k][1], g2 = g[k][2], g3 = g[k][3];
+            const int32_t self = (dc == 0) ? (int32_t)s : -1;
+            const bool raw = cw && !R.min_image;
+#pragma unroll 2
+            for (int32_t j = g0; j < g3; j++) {
+                if (j == self) continue;
+                const int dr = j < g1 ? -1 : (j < g2 ? 0 : 1);
+                int32_t uq = 0;
+                if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
+                if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)dr * R.sy_u, acc);
+                else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi_c, acc);
+            }
+        }
+        return;
+    }
 #pragma unroll 1
     for (int dc = -1; dc <= 1; dc++) {
         int ncol = col + dc;
@@ -758,39 +807,24 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
         const int32_t shx = -dc * R.sx_i;
         const long long rshx = -(long long)(ncol - col) * R.sx_u;
         const int64_t cb = R.c0 + (int64_t)ncol * R.rows;
-        if (rows_inside) {
-            const int32_t g0 = C.start[cb + row - 1], g1 = C.start[cb + row];
-            const int32_t g2 = C.start[cb + row + 1], g3 = C.start[cb + row + 2];
-            const int32_t self = (dc == 0) ? (int32_t)s : -1;
-            const bool raw = cw && !R.min_image;
-#pragma unroll 2
-            for (int32_t j = g0; j < g3; j++) {
-                if (j == self) continue;
-                const int dr = j < g1 ? -1 : (j < g2 ? 0 : 1);
+        // rows row-1..row+1 clipped or wrapped: chunk by chunk
+#pragma unroll 1
+        for (int dr = -1; dr <= 1; dr++) {
+            int nrow = row + dr;
+            bool rw = false;
+            if (R.periodic) {
+                if (nrow < 0) { nrow += R.rows; rw = true; }
+                else if (nrow >= R.rows) { nrow -= R.rows; rw = true; }
+            } else if (nrow < 0 || nrow >= R.rows) continue;
+            const int32_t b = C.start[cb + nrow], e = C.start[cb + nrow + 1];
+            const bool mi = mi_c || (R.min_image && rw);
+            const bool raw = (cw || rw) && !R.min_image;
+            for (int32_t j = b; j < e; j++) {
+                if (j == (int32_t)s) continue;
                 int32_t uq = 0;
                 if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
-                if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)dr * R.sy_u, acc);
-                else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi_c, acc);
-            }
-        } else {
-#pragma unroll 1
-            for (int dr = -1; dr <= 1; dr++) {
-                int nrow = row + dr;
-                bool rw = false;
-                if (R.periodic) {
-                    if (nrow < 0) { nrow += R.rows; rw = true; }
-                    else if (nrow >= R.rows) { nrow -= R.rows; rw = true; }
-                } else if (nrow < 0 || nrow >= R.rows) continue;
-                const int32_t b = C.start[cb + nrow], e = C.start[cb + nrow + 1];
-                const bool mi = mi_c || (R.min_image && rw);
-                const bool raw = (cw || rw) && !R.min_image;
-                for (int32_t j = b; j < e; j++) {
-                    if (j == (int32_t)s) continue;
-                    int32_t uq = 0;
-                    if constexpr (DYN == MAVI_DYN_RINGS) uq = C.uid_cur[j];
-                    if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)(nrow - row) * R.sy_u, acc);
-                    else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi, acc);
-                }
+                if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, (long long)(nrow - row) * R.sy_u, acc);
+                else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, dr * R.sy_i, mi, acc);
             }
         }
     }
@@ -1192,8 +1226,15 @@ __device__ __forceinline__ int64_t walls_and_bin(const Ctx& C, int32_t rep, cons
     return bin_final<PREC>(C, R, s, x, y, cell);
 }
 
+#ifndef MAVI_PASS_BLOCKS_MIXED
+#define MAVI_PASS_BLOCKS_MIXED 8   // resident pair-pass blocks per SM, mixed form (64 registers)
+#endif
+#ifndef MAVI_PASS_BLOCKS_FP64
+#define MAVI_PASS_BLOCKS_FP64 4    // FP64 form (128 registers)
+#endif
 template <int PREC, int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
-__global__ void __launch_bounds__(kPassThreads, PREC == kPrecFP64 ? 4 : 8) k_pass(Ctx C, int32_t with_wall_forces) {
+__global__ void __launch_bounds__(kPassThreads, PREC == kPrecFP64 ? MAVI_PASS_BLOCKS_FP64 : MAVI_PASS_BLOCKS_MIXED)
+k_pass(Ctx C, int32_t with_wall_forces) {
     __shared__ Stage<PREC, DYN> stage[kPassWarps];
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = s < C.M;
