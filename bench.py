@@ -279,7 +279,18 @@ def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
 FLOPS_PER_PAIR = {0: 16, 1: 23, 2: 14, 3: 23, 4: 16}
 
 
-def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind, has_vel):
+def ncu_traffic(workload, precision, kernel):
+    """DRAM bytes per launch of `kernel` from a committed ncu capture, or None."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        e = d[workload][precision]
+        return e["bytes_per_launch"] if e["kernel"] == kernel else None
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind, has_vel,
+             workload=None):
     kinds = meas["kinds"]
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     avg_ms = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1)
@@ -288,7 +299,8 @@ def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_pea
     achieved = traffic_bytes / (avg_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
     rf = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-          "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": traffic_bytes,
+          "frac": achieved / peak, "traffic": ncu_traffic(workload, precision, dom),
+          "algorithmic_bytes_per_launch": traffic_bytes,
           "avg_launch_ms": avg_ms, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     if dom == "force" and candidate_pairs:
         flops_pair = FLOPS_PER_PAIR[dyn_kind]
@@ -500,7 +512,8 @@ def main():
         params = abi.MaviReplicaParams()
         r.first.fill_params(params, r.kind)
         rf = roofline(m, n, precision, r.kind, abi, peaks, stats.candidate_pairs,
-                      fma[precision], params.dyn.kind, getattr(r.first.state, "vel", None) is not None)
+                      fma[precision], params.dyn.kind, getattr(r.first.state, "vel", None) is not None,
+                      args.workload)
         line_forms[precision] = {"value": v, "ms_per_step": m["total_ms"] / K, "roofline": rf,
                                  "kernels_ms_per_step": {k: d["ms"] / K for k, d in m["kinds"].items()},
                                  "gpu_launches": m["launches_per_step"] * K}
