@@ -583,7 +583,18 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         if (s->is_rings) {
             R.num_rings = p.rings.num_rings;
             R.nmax = p.rings.nmax;
+            for (int t = 0; t < p.rings.num_types && t < MAVI_MAX_TYPES; t++) {
+                // area0 (src/rings/configs.jl:221-226)
+                const double a0 = p.rings.num_particles[t] * p.rings.l_spring[t] / p.rings.p0[t];
+                R.ring_a0sq[t] = a0 * a0;
+                R.ring_ks_f[t] = (float)p.rings.k_spring[t];
+                R.ring_ls_f[t] = (float)p.rings.l_spring[t];
+                R.ring_kb_f[t] = (float)p.rings.k_bend[t];
+                R.ring_vo_f[t] = (float)p.rings.vo[t];
+                R.ring_mu_f[t] = (float)p.rings.mobility[t];
+            }
         }
+        R.dt_f = (float)p.dt;
         s->reps_h.push_back(R);
         s->rep_active.push_back(R.na);
         slot0 += p.num_particles;

@@ -74,6 +74,13 @@ struct DevRep {
     // (bh + bl) = 24 eps sigma^6 u g^-4 with g = 2^k u^2
     float lj_sk, lj_ah, lj_al, lj_bh, lj_bl;
     int32_t _pad2;
+    // rings, per type: target area A0^2 = (n l / p0)^2 and float copies of the
+    // ring-internal constants (mixed form)
+    double ring_a0sq[MAVI_MAX_TYPES];
+    float ring_ks_f[MAVI_MAX_TYPES], ring_ls_f[MAVI_MAX_TYPES], ring_kb_f[MAVI_MAX_TYPES];
+    float ring_vo_f[MAVI_MAX_TYPES], ring_mu_f[MAVI_MAX_TYPES];
+    float dt_f;
+    int32_t _pad3;
 };
 
 // ---------------------------------------------------------------------------

@@ -1417,8 +1417,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
     const double area = area2 / 2.0;
     if (lane == 0) C.ring_area[g] = area;
     const double k_s = rc.k_spring[t], l_s = rc.l_spring[t];
-    const double a0 = n * rc.l_spring[t] / rc.p0[t];
-    const double fmod_area = rc.k_area[t] * (area - a0 * a0);
+    const double fmod_area = rc.k_area[t] * (area - R.ring_a0sq[t]);
     const double kb = rc.k_bend[t];
     // overdamped active update parameters; (cos, sin) of the polarisation
     // come from k_ring_pol (one thread per ring, not one warp)
@@ -1429,25 +1428,43 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         ps = cs.y;
     }
     const double vo = rc.vo[t], mu = rc.mobility[t], dt = R.dt;
-    double vcx = 0, vcy = 0;
+    // the mixed form sums the ring's velocity and forms the position
+    // increment in FP32 (FP64 only for x += increment); FP64 form: all double
+    using V = typename std::conditional<PREC == kPrecFP64, double, float>::type;
+    V vcx = 0, vcy = 0;
+    const V pcv = (V)pc, psv = (V)ps;
     // pair + wall forces, then the overdamped active update of particle p
-    auto finish = [&](int p, double2 xc, double fx, double fy) {
+    auto finish = [&](int p, double2 xc, V fx, V fy) {
         int32_t s = S[p];
         if constexpr (PREC == kPrecFP64) { double2 f = C.fd[s]; fx += f.x; fy += f.y; }
         else { float2 f = C.ff[s]; fx += f.x; fy += f.y; }
-        if (R.has_wall_forces) add_wall_forces(C, rep, R, xc.x, xc.y, fx, fy);
+        if (R.has_wall_forces) {
+            double wx = 0.0, wy = 0.0;
+            add_wall_forces(C, rep, R, xc.x, xc.y, wx, wy);
+            fx += (V)wx;
+            fy += (V)wy;
+        }
         if (!do_update) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
-            else C.ff[s] = make_float2((float)fx, (float)fy);
+            else C.ff[s] = make_float2(fx, fy);
             return;
         }
-        double vx = __dadd_rn(__dmul_rn(vo, pc), __dmul_rn(mu, fx));
-        double vy = __dadd_rn(__dmul_rn(vo, ps), __dmul_rn(mu, fy));
-        vcx += vx; vcy += vy;
-        double x = __dadd_rn(xc.x, __dmul_rn(vx, dt));
-        double y = __dadd_rn(xc.y, __dmul_rn(vy, dt));
+        double x, y;
+        if constexpr (PREC == kPrecFP64) {
+            double vx = __dadd_rn(__dmul_rn(vo, pc), __dmul_rn(mu, fx));
+            double vy = __dadd_rn(__dmul_rn(vo, ps), __dmul_rn(mu, fy));
+            vcx += vx; vcy += vy;
+            x = __dadd_rn(xc.x, __dmul_rn(vx, dt));
+            y = __dadd_rn(xc.y, __dmul_rn(vy, dt));
+        } else {
+            const float vx = fmaf(R.ring_vo_f[t], pcv, R.ring_mu_f[t] * fx);
+            const float vy = fmaf(R.ring_vo_f[t], psv, R.ring_mu_f[t] * fy);
+            vcx += vx; vcy += vy;
+            x = __dadd_rn(xc.x, (double)(vx * R.dt_f));
+            y = __dadd_rn(xc.y, (double)(vy * R.dt_f));
+        }
         double dvx = 0, dvy = 0;
-        apply_walls(C, rep, R, rc.inter_dist_eq[t][t] / 2.0, x, y, dvx, dvy, false);
+        apply_walls(C, rep, R, rc.inter_dist_eq[t][t] * 0.5, x, y, dvx, dvy, false);
         C.pos_out[s] = make_double2(x, y);
         C.uid_out[s] = C.uid_cur[s];
         C.rep_out[s] = rep;
@@ -1470,7 +1487,9 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         const T inv = T(1) / L;
         const T bmx = __shfl_sync(full, bx, pm), bmy = __shfl_sync(full, by, pm);   // bond p-1
         const T Lm = __shfl_sync(full, L, pm), invm = __shfl_sync(full, inv, pm);
-        const T ks = (T)k_s, ls = (T)l_s;
+        T ks, ls, kbt;
+        if constexpr (PREC == kPrecFP64) { ks = k_s; ls = l_s; kbt = kb; }
+        else { ks = R.ring_ks_f[t]; ls = R.ring_ls_f[t]; kbt = R.ring_kb_f[t]; }
         // springs (p, p+1) and (p-1, p)
         const T sp = ks * (L - ls) * inv, sm = ks * (Lm - ls) * invm;
         T fx = sp * bx - sm * bmx;
@@ -1479,12 +1498,16 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         {
             const double2 d = diff(xp, xm);
             const T fa = (T)fmod_area;
-            fx -= fa * (T)(d.y / 2);
-            fy -= fa * (T)(-d.x / 2);
+            if constexpr (PREC == kPrecFP64) {
+                fx -= fa * (d.y / 2);
+                fy -= fa * (-d.x / 2);
+            } else {
+                fx -= fa * ((float)d.y * 0.5f);
+                fy -= fa * (-(float)d.x * 0.5f);
+            }
         }
         // bending: angle at p between a = bond p-1 and b = bond p,
         // c = a.b/(|a||b|); dc/da = b/(|a||b|) - c a/|a|^2, dc/db = a/(|a||b|) - c b/|b|^2
-        const T kbt = (T)kb;
         const T iab = invm * inv;
         const T c = (bmx * bx + bmy * by) * iab;
         const T dcax = bx * iab - c * bmx * (invm * invm), dcay = by * iab - c * bmy * (invm * invm);
@@ -1495,7 +1518,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
             fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
             fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
         }
-        if (act) finish(p, xc, (double)fx, (double)fy);
+        if (act) finish(p, xc, (V)fx, (V)fy);
     } else {
         for (int p = lane; p < n; p += 32) {
             int pm = p == 0 ? n - 1 : p - 1, pp = p == n - 1 ? 0 : p + 1;
@@ -1538,7 +1561,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
                 dcos(diff(xm, xmm), diff(xc, xm), dca, dcb);      // angle at p-1: p is its "i+1"
                 fx += kb * dcb.x; fy += kb * dcb.y;
             }
-            finish(p, xc, fx, fy);
+            finish(p, xc, (V)fx, (V)fy);
         }
     }
     if (!do_update) return;
@@ -1547,7 +1570,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         vcx += __shfl_xor_sync(0xffffffffu, vcx, o);
         vcy += __shfl_xor_sync(0xffffffffu, vcy, o);
     }
-    if (lane == 0) C.ring_vc[g] = make_double2(vcx / n, vcy / n);
+    if (lane == 0) C.ring_vc[g] = make_double2((double)vcx, (double)vcy);   // sums; k_ring_pol divides
 }
 
 // ===========================================================================
@@ -1566,7 +1589,9 @@ static __global__ void k_ring_pol(Ctx C, int64_t total_rings, int32_t update) {
         const DevRep& R = C.reps[rep];
         const MaviRingsCfg& rc = C.rcfg[rep];
         const int t = C.ring_types[g] - 1;
-        const double2 vc = C.ring_vc[g], cs = C.ring_cs[g];
+        const double2 vs = C.ring_vc[g], cs = C.ring_cs[g];
+        const int32_t n = rc.num_particles[t];
+        const double2 vc = make_double2(vs.x / n, vs.y / n);
         const double dt = R.dt;
         const double speed = sqrt(vc.x * vc.x + vc.y * vc.y);
         double cr = 0.0;

@@ -283,20 +283,22 @@ def run_experiment(experiment: Experiment, stop_func: Callable | None = None, ch
     col = experiment.col
     root = pathlib.Path(cfg.root)
     (root / COL_DIRNAME).mkdir(parents=True, exist_ok=True)
-    if experiment.checkpoint is not None:
+    # checkpoints only when the configuration asks for them
+    cp = experiment.checkpoint if cfg.checkpoint_cfg is not None else None
+    if cp is not None:
         for n in ("1", "2"):
             (root / CHECKPOINT_DIRNAME / n).mkdir(parents=True, exist_ok=True)
     dt = float(system.int_cfg.dt)
-    delta = cfg.checkpoint_cfg.delta_time if cfg.checkpoint_cfg is not None else None
+    delta = cfg.checkpoint_cfg.delta_time if cp is not None else None
     while True:
-        k = schedule(float(system.time_info.time), dt, cfg.tf, col, experiment.checkpoint, delta, check_every)
+        k = schedule(float(system.time_info.time), dt, cfg.tf, col, cp, delta, check_every)
         if k == 0:
             break
         system.run(k, experiment.custom_step)          # one mavi_step(k); state downloaded once
         col.collect(system)
-        if experiment.checkpoint is not None:
+        if cp is not None:
             t = float(system.time_info.time)
-            if not (t - experiment.checkpoint.last_time < delta):
+            if not (t - cp.last_time < delta):
                 _save_checkpoint(experiment)
         if stop_func is not None and stop_func(system):
             break

@@ -83,7 +83,7 @@ def test_event_steps_match_the_reference_loop(mg, tmp_path, dt, tf, delay, delta
 @pytest.mark.gpu
 def test_experiment_on_gpu_and_resume_from_checkpoint(mg, tmp_path):
     ex = mg.experiments
-    tf, dt = 0.3, 1e-3
+    tf, dt = 0.35, 1e-3
     s = lj_grid(mg, 16, 16, wall="periodic", dt=dt)
     exp = ex.Experiment(ex.ExperimentCfg(tf=tf, root=str(tmp_path / "a"), checkpoint_cfg=ex.CheckpointCfg(0.1)),
                         ex.DelayedCfg(0.05), s)
