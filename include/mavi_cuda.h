@@ -44,6 +44,8 @@ extern "C" {
 #define MAVI_ERR_UNSUPPORTED    7  /* combination the reference does not define             */
 #define MAVI_ERR_NO_DEVICE      8  /* no CUDA device available                              */
 #define MAVI_ERR_NOISE_MISSING  9  /* injected-noise mode but no noise supplied for a step  */
+#define MAVI_ERR_NEIGHBOR_OVERFLOW 10 /* more rings particle neighbours than MAVI_MAX_NEIGHBORS
+                                      (reference: BoundsError, src/rings/neighbors.jl:107-113) */
 
 /* ---- enums -------------------------------------------------------------- */
 /* State kinds: src/states.jl:75 (SecondLawState), :104 (SelfPropelledState),
@@ -106,6 +108,7 @@ extern "C" {
 #define MAVI_PE_STENCIL   0  /* over the chunk-stencil pair set the forces use            */
 #define MAVI_PE_ALL_PAIRS 1  /* all pairs i<j, as src/quantities.jl:46-66 does for LJ      */
 
+#define MAVI_MAX_NEIGHBORS 15  /* neighbour list length (src/rings/rings.jl:133, 145) */
 #define MAVI_MAX_SPACES 4
 #define MAVI_MAX_LINES  16
 #define MAVI_MAX_TYPES  4
@@ -291,6 +294,22 @@ int mavi_energies(MaviSystem* sys, int32_t pe_mode, double* ke, double* pe);
 
 /* time_info (src/systems.jl:30-33, src/integration.jl:500-503). */
 int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
+
+/* Particle neighbour lists of the rings model (NeighborsCfg / ParticleNeighbors,
+ * src/rings/neighbors.jl:8-136, src/rings/rings.jl:143-158): with enable != 0,
+ * every pair pass of the rings step (and mavi_calc_forces) records, for each
+ * particle, the candidate pairs with dist < dist_eq * tol (dist_eq of the
+ * pair's types) that are in different rings, or in any ring when type_all.
+ * only_count keeps the counts only. The test is the reference's FP64
+ * arithmetic on FP64 positions in both precisions, so the sets are exact.
+ * mavi_rings_neighbors returns, for one replica and in user slot order, the
+ * counts (num_particles int32) and, unless only_count, the lists
+ * (num_particles x MAVI_MAX_NEIGHBORS int32, 0-based slot ids, -1 padded; the
+ * order inside a list is the GPU's visiting order, not the reference's append
+ * order). Reflects the state at the last pair pass. */
+int mavi_rings_neighbors_config(MaviSystem* sys, int32_t enable, int32_t only_count, int32_t type_all,
+                                double tol);
+int mavi_rings_neighbors(MaviSystem* sys, int32_t replica, int32_t* counts, int32_t* lists);
 
 int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
 /* Device-time profiling (and reset of the accumulated profile). on: 0 off,

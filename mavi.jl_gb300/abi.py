@@ -22,6 +22,8 @@ MAVI_ERR_OUTSIDE_SPACE = 6
 MAVI_ERR_UNSUPPORTED = 7
 MAVI_ERR_NO_DEVICE = 8
 MAVI_ERR_NOISE_MISSING = 9
+MAVI_ERR_NEIGHBOR_OVERFLOW = 10
+MAVI_MAX_NEIGHBORS = 15
 
 MAVI_STATE_SECOND_LAW = 0
 MAVI_STATE_SELF_PROPELLED = 1
@@ -184,6 +186,8 @@ SIGNATURES = {
     "mavi_profile_read": (C.c_int, [_vp, C.POINTER(MaviProfile)]),
     "mavi_last_error": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "mavi_fma_peak": (C.c_int, [C.c_int32, C.c_int32, _dp]),
+    "mavi_rings_neighbors_config": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
+    "mavi_rings_neighbors": (C.c_int, [_vp, C.c_int32, _ip, _ip]),
     "mavi_chunk_lists_noalloc": (C.c_int, [C.POINTER(MaviReplicaParams), _vp, C.c_int64, _vp, _vp, _vp,
                                            C.c_char_p, C.c_int32]),
 }

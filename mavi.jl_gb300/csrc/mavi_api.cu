@@ -458,6 +458,7 @@ const char* mavi_status_string(int st) {
     case MAVI_ERR_UNSUPPORTED: return "unsupported configuration";
     case MAVI_ERR_NO_DEVICE: return "no CUDA device";
     case MAVI_ERR_NOISE_MISSING: return "noise not supplied";
+    case MAVI_ERR_NEIGHBOR_OVERFLOW: return "neighbour list overflow";
     }
     return "unknown status";
 }
@@ -983,6 +984,64 @@ int mavi_get_time(MaviSystem* s, int64_t* num_steps, double* time) {
     if (num_steps) *num_steps = s->num_steps[0];
     if (time) *time = s->time[0];
     return MAVI_OK;
+}
+
+int mavi_rings_neighbors_config(MaviSystem* s, int32_t enable, int32_t only_count, int32_t type_all, double tol) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    if (!s->is_rings) return fail(s, MAVI_ERR_UNSUPPORTED, "particle neighbour lists belong to the rings model");
+    if (!enable) {
+        s->C.nb_mode = 0;
+        drop_graph(s);
+        return MAVI_OK;
+    }
+    if (!(tol > 0)) return fail(s, MAVI_ERR_INVALID_ARG, "tol must be > 0");
+    if (!s->C.nb_count && dalloc(s, &s->C.nb_count, s->Nslots) != cudaSuccess)
+        return fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for the neighbour counts");
+    if (!only_count && !s->C.nb_list &&
+        dalloc(s, &s->C.nb_list, s->Nslots * (int64_t)MAVI_MAX_NEIGHBORS) != cudaSuccess)
+        return fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for the neighbour lists");
+    // squared thresholds (dist_eq * tol)^2 in units^2 with the +-1e-6 band of the FP32 test
+    std::vector<FixPair> fix_h((size_t)s->R * MAVI_MAX_TYPES * MAVI_MAX_TYPES);
+    for (int r = 0; r < s->R; r++) {
+        FixPair* f = fix_h.data() + (size_t)r * MAVI_MAX_TYPES * MAVI_MAX_TYPES;
+        fill_fix_pairs(s->params[r], s->reps_h[r], f);
+        const MaviRingsCfg& rc = s->params[r].rings;
+        for (int a = 0; a < rc.num_types; a++)
+            for (int b = 0; b < rc.num_types; b++) {
+                const double thr = 2.0 * (rc.inter_dist_eq[a][b] / 2.0) * tol * s->reps_h[r].inv_u;
+                f[a * MAVI_MAX_TYPES + b].nb2_hi = (float)(thr * thr * (1.0 + 1e-6));
+                f[a * MAVI_MAX_TYPES + b].nb2_lo = (float)(thr * thr * (1.0 - 1e-6));
+            }
+    }
+    CUDA_TRY(s, cudaMemcpyAsync(const_cast<FixPair*>(s->C.fix), fix_h.data(), sizeof(FixPair) * fix_h.size(),
+                                cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemsetAsync(s->C.nb_count, 0, sizeof(int32_t) * s->Nslots, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    s->C.nb_mode = only_count ? 1 : 2;
+    s->C.nb_type_all = type_all ? 1 : 0;
+    s->C.nb_tol = tol;
+    drop_graph(s);
+    return MAVI_OK;
+}
+
+int mavi_rings_neighbors(MaviSystem* s, int32_t replica, int32_t* counts, int32_t* lists) {
+    if (!s || !counts || replica < 0 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    if (!s->C.nb_mode) return fail(s, MAVI_ERR_INVALID_ARG, "neighbour lists are not enabled");
+    if (lists && s->C.nb_mode != 2) return fail(s, MAVI_ERR_INVALID_ARG, "only neighbour counts are kept");
+    const DevRep& R = s->reps_h[replica];
+    const int64_t n = R.nslots;
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    CUDA_TRY(s, cudaMemcpy(counts, s->C.nb_count + R.slot0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    if (lists) {
+        std::vector<int32_t> tmp((size_t)n * MAVI_MAX_NEIGHBORS);
+        CUDA_TRY(s, cudaMemcpy(tmp.data(), s->C.nb_list + R.slot0 * MAVI_MAX_NEIGHBORS,
+                               sizeof(int32_t) * tmp.size(), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < MAVI_MAX_NEIGHBORS; k++)
+                lists[i * MAVI_MAX_NEIGHBORS + k] =
+                    k < counts[i] ? tmp[i * MAVI_MAX_NEIGHBORS + k] - (int32_t)R.slot0 : -1;
+    }
+    return check_device_error(s);
 }
 
 int mavi_get_stats(MaviSystem* s, MaviStats* st) {

@@ -44,6 +44,7 @@ struct FixPair {
     float cut2_hi, cut2_lo;    // cut2 * (1 +- 1e-6): FP32 squared distances beyond / below
                                // these are certainly outside / inside the cutoff
     float pad;
+    float nb2_hi, nb2_lo;      // rings neighbour threshold (dist_eq * tol)^2 in units^2 * (1 +- 1e-6)
 };
 
 struct Ctx {
@@ -68,6 +69,11 @@ struct Ctx {
     const int32_t *ring_types;
     const int32_t *ring_rep;   // replica of each ring
     const double *cxu, *cyu;   // chunk-centre x per column, y per row, in units of u
+    // rings particle neighbour lists (0: off, 1: counts, 2: counts and lists),
+    // indexed by user slot; neighbours stored as user slots
+    int32_t nb_mode, nb_type_all;
+    double nb_tol;
+    int32_t *nb_count, *nb_list;
     double2 *ring_cs;          // (cos, sin) of the ring's polarisation angle
     double2 *ring_vc;          // mean particle velocity of the ring in the last update
     // descriptors
@@ -533,11 +539,13 @@ __device__ __forceinline__ void lj_pair_df(const DevRep& R, int32_t dxi, int32_t
 template <int PREC, int DYN> struct Acc;
 template <int DYN> struct Acc<kPrecFP64, DYN> {
     double x = 0, y = 0;
+    int32_t nb = 0;   // rings neighbour count of the lane's particle
     __device__ __forceinline__ double gx() const { return x; }
     __device__ __forceinline__ double gy() const { return y; }
 };
 template <int DYN> struct Acc<kPrecMixed, DYN> {
     float x = 0, y = 0, cx = 0, cy = 0;
+    int32_t nb = 0;   // rings neighbour count of the lane's particle
     __device__ __forceinline__ void add(float fx, float fy) {
         if constexpr (DYN == MAVI_DYN_LEN_JONES) {
             float yx = fx - cx, tx = x + yx;
@@ -576,6 +584,8 @@ template <> struct PartOf<kPrecFP64> { using T = double2; };       // FP64 posit
 // The particle whose force a lane sums.
 template <int PREC, int DYN> struct Me {
     typename PartOf<PREC>::T p;
+    int64_t s;        // own sorted slot
+    int32_t uid;      // own user slot (rings neighbour lists)
     RingInfo ri;
     int32_t n_ring;
     const FixPair* fixr;
@@ -587,15 +597,39 @@ __device__ __forceinline__ Me<PREC, DYN> make_me(const Ctx& C, const DevRep& R, 
                                                  const typename PartOf<PREC>::T* __restrict__ P) {
     Me<PREC, DYN> m;
     m.p = P[s];
+    m.s = s;
+    m.uid = 0;
     m.ri = RingInfo{0, 0, 0};
     m.n_ring = 0;
     m.fixr = C.fix + (int64_t)rep * MAVI_MAX_TYPES * MAVI_MAX_TYPES;
     if constexpr (PREC == kPrecMixed) m.fp0 = m.fixr[0];
     if constexpr (DYN == MAVI_DYN_RINGS) {
-        m.ri = ring_info(C, R, C.uid_cur[s]);
+        m.uid = C.uid_cur[s];
+        m.ri = ring_info(C, R, m.uid);
         m.n_ring = C.rcfg[rep].num_particles[m.ri.type];
     }
     return m;
+}
+
+// Rings particle neighbour lists (src/rings/neighbors.jl:116-136, called for
+// every candidate pair from calc_interaction, src/rings/integration.jl:32-44):
+// j is a neighbour of i when dist < max_dist * tol with max_dist =
+// 2 * particle_radius = dist_eq of the pair's types, and (type :all or
+// different rings). The test uses the reference's FP64 arithmetic on the FP64
+// positions (no fused operations), so the sets are exact.
+template <int DYN>
+__device__ __forceinline__ bool nb_test_fp64(const Ctx& C, const DevRep& R, double dx, double dy, double dist_eq) {
+    const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    return dist < __dmul_rn(2.0 * (dist_eq / 2.0), C.nb_tol);
+}
+
+template <class A>
+__device__ __forceinline__ void nb_record(const Ctx& C, int32_t me_uid, int32_t other_uid, A& acc) {
+    const int32_t k = acc.nb++;
+    if (C.nb_mode == 2) {
+        if (k < MAVI_MAX_NEIGHBORS) C.nb_list[(int64_t)me_uid * MAVI_MAX_NEIGHBORS + k] = other_uid;
+        else raise_error(C.err, MAVI_ERR_NEIGHBOR_OVERFLOW, me_uid, k);
+    }
 }
 
 // One pair term added to acc: q is the neighbour's position (FP64) or
@@ -612,6 +646,9 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
     double sc;
     if constexpr (DYN == MAVI_DYN_RINGS) {
         RingInfo o = ring_info(C, R, uq);
+        if (C.nb_mode && (C.nb_type_all || o.ring != me.ri.ring) &&
+            nb_test_fp64<DYN>(C, R, dx, dy, C.rcfg[rep].inter_dist_eq[me.ri.type][o.type]))
+            nb_record(C, me.uid, uq, acc);
         sc = rings_pair_scalar_d(C.rcfg[rep], me.ri.type, o.type, o.ring == me.ri.ring, me.ri.p, o.p, me.n_ring, d2);
     } else {
         sc = pair_scalar<DYN, double>(R.pd, d2);
@@ -621,7 +658,7 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
 }
 
 template <int DYN>
-__device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t, const Me<kPrecMixed, DYN>& me,
+__device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t rep, const Me<kPrecMixed, DYN>& me,
                                           int2 oj, int32_t uq, int32_t shx, int32_t shy, bool mi,
                                           Acc<kPrecMixed, DYN>& acc) {
     // offsets are clamped to +-4 chunks and neighbours are <= 1 chunk apart,
@@ -645,6 +682,21 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
     if constexpr (DYN == MAVI_DYN_RINGS) {
         RingInfo o = ring_info(C, R, uq);
         bool same = o.ring == me.ri.ring;
+        if (C.nb_mode && (C.nb_type_all || !same)) {
+            // FP32 test on the exact integer displacement; inside the +-1e-6
+            // band around the threshold, the reference's FP64 test on positions
+            const FixPair& fq = me.fixr[me.ri.type * MAVI_MAX_TYPES + o.type];
+            const float dxf = (float)dxi, dyf = (float)dyi;
+            const float d2f = fmaf(dxf, dxf, dyf * dyf);
+            bool in = d2f < fq.nb2_lo;
+            if (!in && d2f <= fq.nb2_hi) {
+                const double2 pi = C.pos_cur[me.s], pj = C.pos_cur[C.slot_of[uq]];
+                double ex = pi.x - pj.x, ey = pi.y - pj.y;
+                if (R.min_image) { ex = min_image1(ex, R.box_x, R.half_box_x); ey = min_image1(ey, R.box_y, R.half_box_y); }
+                in = nb_test_fp64<DYN>(C, R, ex, ey, C.rcfg[rep].inter_dist_eq[me.ri.type][o.type]);
+            }
+            if (in) nb_record(C, me.uid, uq, acc);
+        }
         if (same) {
             int32_t diff = me.ri.p > o.p ? me.ri.p - o.p : o.p - me.ri.p;
             if (diff == 1 || diff == me.n_ring - 1) return;
@@ -682,6 +734,11 @@ __device__ __forceinline__ void pair_term_raw(const Ctx& C, const DevRep& R, int
     double sc;
     if constexpr (DYN == MAVI_DYN_RINGS) {
         RingInfo o = ring_info(C, R, uq);
+        if (C.nb_mode && (C.nb_type_all || o.ring != me.ri.ring)) {
+            const double2 pi = C.pos_cur[me.s], pj = C.pos_cur[C.slot_of[uq]];
+            if (nb_test_fp64<DYN>(C, R, pi.x - pj.x, pi.y - pj.y, C.rcfg[rep].inter_dist_eq[me.ri.type][o.type]))
+                nb_record(C, me.uid, uq, acc);
+        }
         sc = rings_pair_scalar_d(C.rcfg[rep], me.ri.type, o.type, o.ring == me.ri.ring, me.ri.p, o.p, me.n_ring, d2);
     } else {
         sc = pair_scalar<DYN, double>(R.pd, d2);
@@ -1261,6 +1318,9 @@ k_pass(Ctx C, int32_t with_wall_forces) {
         if constexpr (PASS == kPassForce) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
             else C.ff[s] = make_float2((float)fx, (float)fy);
+            if constexpr (DYN == MAVI_DYN_RINGS) {
+                if (C.nb_mode) C.nb_count[C.uid_cur[s]] = acc.nb;
+            }
         } else if constexpr (PASS == kPassVerlet1) {
             // update_verlet! (src/integration.jl:415-431), first half
             double2 v = C.vel_cur[s];

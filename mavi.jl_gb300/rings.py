@@ -159,15 +159,52 @@ class RingsState:
         return int(n)
 
 
+@dataclass
+class NeighborsCfg:
+    """NeighborsCfg(only_count, type, tol) (src/rings/neighbors.jl:10-14) for the
+    particle neighbour lists; type "rings" ignores particles of the same ring,
+    "all" counts every particle."""
+    only_count: bool = False
+    type: str = "all"
+    tol: float = 1.1
+
+
 class RingsSystem(System):
-    """RingsSystem (src/rings/rings.jl:231-291) on the GPU."""
+    """RingsSystem (src/rings/rings.jl:231-291) on the GPU. With
+    ``p_neighbors_cfg`` every pair pass also records the particle neighbour
+    lists (``neighbors()``)."""
     is_rings = True
 
     def __init__(self, state: RingsState, space_cfg, dynamic_cfg: RingsCfg, int_cfg: IntCfg,
-                 time_info: TimeInfo | None = None):
+                 time_info: TimeInfo | None = None, p_neighbors_cfg: NeighborsCfg | None = None):
         super().__init__(state, space_cfg, dynamic_cfg, int_cfg, time_info)
         if dynamic_cfg.num_types > 1 and state.types is None:
             raise ValueError("DynamicCfg has multiple types, but state.types is nothing!")
+        self.p_neighbors_cfg = p_neighbors_cfg
+
+    def _ensure(self, step_kind=None):
+        fresh = self._handle is None
+        h = super()._ensure(step_kind)
+        if self.p_neighbors_cfg is not None and (fresh or h is not getattr(self, "_nb_handle", None)):
+            c = self.p_neighbors_cfg
+            h.check(h.lib.mavi_rings_neighbors_config(h.handle, 1, 1 if c.only_count else 0,
+                                                      1 if c.type == "all" else 0, float(c.tol)),
+                    "mavi_rings_neighbors_config")
+            self._nb_handle = h
+        return h
+
+    def neighbors(self):
+        """(counts[num_slots], lists[num_slots, 15] or None): the particle
+        neighbour lists at the last pair pass, 0-based slot ids, -1 padded."""
+        if self.p_neighbors_cfg is None:
+            raise RuntimeError("p_neighbors_cfg was not given")
+        h = self._ensure()
+        n = self.num_slots
+        counts = np.zeros(n, dtype=np.int32)
+        lists = None if self.p_neighbors_cfg.only_count else np.zeros(n * abi.MAVI_MAX_NEIGHBORS, dtype=np.int32)
+        h.check(h.lib.mavi_rings_neighbors(h.handle, 0, abi.as_iptr(counts), abi.as_iptr(lists)),
+                "mavi_rings_neighbors")
+        return counts, (None if lists is None else lists.reshape(n, abi.MAVI_MAX_NEIGHBORS))
 
     @property
     def num_slots(self) -> int:

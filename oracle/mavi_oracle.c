@@ -914,6 +914,56 @@ int64_t oracle_count_pairs(OracleSys* s) {
     return pairs;
 }
 
+/* Particle neighbour lists of the rings model (src/rings/neighbors.jl:116-136,
+ * called from calc_interaction, src/rings/integration.jl:32-44): every
+ * candidate pair (i, j) of the chunk loop with dist < max_dist * tol, where
+ * max_dist = 2 * particle_radius(interaction) = dist_eq of the pair's types,
+ * and (type :all or different rings) adds j to i's list and i to j's list,
+ * in the loop order of calc_forces! (src/integration.jl:112-157). `lists`
+ * (n x max_list, may be NULL) receives 0-based slot ids; a list longer than
+ * max_list is an error (the reference's array bound). */
+int32_t oracle_rings_neighbors(OracleSys* s, double tol, int32_t type_all, int32_t max_list, int32_t* counts,
+                               int32_t* lists) {
+    if (s->p.dyn.kind != MAVI_DYN_RINGS || !s->has_chunks) return MAVI_ERR_INVALID_ARG;
+    if (oracle_update_chunks(s)) return s->err;
+    const MaviRingsCfg* rc = &s->p.rings;
+    memset(counts, 0, sizeof(int32_t) * s->n);
+    int32_t st = MAVI_OK;
+    #define NEIGH_PAIR(I, J) do {                                                          \
+        int64_t ri_ = (I) / s->nmax, rj_ = (J) / s->nmax;                                   \
+        int ti_ = s->types[ri_] - 1, tj_ = s->types[rj_] - 1;                               \
+        V2 dr_ = calc_diff(s, P(s, (I)), P(s, (J)));                                        \
+        double dist_ = sqrt(sum_sq(dr_));                                                   \
+        double max_dist_ = 2 * (rc->inter_dist_eq[ti_][tj_] / 2.0);                         \
+        if (dist_ < max_dist_ * tol && (type_all || ri_ != rj_)) {                          \
+            int32_t ci_ = ++counts[(I)], cj_ = ++counts[(J)];                               \
+            if (lists) {                                                                    \
+                if (ci_ > max_list || cj_ > max_list) st = MAVI_ERR_CHUNK_OVERFLOW;         \
+                else { lists[(I) * max_list + ci_ - 1] = (int32_t)(J);                      \
+                       lists[(J) * max_list + cj_ - 1] = (int32_t)(I); }                    \
+            }                                                                               \
+        }                                                                                   \
+    } while (0)
+    for (int64_t col = 0; col < s->cols; col++) {
+        for (int64_t row = 0; row < s->rows; row++) {
+            int64_t ch = col * s->rows + row;
+            int32_t np = s->num_in_chunk[ch];
+            const int32_t* chunk = s->chunk_particles + ch * s->cap;
+            for (int32_t i = 0; i < np; i++) {
+                int64_t p1 = chunk[i];
+                for (int32_t j = i + 1; j < np; j++) NEIGH_PAIR(p1, (int64_t)chunk[j]);
+                for (int32_t k = 0; k < s->nbr_cnt[ch]; k++) {
+                    int64_t nb = s->nbr[ch * 4 + k];
+                    const int32_t* nchunk = s->chunk_particles + nb * s->cap;
+                    for (int32_t j = 0; j < s->num_in_chunk[nb]; j++) NEIGH_PAIR(p1, (int64_t)nchunk[j]);
+                }
+            }
+        }
+    }
+    #undef NEIGH_PAIR
+    return st;
+}
+
 /* ------------------------------------------------------------------------ */
 /* construction                                                              */
 /* ------------------------------------------------------------------------ */

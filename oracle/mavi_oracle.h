@@ -51,6 +51,8 @@ int32_t oracle_energies(OracleSys* s, int32_t pe_mode, double* ke, double* pe);
 int32_t oracle_get_time(OracleSys* s, int64_t* num_steps, double* time);
 int32_t oracle_get_areas(OracleSys* s, double* areas);
 int64_t oracle_count_pairs(OracleSys* s);
+int32_t oracle_rings_neighbors(OracleSys* s, double tol, int32_t type_all, int32_t max_list, int32_t* counts,
+                               int32_t* lists);
 /* Julia float `div` as used by update_particle_chunk! (src/chunks.jl:129-130). */
 double  oracle_julia_div(double x, double y);
 /* update_particle_chunk! row/col (1-based, before bounds checks) for a point. */

@@ -54,6 +54,8 @@ def _load_lib():
         "oracle_get_time": (C.c_int32, [vp, lp, dp]),
         "oracle_get_areas": (C.c_int32, [vp, dp]),
         "oracle_count_pairs": (C.c_int64, [vp]),
+        "oracle_rings_neighbors": (C.c_int32, [vp, C.c_double, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                               C.POINTER(C.c_int32)]),
         "oracle_julia_div": (C.c_double, [C.c_double, C.c_double]),
         "oracle_chunk_of": (C.c_int32, [vp, C.c_double, C.c_double, lp, lp]),
         "oracle_struct_sizes": (C.c_int32, [lp]),
@@ -183,6 +185,18 @@ class OracleSystem:
         a = np.zeros(num_rings)
         self._ck(self.lib.oracle_get_areas(self.h, _dp(a)), "areas")
         return a
+
+    def rings_neighbors(self, tol=1.1, type_all=False, max_list=15, with_lists=True):
+        """Particle neighbour counts (n) and lists (n x max_list, -1 padded,
+        reference append order) of the rings model at the current state."""
+        counts = np.zeros(self.n, dtype=np.int32)
+        lists = np.full(self.n * max_list, -1, dtype=np.int32) if with_lists else None
+        ip = C.POINTER(C.c_int32)
+        st = self.lib.oracle_rings_neighbors(self.h, float(tol), 1 if type_all else 0, int(max_list),
+                                             counts.ctypes.data_as(ip),
+                                             lists.ctypes.data_as(ip) if lists is not None else None)
+        self._ck(st, "rings_neighbors")
+        return counts, (lists.reshape(self.n, max_list) if lists is not None else None)
 
     def count_pairs(self) -> int:
         return int(self.lib.oracle_count_pairs(self.h))

@@ -327,3 +327,26 @@ def test_periodic_circle_raw_displacement(mg, orc, precision):
         ref.close()
     b.run(50)
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("ntype", ["all", "rings"])
+def test_rings_particle_neighbors_exact(mg, orc, precision, ntype):
+    """Particle neighbour lists (src/rings/neighbors.jl:116-136): counts equal
+    the oracle's and every list holds the same neighbours (order aside)."""
+    from mavi_gb300 import rings as R, workloads
+    systems, _ = workloads.rings_batch(num_replicas=1, rings_min=120, rings_max=120, precision=precision)
+    s = systems[0]
+    s.p_neighbors_cfg = R.NeighborsCfg(only_count=False, type=ntype, tol=1.1)
+    s.run(300)                     # rings drift into contact
+    s.calc_forces()                # a pair pass on the downloaded state
+    counts, lists = s.neighbors()
+    ref = orc.from_system(s)
+    rc, rl = ref.rings_neighbors(tol=1.1, type_all=(ntype == "all"))
+    assert np.array_equal(counts, rc)
+    assert counts.sum() > 0
+    for i in np.nonzero(counts)[0]:
+        assert sorted(lists[i, :counts[i]]) == sorted(rl[i, :rc[i]])
+        assert np.all(lists[i, counts[i]:] == -1)
+    ref.close()
+    s.close()
