@@ -270,6 +270,7 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
     R.inv_u = 1.0 / u;
     R.u_f = (float)u;
     R.u2_f = (float)(u * u);
+    R.u2_d = u * u;
     R.sx_u = std::llround(R.chunk_l / u);
     R.sy_u = std::llround(R.chunk_h / u);
     R.bx_u = R.sx_u * R.cols;

@@ -81,6 +81,7 @@ struct DevRep {
     float ring_vo_f[MAVI_MAX_TYPES], ring_mu_f[MAVI_MAX_TYPES];
     float dt_f;
     int32_t _pad3;
+    double u2_d;           // u^2 in double (areas from integer units^2)
 };
 
 // ---------------------------------------------------------------------------

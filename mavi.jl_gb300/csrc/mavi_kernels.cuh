@@ -1418,6 +1418,18 @@ k_pass(Ctx C, int32_t with_wall_forces) {
 constexpr int kRingMax = 256;     // particles per ring supported
 constexpr int kRingWarps = 4;     // rings per block
 
+// Sum of the ring's particle velocities (k_ring_pol divides by n).
+template <class V>
+__device__ __forceinline__ void ring_vc_store(const Ctx& C, int64_t g, int lane, int32_t do_update, V vcx, V vcy) {
+    if (!do_update) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vcx += __shfl_xor_sync(0xffffffffu, vcx, o);
+        vcy += __shfl_xor_sync(0xffffffffu, vcy, o);
+    }
+    if (lane == 0) C.ring_vc[g] = make_double2((double)vcx, (double)vcy);
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_rings, int32_t do_update) {
     __shared__ double2 sp_[kRingWarps][kRingMax];
@@ -1445,40 +1457,6 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
         return make_double2(dx, dy);
     };
-    // unwrapped coordinates relative to particle 0 (update_continuos_pos!):
-    // u[p] = sum_{q<p} calc_diff(P[q+1], P[q]); area by the shoelace formula.
-    double area2 = 0.0;
-    double carry_x = 0.0, carry_y = 0.0;   // u of the first particle of this 32-block
-    double prev_last_x = 0.0, prev_last_y = 0.0;
-    for (int base = 0; base < n; base += 32) {
-        int p = base + lane;
-        double bx = 0, by = 0;
-        if (p >= 1 && p < n) { double2 d = diff(P[p], P[p - 1]); bx = d.x; by = d.y; }
-        // inclusive scan of bond vectors inside the block of 32
-        double ix = bx, iy = by;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            double tx = __shfl_up_sync(0xffffffffu, ix, o), ty = __shfl_up_sync(0xffffffffu, iy, o);
-            if (lane >= o) { ix += tx; iy += ty; }
-        }
-        double ux = carry_x + ix, uy = carry_y + iy;
-        // shoelace term cross(u[p-1], u[p]) for p in [max(1,base), n)
-        double upx = __shfl_up_sync(0xffffffffu, ux, 1), upy = __shfl_up_sync(0xffffffffu, uy, 1);
-        if (lane == 0) { upx = prev_last_x; upy = prev_last_y; }
-        if (p >= 1 && p < n) area2 += upx * uy - upy * ux;
-        prev_last_x = __shfl_sync(0xffffffffu, ux, 31);
-        prev_last_y = __shfl_sync(0xffffffffu, uy, 31);
-        carry_x = prev_last_x;
-        carry_y = prev_last_y;
-    }
-    // closing term cross(u[n-1], u[0]) vanishes since u[0] = 0
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) area2 += __shfl_xor_sync(0xffffffffu, area2, o);
-    const double area = area2 / 2.0;
-    if (lane == 0) C.ring_area[g] = area;
-    const double k_s = rc.k_spring[t], l_s = rc.l_spring[t];
-    const double fmod_area = rc.k_area[t] * (area - R.ring_a0sq[t]);
-    const double kb = rc.k_bend[t];
     // overdamped active update parameters; (cos, sin) of the polarisation
     // come from k_ring_pol (one thread per ring, not one warp)
     double pc = 0.0, ps = 0.0;
@@ -1529,6 +1507,115 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         C.uid_out[s] = C.uid_cur[s];
         C.rep_out[s] = rep;
     };
+    if constexpr (PREC == kPrecMixed) {
+        if (n <= 32 && !R.min_image) {
+            // Mixed form, rings of <= 32 particles without minimum image: the
+            // ring geometry comes from the exact integer chunk offsets. Each
+            // lane's absolute position in units from the centre of chunk
+            // (0, 0) is col*sx + ox, -row*sy + oy (int64); bonds are exact
+            // integers, the shoelace area of the unwrapped ring is summed
+            // exactly in 128-bit integers (update_continuos_pos! + calc_area,
+            // src/rings/integration.jl:103-138), and springs, area force and
+            // bending run in FP32 on the bond vectors. FP64 is left to the
+            // position update and the walls.
+            const unsigned full = 0xffffffffu;
+            const bool act = lane < n;
+            const int p = act ? lane : 0;
+            const int pp = p == n - 1 ? 0 : p + 1, pm = p == 0 ? n - 1 : p - 1;
+            const int32_t sp = S[p];
+            const int2 off = C.off_cur[sp];
+            const int32_t lc = C.cell_cur[sp] - (int32_t)R.c0;
+            const int32_t col = lc / R.rows, row = lc - col * R.rows;
+            const long long X = (long long)col * R.sx_u + off.x;
+            const long long Y = -(long long)row * R.sy_u + off.y;
+            const long long bx = __shfl_sync(full, X, pp) - X;   // bond p: x_{p+1} - x_p (units)
+            const long long by = __shfl_sync(full, Y, pp) - Y;
+            // unwrapped position of p relative to particle 0: exclusive scan of the bonds
+            long long ix = act ? bx : 0, iy = act ? by : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long tx = __shfl_up_sync(full, ix, o), ty = __shfl_up_sync(full, iy, o);
+                if (lane >= o) { ix += tx; iy += ty; }
+            }
+            const long long ux = ix - (act ? bx : 0), uy = iy - (act ? by : 0);
+            // shoelace term cross(u_p, u_{p+1}) = cross(u_p, b_p) for p = 0..n-2
+            __int128 a2 = (act && p <= n - 2) ? (__int128)ux * by - (__int128)uy * bx : (__int128)0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long lo = (unsigned long long)a2;
+                const long long hi = (long long)(a2 >> 64);
+                const unsigned long long olo = __shfl_xor_sync(full, lo, o);
+                const long long ohi = __shfl_xor_sync(full, hi, o);
+                a2 += (__int128)(((unsigned __int128)(unsigned long long)ohi << 64) | olo);
+            }
+            const double a2d = fma((double)(long long)(a2 >> 64), 18446744073709551616.0,
+                                   (double)(unsigned long long)a2);
+            const double area = a2d * R.u2_d * 0.5;
+            if (lane == 0) C.ring_area[g] = area;
+            const float fa = (float)(rc.k_area[t] * (area - R.ring_a0sq[t]));
+            const float uf = R.u_f;
+            const float bxf = i64_to_f32(bx) * uf, byf = i64_to_f32(by) * uf;
+            const float L = sqrtf(bxf * bxf + byf * byf);
+            const float inv = 1.0f / L;
+            const float bmx = __shfl_sync(full, bxf, pm), bmy = __shfl_sync(full, byf, pm);   // bond p-1
+            const float Lm = __shfl_sync(full, L, pm), invm = __shfl_sync(full, inv, pm);
+            const float ks = R.ring_ks_f[t], ls = R.ring_ls_f[t], kbt = R.ring_kb_f[t];
+            const float spf = ks * (L - ls) * inv, smf = ks * (Lm - ls) * invm;
+            float fx = spf * bxf - smf * bmx;
+            float fy = spf * byf - smf * bmy;
+            // area force: dr = x_{p+1} - x_{p-1} = b_p + b_{p-1}
+            const long long dbx = bx + __shfl_sync(full, bx, pm), dby = by + __shfl_sync(full, by, pm);
+            fx -= fa * (i64_to_f32(dby) * uf * 0.5f);
+            fy -= fa * (-i64_to_f32(dbx) * uf * 0.5f);
+            const float iab = invm * inv;
+            const float c = (bmx * bxf + bmy * byf) * iab;
+            const float dcax = bxf * iab - c * bmx * (invm * invm), dcay = byf * iab - c * bmy * (invm * invm);
+            const float dcbx = bmx * iab - c * bxf * (inv * inv), dcby = bmy * iab - c * byf * (inv * inv);
+            const float nax = __shfl_sync(full, dcax, pp), nay = __shfl_sync(full, dcay, pp);
+            const float pbx = __shfl_sync(full, dcbx, pm), pby = __shfl_sync(full, dcby, pm);
+            if (kbt != 0.0f) {
+                fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
+                fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
+            }
+            if (act) finish(p, P[p], fx, fy);
+            ring_vc_store(C, g, lane, do_update, vcx, vcy);
+            return;
+        }
+    }
+    // unwrapped coordinates relative to particle 0 (update_continuos_pos!):
+    // u[p] = sum_{q<p} calc_diff(P[q+1], P[q]); area by the shoelace formula.
+    double area2 = 0.0;
+    double carry_x = 0.0, carry_y = 0.0;   // u of the first particle of this 32-block
+    double prev_last_x = 0.0, prev_last_y = 0.0;
+    for (int base = 0; base < n; base += 32) {
+        int p = base + lane;
+        double bx = 0, by = 0;
+        if (p >= 1 && p < n) { double2 d = diff(P[p], P[p - 1]); bx = d.x; by = d.y; }
+        // inclusive scan of bond vectors inside the block of 32
+        double ix = bx, iy = by;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double tx = __shfl_up_sync(0xffffffffu, ix, o), ty = __shfl_up_sync(0xffffffffu, iy, o);
+            if (lane >= o) { ix += tx; iy += ty; }
+        }
+        double ux = carry_x + ix, uy = carry_y + iy;
+        // shoelace term cross(u[p-1], u[p]) for p in [max(1,base), n)
+        double upx = __shfl_up_sync(0xffffffffu, ux, 1), upy = __shfl_up_sync(0xffffffffu, uy, 1);
+        if (lane == 0) { upx = prev_last_x; upy = prev_last_y; }
+        if (p >= 1 && p < n) area2 += upx * uy - upy * ux;
+        prev_last_x = __shfl_sync(0xffffffffu, ux, 31);
+        prev_last_y = __shfl_sync(0xffffffffu, uy, 31);
+        carry_x = prev_last_x;
+        carry_y = prev_last_y;
+    }
+    // closing term cross(u[n-1], u[0]) vanishes since u[0] = 0
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) area2 += __shfl_xor_sync(0xffffffffu, area2, o);
+    const double area = area2 / 2.0;
+    if (lane == 0) C.ring_area[g] = area;
+    const double k_s = rc.k_spring[t], l_s = rc.l_spring[t];
+    const double fmod_area = rc.k_area[t] * (area - R.ring_a0sq[t]);
+    const double kb = rc.k_bend[t];
     if (n <= 32) {
         // One particle per lane; neighbours' bond data by shuffles. Each bond
         // length and its inverse are formed once (one sqrt and one division
@@ -1624,13 +1711,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
             finish(p, xc, (V)fx, (V)fy);
         }
     }
-    if (!do_update) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        vcx += __shfl_xor_sync(0xffffffffu, vcx, o);
-        vcy += __shfl_xor_sync(0xffffffffu, vcy, o);
-    }
-    if (lane == 0) C.ring_vc[g] = make_double2((double)vcx, (double)vcy);   // sums; k_ring_pol divides
+    ring_vc_store(C, g, lane, do_update, vcx, vcy);
 }
 
 // ===========================================================================

@@ -350,3 +350,31 @@ def test_rings_particle_neighbors_exact(mg, orc, precision, ntype):
         assert np.all(lists[i, counts[i]:] == -1)
     ref.close()
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rings_in_circular_container(mg, orc, precision):
+    """Rings inside a PotentialWalls circle (no minimum image): the mixed form
+    takes its ring geometry from the integer chunk offsets (exact shoelace
+    area); forces and a 100-step trajectory with injected noise follow the
+    oracle."""
+    from mavi_gb300 import workloads
+    systems, _ = workloads.rings_batch(num_replicas=1, rings_min=80, rings_max=80, precision=precision, k_bend=1.0)
+    s = systems[0]
+    s.int_cfg.device.noise = "injected"
+    ref = orc.from_system(s)
+    err = rel_force_err(s.calc_forces(), ref.forces())
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+    areas = ref.areas(s.state.num_rings)
+    n = s.handle.noise_count()
+    steps = 100
+    noise = np.random.default_rng(5).normal(size=n * steps)
+    s.run(steps, noise=noise)
+    ref.step(steps, noise=noise)
+    p, _, pol = ref.state()
+    tol = 1e-8 if precision == "fp64" else 1e-3
+    assert np.max(np.abs(s.state.pos - p)) < tol
+    assert np.max(np.abs(s.state.pol - pol)) < tol
+    assert np.all(areas > 0)
+    ref.close()
+    s.close()
