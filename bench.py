@@ -115,7 +115,7 @@ class Clocks:
 def launches_per_step(step_kind, abi):
     rebin = 3   # scan, scatter, deterministic per-chunk order + permutation
     body = {abi.MAVI_STEP_NEWTON: 2, abi.MAVI_STEP_OVERDAMPED: 1, abi.MAVI_STEP_SZABO: 1, abi.MAVI_STEP_RTP: 1,
-            abi.MAVI_STEP_RINGS: 4}[step_kind]   # rings: pair pass, ring terms + update, polarisation, histogram
+            abi.MAVI_STEP_RINGS: 3}[step_kind]   # rings: pair pass, ring terms + update + histogram, polarisation
     return rebin + body
 
 

@@ -239,7 +239,9 @@ __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64
     // FMA and one conversion per coordinate (the FP64 pipe is the scarce one)
     int32_t ix = __double2int_rn(fma(x, R.inv_u, -C.cxu[R.ccol0 + col]));
     int32_t iy = __double2int_rn(fma(y, R.inv_u, -C.cyu[R.crow0 + row]));
-    if (abs(ix) < R.half_sx_i - 1 && abs(iy) < R.half_sy_i - 1) {
+    // two-sided tests: a position many chunks away (a periodic wrap) saturates
+    // the conversion, and abs(INT_MIN) would pass a one-sided test
+    if (ix > 1 - R.half_sx_i && ix < R.half_sx_i - 1 && iy > 1 - R.half_sy_i && iy < R.half_sy_i - 1) {
         if constexpr (PREC == kPrecMixed) C.off_out[s] = make_int2(ix, iy);
         return cell;
     }
@@ -1472,7 +1474,10 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
     V vcx = 0, vcy = 0;
     const V pcv = (V)pc, psv = (V)ps;
     // pair + wall forces, then the overdamped active update of particle p
-    auto finish = [&](int p, double2 xc, V fx, V fy) {
+    // returns the chunk of the updated position (binning fused here: the
+    // histogram of the next step is taken in this kernel)
+    const int32_t cap = R.has_chunks ? R.cap : (1 << 30);
+    auto finish = [&](int p, double2 xc, V fx, V fy) -> int64_t {
         int32_t s = S[p];
         if constexpr (PREC == kPrecFP64) { double2 f = C.fd[s]; fx += f.x; fy += f.y; }
         else { float2 f = C.ff[s]; fx += f.x; fy += f.y; }
@@ -1485,7 +1490,7 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         if (!do_update) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
             else C.ff[s] = make_float2(fx, fy);
-            return;
+            return 0;
         }
         double x, y;
         if constexpr (PREC == kPrecFP64) {
@@ -1503,9 +1508,13 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
         }
         double dvx = 0, dvy = 0;
         apply_walls(C, rep, R, rc.inter_dist_eq[t][t] * 0.5, x, y, dvx, dvy, false);
+        const int32_t cur = C.cell_cur[s];
+        int64_t nc = bin_fast<PREC>(C, R, s, x, y, cur);
+        if (nc < 0) nc = bin_final<PREC>(C, R, s, x, y, cur);
         C.pos_out[s] = make_double2(x, y);
         C.uid_out[s] = C.uid_cur[s];
         C.rep_out[s] = rep;
+        return nc;
     };
     if constexpr (PREC == kPrecMixed) {
         if (n <= 32 && !R.min_image) {
@@ -1577,7 +1586,9 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
                 fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
                 fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
             }
-            if (act) finish(p, P[p], fx, fy);
+            int64_t nc = 0;
+            if (act) nc = finish(p, P[p], fx, fy);
+            if (do_update) count_into_chunk(C, act, S[p], nc, cap);
             ring_vc_store(C, g, lane, do_update, vcx, vcy);
             return;
         }
@@ -1665,9 +1676,15 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
             fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
             fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
         }
-        if (act) finish(p, xc, (V)fx, (V)fy);
+        int64_t nc = 0;
+        if (act) nc = finish(p, xc, (V)fx, (V)fy);
+        if (do_update) count_into_chunk(C, act, S[p], nc, cap);
     } else {
-        for (int p = lane; p < n; p += 32) {
+        for (int base = 0; base < n; base += 32) {
+            const int p = base + lane;
+            const bool act = p < n;
+            int64_t nc = 0;
+            if (act) {
             int pm = p == 0 ? n - 1 : p - 1, pp = p == n - 1 ? 0 : p + 1;
             double2 xc = P[p], xm = P[pm], xp = P[pp];
             double fx = 0, fy = 0;
@@ -1708,7 +1725,9 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_
                 dcos(diff(xm, xmm), diff(xc, xm), dca, dcb);      // angle at p-1: p is its "i+1"
                 fx += kb * dcb.x; fy += kb * dcb.y;
             }
-            finish(p, xc, (V)fx, (V)fy);
+            nc = finish(p, xc, (V)fx, (V)fy);
+            }
+            if (do_update) count_into_chunk(C, act, act ? S[p] : 0, nc, cap);
         }
     }
     ring_vc_store(C, g, lane, do_update, vcx, vcy);

@@ -75,8 +75,7 @@ void step_body(MaviSystem* s) {
             pass<PREC, DYN, kPassForce>(s, 0);
             record_end(s, MAVI_KERNEL_FORCE);
             record_begin(s, MAVI_KERNEL_UPDATE);
-            rings_terms<PREC>(s, 1);
-            count<PREC>(s, 1);
+            rings_terms<PREC>(s, 1);    // ring terms, update, walls, binning and the histogram
             record_end(s, MAVI_KERNEL_UPDATE);
         }
         break;
