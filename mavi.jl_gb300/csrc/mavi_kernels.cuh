@@ -32,6 +32,7 @@ constexpr int kFixBits = 28;                       // fixed-point offsets: chunk
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;                          // one int4 per thread
 constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
+constexpr int64_t kScanDirectTiles = 512;  // above this, tile offsets come from k_tile_offsets
 constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
 
 // Fixed-point parameters of the pair laws of one (type, type) pair, in units
@@ -301,13 +302,21 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total
 // Single-kernel exclusive scan: the histogram already accumulated each tile's
 // total, so every block sums the tiles before its own, scans its tile and
 // clears the counts it consumed (the next histogram starts from zero).
+// With tile_offs (the exclusive scan of the tile totals, from k_tile_offsets)
+// a block reads its offset instead of summing the totals before it, which
+// grows quadratically with the number of tiles.
 static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int32_t* __restrict__ tile_sum,
-                              int32_t* __restrict__ start, int64_t* d_step, int32_t advance) {
+                              int32_t* __restrict__ start, int64_t* d_step, int32_t advance,
+                              const int32_t* __restrict__ tile_offs = nullptr) {
     __shared__ int smem[32];
-    int pre = 0;
-    for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
     int tile_off;
-    block_exclusive_scan(pre, smem, tile_off);
+    if (tile_offs) {
+        tile_off = tile_offs[blockIdx.x];
+    } else {
+        int pre = 0;
+        for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
+        block_exclusive_scan(pre, smem, tile_off);
+    }
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
     const bool full4 = base + kScanItems <= n;   // count is 16-byte aligned and base a multiple of 4
@@ -336,6 +345,35 @@ static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int3
     if (threadIdx.x == 0) {
         if (blockIdx.x == gridDim.x - 1) start[n] = tile_off + total;
         if (advance && blockIdx.x == 0) d_step[0] += 1;
+    }
+}
+
+// Exclusive scan of the tile totals in one block (grids with many tiles):
+// each thread takes kTileScanItems consecutive totals per round.
+constexpr int kTileScanThreads = 1024;
+constexpr int kTileScanItems = 16;
+static __global__ void __launch_bounds__(kTileScanThreads) k_tile_offsets(const int32_t* __restrict__ tile_sum,
+                                                                          int64_t ntiles,
+                                                                          int32_t* __restrict__ tile_offs) {
+    __shared__ int smem[32];
+    int carry = 0;
+    for (int64_t b0 = 0; b0 < ntiles; b0 += (int64_t)kTileScanThreads * kTileScanItems) {
+        const int64_t t0 = b0 + (int64_t)threadIdx.x * kTileScanItems;
+        int v[kTileScanItems];
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < kTileScanItems; k++) {
+            v[k] = (t0 + k < ntiles) ? tile_sum[t0 + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int ex = block_exclusive_scan(sum, smem, total) + carry;
+#pragma unroll
+        for (int k = 0; k < kTileScanItems; k++) {
+            if (t0 + k < ntiles) tile_offs[t0 + k] = ex;
+            ex += v[k];
+        }
+        carry += total;
     }
 }
 
@@ -591,7 +629,6 @@ template <int PREC, int DYN> struct Me {
     RingInfo ri;
     int32_t n_ring;
     const FixPair* fixr;
-    FixPair fp0;
 };
 
 template <int PREC, int DYN>
@@ -604,7 +641,6 @@ __device__ __forceinline__ Me<PREC, DYN> make_me(const Ctx& C, const DevRep& R, 
     m.ri = RingInfo{0, 0, 0};
     m.n_ring = 0;
     m.fixr = C.fix + (int64_t)rep * MAVI_MAX_TYPES * MAVI_MAX_TYPES;
-    if constexpr (PREC == kPrecMixed) m.fp0 = m.fixr[0];
     if constexpr (DYN == MAVI_DYN_RINGS) {
         m.uid = C.uid_cur[s];
         m.ri = ring_info(C, R, m.uid);
@@ -673,7 +709,7 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
     }
     if constexpr (DYN == MAVI_DYN_LEN_JONES || DYN == MAVI_DYN_RUN_TUMBLE) {
         if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
-            if (!inside_cutoff(me.fp0, dxi, dyi)) return;
+            if (!inside_cutoff(me.fixr[0], dxi, dyi)) return;
         }
         float fxh, fxl, fyh, fyl;
         lj_pair_df(R, dxi, dyi, fxh, fxl, fyh, fyl);
@@ -707,7 +743,7 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
         if (same) fp.k_atr = 0.f;
         pair_fixed<DYN>(R, fp, dxi, dyi, fx, fy);
     } else {
-        pair_fixed<DYN>(R, me.fp0, dxi, dyi, fx, fy);
+        pair_fixed<DYN>(R, me.fixr[0], dxi, dyi, fx, fy);
     }
     acc.add(fx, fy);
 }
@@ -1291,8 +1327,18 @@ __device__ __forceinline__ int64_t walls_and_bin(const Ctx& C, int32_t rep, cons
 #ifndef MAVI_PASS_BLOCKS_FP64
 #define MAVI_PASS_BLOCKS_FP64 4    // FP64 form (128 registers)
 #endif
+#ifndef MAVI_PASS_BLOCKS_RINGS
+#define MAVI_PASS_BLOCKS_RINGS 8   // mixed-form rings pair pass
+#endif
+#ifndef MAVI_PASS_BLOCKS_LJ
+#define MAVI_PASS_BLOCKS_LJ 8      // mixed-form Lennard-Jones / WCA passes (double-float pair term)
+#endif
 template <int PREC, int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
-__global__ void __launch_bounds__(kPassThreads, PREC == kPrecFP64 ? MAVI_PASS_BLOCKS_FP64 : MAVI_PASS_BLOCKS_MIXED)
+__global__ void __launch_bounds__(kPassThreads,
+                                  PREC == kPrecFP64 ? MAVI_PASS_BLOCKS_FP64
+                                  : DYN == MAVI_DYN_RINGS ? MAVI_PASS_BLOCKS_RINGS
+                                  : (DYN == MAVI_DYN_LEN_JONES || DYN == MAVI_DYN_RUN_TUMBLE) ? MAVI_PASS_BLOCKS_LJ
+                                  : MAVI_PASS_BLOCKS_MIXED)
 k_pass(Ctx C, int32_t with_wall_forces) {
     __shared__ Stage<PREC, DYN> stage[kPassWarps];
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1432,8 +1478,12 @@ __device__ __forceinline__ void ring_vc_store(const Ctx& C, int64_t g, int lane,
     if (lane == 0) C.ring_vc[g] = make_double2((double)vcx, (double)vcy);
 }
 
+#ifndef MAVI_RINGS_MIN_BLOCKS
+#define MAVI_RINGS_MIN_BLOCKS 8    // ring-kernel blocks per SM (64 registers; measured faster than 4, 5 or 6)
+#endif
 template <int PREC>
-__global__ void __launch_bounds__(32 * kRingWarps) k_rings(Ctx C, int64_t total_rings, int32_t do_update) {
+__global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_rings(Ctx C, int64_t total_rings,
+                                                                                 int32_t do_update) {
     __shared__ double2 sp_[kRingWarps][kRingMax];
     __shared__ int32_t ss_[kRingWarps][kRingMax];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

@@ -51,6 +51,7 @@ struct MaviSystem {
     bool counts_valid = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    int32_t* tile_offs = nullptr;  // exclusive scan of the tile totals (grids of many tiles)
     bool profiling = false;
     int profile_mode = 0;          // 0 off, 1 per kernel kind + whole step, 2 whole step only
     int graph_profile_mode = 0;    // profile_mode the captured graph was recorded with
