@@ -133,3 +133,36 @@ def rms(f):
 def rel_force_err(f, ref):
     """max_i |F_i - F_i^ref| / RMS(|F^ref|)."""
     return float(np.max(np.linalg.norm(f - ref, axis=1)) / max(rms(ref), 1e-300))
+
+
+def lj_lines(mg, kind="slippery", precision="fp64", seed=6, n_side=14, potential="harm"):
+    """LJ gas in a rigid square box with line walls inside (ManyWalls): three
+    slippery segments, or the same segments as PotentialWalls (harmonic or
+    Lennard-Jones, repulsion mode)."""
+    lj = mg.LenJonesCfg(1.0, 1.0)
+    a = 1.3
+    L = n_side * a
+    rng = np.random.default_rng(seed)
+    g = (np.arange(n_side) + 0.5) * a
+    pts = np.stack(np.meshgrid(g, g), axis=-1).reshape(-1, 2) + rng.uniform(-0.05, 0.05, (n_side * n_side, 2))
+    segs = [((0.3 * L, 0.2 * L), (0.3 * L, 0.7 * L)), ((0.55 * L, 0.5 * L), (0.85 * L, 0.8 * L)),
+            ((0.5 * L, 0.15 * L), (0.8 * L, 0.15 * L))]
+    # keep particles off the segments (distance > 0.6)
+    def seg_dist(p, s):
+        (x1, y1), (x2, y2) = s
+        d = np.array([x2 - x1, y2 - y1]); t = np.clip(((p - [x1, y1]) @ d) / (d @ d), 0, 1)
+        return np.linalg.norm(p - ([x1, y1] + t[:, None] * d), axis=1)
+    keep = np.min(np.stack([seg_dist(pts, s) for s in segs]), axis=0) > 0.6
+    pts = pts[keep]
+    vel = mg.maxwell_vel(len(pts), 0.8, rng)
+    lines = mg.LinesCfg(segs)
+    if kind == "slippery":
+        inner = (mg.SlipperyWalls(), lines)
+    else:
+        pot = mg.HarmTruncCfg(k_rep=20.0, k_atr=0.0, dist_eq=1.0, dist_max=1.0) if potential == "harm" \
+            else mg.LenJonesCfg(0.8, 1.0)
+        inner = (mg.PotentialWalls(pot, mode="repulsion"), lines)
+    space = mg.SpaceCfg.many([(mg.RigidWalls(), mg.RectangleCfg(L, L, (0.0, 0.0))), inner])
+    nc = max(3, int(L // 2.5))
+    return mg.System(mg.SecondLawState(pts, vel), space, lj,
+                     mg.IntCfg(dt=1e-3, chunks_cfg=mg.ChunksCfg(nc, nc), device=mg.CUDADevice(precision=precision)))

@@ -82,10 +82,13 @@ def test_circle_walls(mg, orc, wall):
 
 
 @pytest.mark.parametrize("kind", ["szabo", "rtp"])
-def test_self_propelled_injected_noise(mg, orc, kind):
-    s = self_propelled(mg, kind, 400)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_self_propelled_injected_noise(mg, orc, kind, precision):
+    s = self_propelled(mg, kind, 400, precision=precision)
     step = mg.szabo_step if kind == "szabo" else mg.rtp_step
     ref = orc.from_system(s)
+    err = rel_force_err(s.calc_forces(), ref.forces())
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
     n = s.handle.noise_count()
     assert n == ref.noise_count()
     rng = np.random.default_rng(11)
@@ -94,8 +97,9 @@ def test_self_propelled_injected_noise(mg, orc, kind):
     s.run(steps, step, noise=noise)
     ref.step(steps, noise=noise)
     p, _, pol = ref.state()
-    assert np.max(np.abs(s.state.pos - p)) < 1e-9
-    assert np.max(np.abs(s.state.pol_angle - pol)) < 1e-9
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert np.max(np.abs(s.state.pos - p)) < tol
+    assert np.max(np.abs(s.state.pol_angle - pol)) < tol
     s.close()
 
 
@@ -377,4 +381,25 @@ def test_rings_in_circular_container(mg, orc, precision):
     assert np.max(np.abs(s.state.pol - pol)) < tol
     assert np.all(areas > 0)
     ref.close()
+    s.close()
+
+
+@pytest.mark.parametrize("kind,potential", [("slippery", None), ("potential", "harm"), ("potential", "lj")])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_line_walls(mg, orc, kind, potential, precision):
+    """LinesCfg walls inside a rigid box: slippery segments (walls!,
+    src/integration.jl:327-378) and PotentialWalls on segments
+    (calc_walls_forces!, src/integration.jl:243-256, signed_pos
+    src/configs.jl:119-135)."""
+    from helpers import lj_lines
+    s = lj_lines(mg, kind=kind, precision=precision, potential=potential or "harm")
+    ref = orc.from_system(s)
+    err = rel_force_err(s.calc_forces(include_walls=True), ref.forces(include_walls=True))
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+    mg.run_system(s, num_steps=1000)
+    ref.step(1000)
+    p, v, _ = ref.state()
+    tol = 1e-8 if precision == "fp64" else 1e-3
+    assert np.max(np.abs(s.state.pos - p)) < tol
+    assert np.max(np.abs(s.state.vel - v)) < tol * 10
     s.close()
