@@ -260,7 +260,7 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
     int64_t cell = 0;
     int32_t cap = 1 << 30;
     if (valid) {
-        const DevRep& R = C.reps[C.rep_out[s]];
+        const DevRep& R = C.reps[C.num_reps > 1 ? C.rep_out[s] : 0];
         double2 p = C.pos_out[s];
         const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
         cell = bin_final<PREC>(C, R, s, p.x, p.y, guess);
@@ -412,7 +412,7 @@ __global__ void k_permute(Ctx C) {
     int32_t dst = b + rank;
     C.pos_cur[dst] = C.pos_out[sm];
     C.uid_cur[dst] = u;
-    C.rep_cur[dst] = C.rep_out[sm];
+    if (C.num_reps > 1) C.rep_cur[dst] = C.rep_out[sm];   // one replica: stays 0
     C.cell_cur[dst] = c;
     C.slot_of[u] = dst;
     if constexpr (HAS_VEL) C.vel_cur[dst] = C.vel_out[sm];
@@ -1345,7 +1345,9 @@ k_pass(Ctx C, int32_t with_wall_forces) {
     bool valid = s < C.M;
     int64_t new_cell = 0;
     int32_t cap = 1 << 30;
-    int32_t rep = valid ? C.rep_cur[s] : 0;
+    // one replica: no load in the way of the descriptor (its fields load in
+    // parallel with the particle's own state)
+    int32_t rep = (valid && C.num_reps > 1) ? C.rep_cur[s] : 0;
     const DevRep& R = C.reps[rep];
     int32_t cell = valid ? C.cell_cur[s] : 0;
     const double2* P = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
@@ -1449,7 +1451,7 @@ k_pass(Ctx C, int32_t with_wall_forces) {
             if constexpr (HAS_VEL) C.vel_out[s] = make_double2(vx, vy);
             if constexpr (HAS_POL && !(PASS == kPassSzabo || PASS == kPassRTP)) C.pol_out[s] = C.pol_cur[s];
             C.uid_out[s] = C.uid_cur[s];
-            C.rep_out[s] = rep;
+            if (C.num_reps > 1) C.rep_out[s] = rep;
             cap = R.has_chunks ? R.cap : (1 << 30);
         }
     }
