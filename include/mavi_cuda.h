@@ -275,7 +275,13 @@ int mavi_get_chunks(MaviSystem* sys, int32_t replica, int32_t* num_in_chunk,
  * Writes forces of all replicas (2*N doubles, user particle order). */
 int mavi_calc_forces(MaviSystem* sys, int32_t include_walls, double* forces_out);
 
-/* Copy host state in / out (user particle order, same layout as mavi_create). */
+/* Copy host state in / out (user particle order, same layout as mavi_create).
+ * mavi_upload_state returns once the copy and the chunk histogram of the new
+ * state are queued on the handle's stream: from page-locked host memory the
+ * copy may still be in flight, so the arrays must not change before the next
+ * call on this handle that returns results (mavi_step, mavi_download_state,
+ * mavi_calc_forces, ...); a state outside the chunk grid is reported by that
+ * call. mavi_download_state waits for its copies. */
 int mavi_upload_state(MaviSystem* sys, const double* pos, const double* vel,
                       const double* pol);
 int mavi_download_state(MaviSystem* sys, double* pos, double* vel, double* pol);

@@ -813,7 +813,7 @@ int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const
     launch_count(s);
     s->counts_valid = true;
     CUDA_TRY(s, cudaGetLastError());
-    return check_device_error(s);
+    return MAVI_OK;   // device errors of this state surface at the next synchronising call
 }
 
 int mavi_download_state(MaviSystem* s, double* pos, double* vel, double* pol) {
@@ -828,8 +828,7 @@ int mavi_download_state(MaviSystem* s, double* pos, double* vel, double* pol) {
         CUDA_TRY(s, cudaMemcpyAsync(pol, s->pol_user, sizeof(double) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
     if (pol && s->is_rings)
         CUDA_TRY(s, cudaMemcpyAsync(pol, s->C.ring_pol, sizeof(double) * s->total_rings, cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
-    return MAVI_OK;
+    return check_device_error(s);   // waits for the copies
 }
 
 int64_t mavi_noise_count(MaviSystem* s) { return s ? s->noise_count : -1; }

@@ -8,7 +8,8 @@
                  at area fraction 0.70, relaxed by 200 overdamped steps;
                  overdamped mobility 1, dt = 1e-2, chunks 542x542.
   lj_4194304     2D LJ, 2048x2048 grid (offset 0.4), periodic box, Maxwell
-                 velocities T = 0.5, Verlet dt = 5e-4, chunks 1103x1103.
+                 velocities T = 0.5, Verlet dt = 5e-4, chunks 1103x1103
+                 (lj_262144: the same at 512x512, for profiling).
   lj_batch_512   512 LJ replicas, N log-uniform in [1000, 65536], density
                  0.6, rigid/periodic x rectangle/circle, Maxwell T in
                  [0.3, 1.0], dt = 1e-3, one handle.
@@ -161,9 +162,15 @@ def rings_batch(num_replicas=64, precision="mixed", seed=5, n_per_ring=30, rings
     return systems, None
 
 
+def lj_262144(precision="fp64", seed=3, use_graph=True):
+    """The 4,194,304-particle LJ state at 512 x 512 (profiling-size case)."""
+    return lj_4194304(precision=precision, seed=seed, use_graph=use_graph, side=512)
+
+
 WORKLOADS = {
     "lj_1024": lj_1024,
     "harm_262144": harm_262144,
+    "lj_262144": lj_262144,
     "lj_4194304": lj_4194304,
     "lj_batch_512": lj_batch,
     "rings_64": rings_batch,

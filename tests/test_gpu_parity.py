@@ -186,8 +186,9 @@ def test_out_of_grid_reports_error(mg):
     s = lj_grid(mg, 8, 8, wall="rigid", chunks=(4, 4))
     s.calc_forces()
     s.state.pos[5] = (-20.0, 3.0)
+    s.upload()                      # queued; the next call that returns results reports it
     with pytest.raises(mg.MaviError) as e:
-        s.upload()
+        s.calc_forces()
     assert e.value.status == mg.abi.MAVI_ERR_OUT_OF_GRID
     s.state.pos[5] = (1.0, 1.0)
     s.upload()                      # the handle stays usable
