@@ -273,6 +273,23 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
     R.u_f = (float)u;
     R.u2_f = (float)(u * u);
     R.u2_d = u * u;
+    // float pre-check of a single PotentialWalls circle with the truncated
+    // harmonic potential (the wall force vanishes away from the circle)
+    R.wall_precheck = 0;
+    if (p.num_spaces == 1 && p.spaces[0].wall == MAVI_WALL_POTENTIAL && p.spaces[0].geometry == MAVI_GEOM_CIRCLE &&
+        p.spaces[0].pot_kind == MAVI_DYN_HARM_TRUNC &&
+        (p.spaces[0].pot_mode == MAVI_POTMODE_INSIDE || p.spaces[0].pot_mode == MAVI_POTMODE_REPULSION)) {
+        const MaviSpace& sp = p.spaces[0];
+        const double lo = sp.radius - sp.pot_params[3], hi = sp.radius + sp.pot_params[3];
+        if (lo > 0) {
+            R.wall_precheck = sp.pot_mode == MAVI_POTMODE_INSIDE ? 1 : 2;
+            R.wall_cx_u = std::llround((sp.cx - R.cx0) * R.inv_u);
+            R.wall_cy_u = std::llround((sp.cy - R.cy0) * R.inv_u);
+            // margins far above the float rounding of the test (relative 1e-7)
+            R.wall_lo2_u = (float)(lo * R.inv_u * lo * R.inv_u * (1.0 - 1e-4));
+            R.wall_hi2_u = (float)(hi * R.inv_u * hi * R.inv_u * (1.0 + 1e-4));
+        }
+    }
     R.sx_u = std::llround(R.chunk_l / u);
     R.sy_u = std::llround(R.chunk_h / u);
     R.bx_u = R.sx_u * R.cols;
@@ -591,6 +608,12 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
                 // area0 (src/rings/configs.jl:221-226)
                 const double a0 = p.rings.num_particles[t] * p.rings.l_spring[t] / p.rings.p0[t];
                 R.ring_a0sq[t] = a0 * a0;
+                // mixed form: 2 A0 / u^2 as an integer (the area is summed exactly in units^2)
+                const long double uu = (long double)R.u2_d;
+                const __int128 iv = (__int128)(2.0L * (long double)R.ring_a0sq[t] / uu + 0.5L);
+                R.ring_a0x2_hi[t] = (long long)(iv >> 64);
+                R.ring_a0x2_lo[t] = (unsigned long long)iv;
+                R.ring_karea_f[t] = (float)(p.rings.k_area[t] * R.u2_d * 0.5);
                 R.ring_ks_f[t] = (float)p.rings.k_spring[t];
                 R.ring_ls_f[t] = (float)p.rings.l_spring[t];
                 R.ring_kb_f[t] = (float)p.rings.k_bend[t];

@@ -82,6 +82,16 @@ struct DevRep {
     float dt_f;
     int32_t _pad3;
     double u2_d;           // u^2 in double (areas from integer units^2)
+    // mixed-form rings: 2 A0 / u^2 per type as a 128-bit integer (hi, lo words),
+    // k_area * u^2 / 2 in float, and the PotentialWalls circle pre-check in
+    // units from the centre of chunk (0, 0): no force where r^2 < wall_lo2
+    // (inside mode) or outside [wall_lo2, wall_hi2] (repulsion)
+    long long ring_a0x2_hi[MAVI_MAX_TYPES];
+    unsigned long long ring_a0x2_lo[MAVI_MAX_TYPES];
+    float ring_karea_f[MAVI_MAX_TYPES];
+    int32_t wall_precheck;          // 0 none, 1 inside mode, 2 repulsion
+    long long wall_cx_u, wall_cy_u;
+    float wall_lo2_u, wall_hi2_u;
 };
 
 // ---------------------------------------------------------------------------

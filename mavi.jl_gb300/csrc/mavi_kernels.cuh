@@ -1529,11 +1529,11 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     // returns the chunk of the updated position (binning fused here: the
     // histogram of the next step is taken in this kernel)
     const int32_t cap = R.has_chunks ? R.cap : (1 << 30);
-    auto finish = [&](int p, double2 xc, V fx, V fy) -> int64_t {
+    auto finish = [&](int p, double2 xc, V fx, V fy, bool near_wall = true) -> int64_t {
         int32_t s = S[p];
         if constexpr (PREC == kPrecFP64) { double2 f = C.fd[s]; fx += f.x; fy += f.y; }
         else { float2 f = C.ff[s]; fx += f.x; fy += f.y; }
-        if (R.has_wall_forces) {
+        if (R.has_wall_forces && near_wall) {
             double wx = 0.0, wy = 0.0;
             add_wall_forces(C, rep, R, xc.x, xc.y, wx, wy);
             fx += (V)wx;
@@ -1609,11 +1609,18 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
                 const long long ohi = __shfl_xor_sync(full, hi, o);
                 a2 += (__int128)(((unsigned __int128)(unsigned long long)ohi << 64) | olo);
             }
-            const double a2d = fma((double)(long long)(a2 >> 64), 18446744073709551616.0,
-                                   (double)(unsigned long long)a2);
-            const double area = a2d * R.u2_d * 0.5;
-            if (lane == 0) C.ring_area[g] = area;
-            const float fa = (float)(rc.k_area[t] * (area - R.ring_a0sq[t]));
+            // area force factor k_area (A - A0) from the exact integer 2A - 2A0 (units^2)
+            const __int128 a0x2 = (__int128)(((unsigned __int128)(unsigned long long)R.ring_a0x2_hi[t] << 64) |
+                                             R.ring_a0x2_lo[t]);
+            const __int128 d2a = a2 - a0x2;
+            const long long d2a_c = d2a > (__int128)INT64_MAX ? INT64_MAX
+                                  : (d2a < (__int128)INT64_MIN ? INT64_MIN : (long long)d2a);
+            const float fa = i64_to_f32(d2a_c) * R.ring_karea_f[t];
+            if (lane == 0) {
+                const double a2d = fma((double)(long long)(a2 >> 64), 18446744073709551616.0,
+                                       (double)(unsigned long long)a2);
+                C.ring_area[g] = a2d * R.u2_d * 0.5;
+            }
             const float uf = R.u_f;
             const float bxf = i64_to_f32(bx) * uf, byf = i64_to_f32(by) * uf;
             const float L = sqrtf(bxf * bxf + byf * byf);
@@ -1638,8 +1645,15 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
                 fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
                 fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
             }
+            // PotentialWalls circle: float test in units, exact FP64 only near the wall
+            bool near_wall = true;
+            if (R.wall_precheck) {
+                const float wx = i64_to_f32(X - R.wall_cx_u), wy = i64_to_f32(Y - R.wall_cy_u);
+                const float r2 = fmaf(wx, wx, wy * wy);
+                near_wall = !(r2 < R.wall_lo2_u) && !(R.wall_precheck == 2 && r2 > R.wall_hi2_u);
+            }
             int64_t nc = 0;
-            if (act) nc = finish(p, P[p], fx, fy);
+            if (act) nc = finish(p, P[p], fx, fy, near_wall);
             if (do_update) count_into_chunk(C, act, S[p], nc, cap);
             ring_vc_store(C, g, lane, do_update, vcx, vcy);
             return;
