@@ -271,7 +271,18 @@ def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
         return 4 + 4 + 4 + 4 + 4 + 4   # r cell, rank, uid; w src_of, key_of, cell_at
     if kind == "bin_scan":
         return 0                  # per chunk, not per particle (counted in the chunk term)
+    if kind == "update" and step_kind == abi.MAVI_STEP_RINGS:
+        # k_rings: r slot_of, x, (off), cell, F, uid; w x', (off'), uid, rep, cell, rank
+        f = 8 if mixed else 16
+        return (4 + 16 + off + 4 + f + 4) + (16 + off + 4 + 4 + 4 + 4)
     return 0
+
+
+def ring_bytes(precision):
+    """Per-ring bytes of the rings update (k_rings + k_ring_pol): ring replica,
+    type, (cos, sin), velocity sum, area, angle; FP32 pairs in the mixed form."""
+    v = 8 if precision == "mixed" else 16
+    return (4 + 4 + v) + (v + 8) + (8 + 4 + 4 + v + v) + (8 + v)
 
 
 # Flops per pair evaluation (sqrt and division count 1 each): HarmTrunc 16,
@@ -290,12 +301,14 @@ def ncu_traffic(workload, precision, kernel):
 
 
 def roofline(meas, n, precision, step_kind, abi, peaks, candidate_pairs, fma_peak, dyn_kind, has_vel,
-             workload=None):
+             workload=None, num_rings=0):
     kinds = meas["kinds"]
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     avg_ms = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1)
     bpp = algorithmic_bytes(dom, precision, step_kind, abi, has_vel)
     traffic_bytes = bpp * n
+    if dom == "update" and step_kind == abi.MAVI_STEP_RINGS:
+        traffic_bytes += ring_bytes(precision) * num_rings
     achieved = traffic_bytes / (avg_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
     rf = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -513,7 +526,7 @@ def main():
         r.first.fill_params(params, r.kind)
         rf = roofline(m, n, precision, r.kind, abi, peaks, stats.candidate_pairs,
                       fma[precision], params.dyn.kind, getattr(r.first.state, "vel", None) is not None,
-                      args.workload)
+                      args.workload, sum(int(getattr(q.state, "num_rings", 0) or 0) for q in r.systems))
         line_forms[precision] = {"value": v, "ms_per_step": m["total_ms"] / K, "roofline": rf,
                                  "kernels_ms_per_step": {k: d["ms"] / K for k, d in m["kinds"].items()},
                                  "gpu_launches": m["launches_per_step"] * K}

@@ -289,7 +289,10 @@ int mavi_download_state(MaviSystem* sys, double* pos, double* vel, double* pol);
 /* Noise for the next step in MAVI_NOISE_INJECTED mode: per replica, Szabo uses
  * one standard normal per particle (src/integration.jl:460), RTP two uniforms
  * per particle (src/integration.jl:493-495), rings one standard normal per ring
- * (src/rings/integration.jl:348). `count` must equal mavi_noise_count(). */
+ * (src/rings/integration.jl:348); after all replicas' numbers, one uniform in
+ * [0, 1) per random-polarisation spawn box of every replica, in replica and
+ * box order (src/rings/sources.jl:24). `count` must be a positive multiple of
+ * mavi_noise_count() (consecutive steps). */
 int64_t mavi_noise_count(MaviSystem* sys);
 int mavi_set_noise(MaviSystem* sys, const double* noise, int64_t count);
 int mavi_set_seed(MaviSystem* sys, uint64_t seed);
@@ -316,6 +319,64 @@ int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
 int mavi_rings_neighbors_config(MaviSystem* sys, int32_t enable, int32_t only_count, int32_t type_all,
                                 double tol);
 int mavi_rings_neighbors(MaviSystem* sys, int32_t replica, int32_t* counts, int32_t* lists);
+
+/* Variable number of rings (VarRingsIds, src/rings/states.jl:20-40, 152-223;
+ * ActiveState, src/states.jl:14-20) with sources and sinks (SourceCfg /
+ * SinkCfg, src/rings/sources.jl; RingsInfo, src/rings/rings.jl:162-186).
+ *
+ * mavi_rings_sources sets, for one replica, the initial active mask (one
+ * int32 per ring, nonzero = active; NULL = all active) and the tuple of
+ * sources and sinks in the reference's order. Every later step begins as the
+ * reference's step! does (src/rings/integration.jl:522-527): the centre of
+ * mass of every active ring (update_cms!), then each entry in order —
+ * a sink removes every ring of the active-id view whose centre lies in its
+ * geometry (process_sink!), a source finds which spawn boxes hold no particle
+ * of its chunk lists (update_area_empty!, ChunksChecker / PosChecker) and
+ * puts a ring into the first inactive slot for each empty box (add_ring!,
+ * process_source!) — then the active ids are recomputed (update_ids!).
+ * Inactive rings keep their positions and take no part in forces, update,
+ * walls or chunks.
+ *
+ * boxes: the spawn boxes of all sources, in entry order (Source.bbox, in the
+ * order of its i, j loops, src/rings/sources.jl:142-160); spawn_xy: nmax
+ * points per box (Source.bbox_spawn_pos); chunk_rc: the (row, col) pairs,
+ * 0-based, of every box's chunk list (ChunksChecker.ids), concatenated.
+ * Random spawn polarisations (spawn_pol = :random) draw one uniform in [0, 1)
+ * per random-polarisation box per step, after the rings' normals in the
+ * step's noise (see mavi_noise_count); the angle is u * 2 * pi.
+ * Call before the first step; the chunk lists and forces are rebuilt for the
+ * active set. */
+#define MAVI_SRC_SOURCE 0
+#define MAVI_SRC_SINK   1
+#define MAVI_SPAWN_POL_FIXED  0
+#define MAVI_SPAWN_POL_RANDOM 1
+#define MAVI_MAX_SOURCE_ENTRIES 8
+#define MAVI_MAX_SPAWN_BOXES   64   /* per source entry */
+
+typedef struct MaviSourceEntry {
+    int32_t kind;          /* MAVI_SRC_SOURCE or MAVI_SRC_SINK                     */
+    int32_t num_boxes;     /* source: spawn boxes, cfg.size[1] * cfg.size[2]        */
+    int32_t pol_mode;      /* source: MAVI_SPAWN_POL_*                              */
+    int32_t geometry;      /* sink: MAVI_GEOM_RECTANGLE or MAVI_GEOM_CIRCLE         */
+    double pol;            /* source: fixed spawn angle                             */
+    double pad;            /* source: cfg.pad (is_inside padding of the boxes)      */
+    double length, height, bl_x, bl_y;   /* sink RectangleCfg                       */
+    double radius, cx, cy;               /* sink CircleCfg                          */
+} MaviSourceEntry;
+
+typedef struct MaviSpawnBox {
+    double bl_x, bl_y, length, height;   /* Source.bbox[i]                          */
+    int32_t num_chunks;    /* chunk-list length; -1: every active particle (PosChecker) */
+    int32_t _pad0;
+} MaviSpawnBox;
+
+int mavi_rings_sources(MaviSystem* sys, int32_t replica, const int32_t* active_mask, int32_t num_entries,
+                       const MaviSourceEntry* entries, const MaviSpawnBox* boxes, const double* spawn_xy,
+                       const int32_t* chunk_rc);
+/* The rings ids of one replica: active mask (num_rings int32), uids
+ * (num_rings int32, VarRingsIds.uids) and the number of active rings. */
+int mavi_rings_active(MaviSystem* sys, int32_t replica, int32_t* active_mask, int32_t* uids,
+                      int32_t* num_active);
 
 int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
 /* Device-time profiling (and reset of the accumulated profile). on: 0 off,

@@ -67,6 +67,13 @@ MAVI_MAX_SPACES = 4
 MAVI_MAX_LINES = 16
 MAVI_MAX_TYPES = 4
 
+MAVI_SRC_SOURCE = 0
+MAVI_SRC_SINK = 1
+MAVI_SPAWN_POL_FIXED = 0
+MAVI_SPAWN_POL_RANDOM = 1
+MAVI_MAX_SOURCE_ENTRIES = 8
+MAVI_MAX_SPAWN_BOXES = 64
+
 MAVI_KERNEL_BIN_COUNT = 0
 MAVI_KERNEL_BIN_SCAN = 1
 MAVI_KERNEL_BIN_SCATTER = 2
@@ -153,10 +160,26 @@ class MaviProfile(C.Structure):
     ]
 
 
+class MaviSourceEntry(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("num_boxes", C.c_int32), ("pol_mode", C.c_int32), ("geometry", C.c_int32),
+        ("pol", C.c_double), ("pad", C.c_double),
+        ("length", C.c_double), ("height", C.c_double), ("bl_x", C.c_double), ("bl_y", C.c_double),
+        ("radius", C.c_double), ("cx", C.c_double), ("cy", C.c_double),
+    ]
+
+
+class MaviSpawnBox(C.Structure):
+    _fields_ = [
+        ("bl_x", C.c_double), ("bl_y", C.c_double), ("length", C.c_double), ("height", C.c_double),
+        ("num_chunks", C.c_int32), ("_pad0", C.c_int32),
+    ]
+
+
 STRUCTS = {
     "MaviSpace": MaviSpace, "MaviRingsCfg": MaviRingsCfg, "MaviDynamicCfg": MaviDynamicCfg,
     "MaviReplicaParams": MaviReplicaParams, "MaviOptions": MaviOptions, "MaviStats": MaviStats,
-    "MaviProfile": MaviProfile,
+    "MaviProfile": MaviProfile, "MaviSourceEntry": MaviSourceEntry, "MaviSpawnBox": MaviSpawnBox,
 }
 
 # Exported entry points and their signatures (restype, argtypes).
@@ -188,6 +211,9 @@ SIGNATURES = {
     "mavi_fma_peak": (C.c_int, [C.c_int32, C.c_int32, _dp]),
     "mavi_rings_neighbors_config": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
     "mavi_rings_neighbors": (C.c_int, [_vp, C.c_int32, _ip, _ip]),
+    "mavi_rings_sources": (C.c_int, [_vp, C.c_int32, _ip, C.c_int32, C.POINTER(MaviSourceEntry),
+                                     C.POINTER(MaviSpawnBox), _dp, _ip]),
+    "mavi_rings_active": (C.c_int, [_vp, C.c_int32, _ip, _ip, _ip]),
     "mavi_chunk_lists_noalloc": (C.c_int, [C.POINTER(MaviReplicaParams), _vp, C.c_int64, _vp, _vp, _vp,
                                            C.c_char_p, C.c_int32]),
 }

@@ -18,7 +18,7 @@ using namespace mavi;
 // ---------------------------------------------------------------------------
 static void launch_count(MaviSystem* s) {
     record_begin(s, MAVI_KERNEL_BIN_COUNT);
-    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->Ctot, s->stream);
+    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->nscan, s->stream);
     cudaMemsetAsync(s->C.tile_sum, 0, sizeof(int32_t) * s->ntiles, s->stream);
     if (s->prec == MAVI_PREC_FP64) count_fp64(s, 2);
     else count_mixed(s, 2);
@@ -34,7 +34,7 @@ static void launch_rebin(MaviSystem* s, bool advance) {
     record_begin(s, MAVI_KERNEL_BIN_SCAN);
     if (s->tile_offs)   // many tiles: their offsets first, in one block
         k_tile_offsets<<<1, kTileScanThreads, 0, s->stream>>>(s->C.tile_sum, s->ntiles, s->tile_offs);
-    k_scan<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->Ctot, s->C.tile_sum, s->C.start,
+    k_scan<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->nscan, s->C.tile_sum, s->C.start,
                                                                s->C.d_step, advance ? 1 : 0, s->tile_offs);
     record_end(s, MAVI_KERNEL_BIN_SCAN);
     record_begin(s, MAVI_KERNEL_BIN_SCATTER);
@@ -43,6 +43,8 @@ static void launch_rebin(MaviSystem* s, bool advance) {
     record_begin(s, MAVI_KERNEL_BIN_SORT);
     if (s->prec == MAVI_PREC_FP64) sort_permute_fp64(s);
     else sort_permute_mixed(s);
+    // outside the step, keep the sources' view (current state in *_out, *_cur order)
+    if (s->var_rings && !advance) k_out_from_cur<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C);
     record_end(s, MAVI_KERNEL_BIN_SORT);
     s->counts_valid = false;
 }
@@ -53,11 +55,20 @@ static void launch_step(MaviSystem* s) {
         cudaEventRecordWithFlags(s->ev.step_a, s->stream, cudaEventRecordExternal);
         s->ev.step_used = 1;
     }
+    if (s->var_rings) {
+        // step! head: update_cms!, sources and sinks, update_ids!
+        // (src/rings/integration.jl:522-526), then the histogram of the active set
+        record_begin(s, MAVI_KERNEL_BIN_COUNT);
+        if (s->prec == MAVI_PREC_FP64) sources_fp64(s);
+        else sources_mixed(s);
+        record_end(s, MAVI_KERNEL_BIN_COUNT);
+        s->counts_valid = true;
+    }
     launch_rebin(s, true);
     if (s->prec == MAVI_PREC_FP64) step_body_fp64(s);
     else step_body_mixed(s);
     if (s->profiling) cudaEventRecordWithFlags(s->ev.step_b, s->stream, cudaEventRecordExternal);
-    s->counts_valid = true;
+    s->counts_valid = !s->var_rings;
 }
 
 // ---------------------------------------------------------------------------
@@ -619,6 +630,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
                 R.ring_kb_f[t] = (float)p.rings.k_bend[t];
                 R.ring_vo_f[t] = (float)p.rings.vo[t];
                 R.ring_mu_f[t] = (float)p.rings.mobility[t];
+                R.ring_dt_tau_f[t] = (float)(p.dt / p.rings.relax_time[t]);
+                R.ring_noise_amp[t] = std::sqrt(2 * p.rings.rot_diff[t] * p.dt);
             }
         }
         R.dt_f = (float)p.dt;
@@ -648,7 +661,10 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     s->Ctot = c0;
     s->total_rings = ring0;
     s->noise_count = noise0;
-    s->ntiles = (s->Ctot + kScanTile - 1) / kScanTile;
+    // rings handles scan one more chunk: the parking chunk of inactive rings
+    s->nscan = s->Ctot + (s->is_rings ? 1 : 0);
+    s->noise_base = s->noise_count;
+    s->ntiles = (s->nscan + kScanTile - 1) / kScanTile;
     if (s->Nslots >= (1ll << 31) || s->M >= (1ll << 31) || s->Ctot >= (1ll << 31) - 1) {
         delete s;
         return MAVI_ERR_UNSUPPORTED;
@@ -693,7 +709,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     if (cudaMemset(C.cell_out, 0xff, sizeof(int32_t) * M) != cudaSuccess)
         return bail(fail(s, MAVI_ERR_CUDA, "cudaMemset failed for cell_out"));
     ALLOC(C.slot_of, N);
-    ALLOC(C.count, s->Ctot); ALLOC(C.start, s->Ctot + 1);
+    ALLOC(C.count, s->nscan); ALLOC(C.start, s->nscan + 1);
     ALLOC(C.tile_sum, s->ntiles);
     int32_t* ring_types_d = nullptr;
     int32_t* ring_rep_d = nullptr;
@@ -726,6 +742,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     ALLOC(s->d_pairs, 1);
     if (s->noise_count > 0) { ALLOC(s->noise_cur, s->noise_count); }
 #undef ALLOC
+    C.ring_csf = reinterpret_cast<float2*>(C.ring_cs);
+    C.ring_vcf = reinterpret_cast<float2*>(C.ring_vc);
     C.ring_types = ring_types_d;
     C.ring_rep = ring_rep_d;
     C.reps = reps_d;
@@ -736,6 +754,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     C.fix = fix_d;
     C.M = M;
     C.Ctot = s->Ctot;
+    C.park = s->Ctot;
     C.ntiles = s->ntiles;
     C.noise = s->noise_cur;
     C.noise_mode = opt->noise_mode;
@@ -828,13 +847,15 @@ int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const
         CUDA_TRY(s, cudaMemcpyAsync(s->pol_user, pol, sizeof(double) * s->Nslots, cudaMemcpyHostToDevice, s->stream));
     if (s->is_rings && pol) {
         CUDA_TRY(s, cudaMemcpyAsync(s->C.ring_pol, pol, sizeof(double) * s->total_rings, cudaMemcpyHostToDevice, s->stream));
-        k_ring_pol<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
+        if (s->prec == MAVI_PREC_MIXED) k_ring_pol<kPrecMixed><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
+        else k_ring_pol<kPrecFP64><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
     }
     k_gather_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, (s->has_vel && vel) ? s->vel_user : nullptr,
                                                            (s->has_pol && pol) ? s->pol_user : nullptr);
     s->counts_valid = false;
     launch_count(s);
     s->counts_valid = true;
+    if (s->var_rings) launch_rebin(s, false);   // chunk lists of the uploaded state
     CUDA_TRY(s, cudaGetLastError());
     return MAVI_OK;   // device errors of this state surface at the next synchronising call
 }
@@ -891,7 +912,7 @@ int mavi_step(MaviSystem* s, int64_t nsteps) {
         return fail(s, MAVI_ERR_NOISE_MISSING, "%lld steps need noise; %lld steps of noise supplied",
                     (long long)nsteps, (long long)(s->noise_queue_len - s->noise_queue_pos));
     if (nsteps == 0) return MAVI_OK;
-    if (!s->counts_valid) {     // after calc_forces/energies/update_chunks
+    if (!s->counts_valid && !s->var_rings) {     // after calc_forces/energies/update_chunks
         launch_count(s);
         for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
         s->counts_valid = true;
@@ -908,7 +929,7 @@ int mavi_step(MaviSystem* s, int64_t nsteps) {
         }
         if (s->graph_exec) {
             CUDA_TRY(s, cudaGraphLaunch(s->graph_exec, s->stream));
-            s->counts_valid = true;
+            s->counts_valid = !s->var_rings;
             collect_profile(s, s->graph_ev_used);
             collect_step_time(s, s->graph_step_used);
         } else {
@@ -1068,6 +1089,225 @@ int mavi_rings_neighbors(MaviSystem* s, int32_t replica, int32_t* counts, int32_
                     k < counts[i] ? tmp[i * MAVI_MAX_NEIGHBORS + k] - (int32_t)R.slot0 : -1;
     }
     return check_device_error(s);
+}
+
+// ---------------------------------------------------------------------------
+// sources and sinks of the rings model
+// ---------------------------------------------------------------------------
+// Replaces a device buffer owned by the handle with a copy of `n` host
+// elements (nullptr when n == 0). The caller synchronises before the host
+// data goes away.
+static int replace_buffer(MaviSystem* s, void*& slot, const void* data, size_t bytes, const void** out) {
+    if (slot) {
+        cudaStreamSynchronize(s->stream);
+        cudaFree(slot);
+        s->allocs.erase(std::remove(s->allocs.begin(), s->allocs.end(), slot), s->allocs.end());
+        slot = nullptr;
+    }
+    *out = nullptr;
+    if (bytes == 0) return MAVI_OK;
+    char* d = nullptr;
+    if (dalloc(s, &d, bytes) != cudaSuccess) return fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for the sources");
+    slot = d;
+    CUDA_TRY(s, cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, s->stream));
+    *out = d;
+    return MAVI_OK;
+}
+
+// Flattens every replica's sources and sinks into the device arrays and the
+// replicas' descriptors; random spawn polarisations get their places in the
+// step's noise after the replicas' own numbers.
+static int upload_sources(MaviSystem* s) {
+    std::vector<SrcEntryD> ent;
+    std::vector<SrcBoxD> box;
+    std::vector<double2> spawn;
+    std::vector<int32_t> chunks;
+    int64_t noise_idx = s->noise_base;
+    for (int r = 0; r < s->R; r++) {
+        DevRep& R = s->reps_h[r];
+        const MaviSystem::SrcCfg& cfg = s->src_cfg[r];
+        R.src_e0 = (int32_t)ent.size();
+        R.src_ne = (int32_t)cfg.entries.size();
+        R.src_has_sink = 0;
+        size_t b = 0, k = 0;
+        for (const MaviSourceEntry& e : cfg.entries) {
+            SrcEntryD d{};
+            d.kind = e.kind; d.num_boxes = e.kind == MAVI_SRC_SOURCE ? e.num_boxes : 0;
+            d.pol_mode = e.pol_mode; d.geometry = e.geometry;
+            d.box0 = (int32_t)box.size();
+            d.pol = e.pol; d.pad = e.pad;
+            d.length = e.length; d.height = e.height; d.bl_x = e.bl_x; d.bl_y = e.bl_y;
+            d.radius = e.radius; d.cx = e.cx; d.cy = e.cy;
+            if (e.kind == MAVI_SRC_SINK) R.src_has_sink = 1;
+            for (int32_t q = 0; q < d.num_boxes; q++, b++) {
+                const MaviSpawnBox& mb = cfg.boxes[b];
+                SrcBoxD bd{};
+                bd.bl_x = mb.bl_x; bd.bl_y = mb.bl_y; bd.length = mb.length; bd.height = mb.height;
+                bd.num_chunks = mb.num_chunks;
+                bd.chunk0 = (int32_t)chunks.size();
+                bd.spawn0 = (int64_t)spawn.size();
+                bd.noise_idx = e.pol_mode == MAVI_SPAWN_POL_RANDOM ? noise_idx++ : -1;
+                for (int32_t p = 0; p < R.nmax; p++)
+                    spawn.push_back(make_double2(cfg.spawn_xy[2 * (b * R.nmax + p)], cfg.spawn_xy[2 * (b * R.nmax + p) + 1]));
+                for (int32_t c = 0; c < std::max(mb.num_chunks, 0); c++, k++) {
+                    const int32_t row = cfg.chunk_rc[2 * k], col = cfg.chunk_rc[2 * k + 1];
+                    chunks.push_back((int32_t)(R.c0 + (int64_t)col * R.rows + row));
+                }
+                box.push_back(bd);
+            }
+            ent.push_back(d);
+        }
+    }
+    int rc;
+    const void* d[4];
+    if ((rc = replace_buffer(s, s->src_buf[0], ent.data(), sizeof(SrcEntryD) * ent.size(), &d[0]))) return rc;
+    if ((rc = replace_buffer(s, s->src_buf[1], box.data(), sizeof(SrcBoxD) * box.size(), &d[1]))) return rc;
+    if ((rc = replace_buffer(s, s->src_buf[2], spawn.data(), sizeof(double2) * spawn.size(), &d[2]))) return rc;
+    if ((rc = replace_buffer(s, s->src_buf[3], chunks.data(), sizeof(int32_t) * chunks.size(), &d[3]))) return rc;
+    s->C.src_entries = static_cast<const SrcEntryD*>(d[0]);
+    s->C.src_boxes = static_cast<const SrcBoxD*>(d[1]);
+    s->C.src_spawn = static_cast<const double2*>(d[2]);
+    s->C.src_chunks = static_cast<const int32_t*>(d[3]);
+    CUDA_TRY(s, cudaMemcpyAsync(const_cast<DevRep*>(s->C.reps), s->reps_h.data(), sizeof(DevRep) * s->R,
+                                cudaMemcpyHostToDevice, s->stream));
+    // the step's noise grows by the spawn uniforms
+    if (noise_idx != s->noise_count) {
+        CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+        if (s->noise_cur) {
+            cudaFree(s->noise_cur);
+            s->allocs.erase(std::remove(s->allocs.begin(), s->allocs.end(), (void*)s->noise_cur), s->allocs.end());
+            s->noise_cur = nullptr;
+        }
+        s->noise_count = noise_idx;
+        if (s->noise_count > 0 && dalloc(s, &s->noise_cur, s->noise_count) != cudaSuccess)
+            return fail(s, MAVI_ERR_CUDA, "noise buffer allocation failed");
+        s->C.noise = s->noise_cur;
+        s->noise_queue_len = 0;
+        s->noise_queue_pos = 0;
+    }
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    return MAVI_OK;
+}
+
+int mavi_rings_sources(MaviSystem* s, int32_t replica, const int32_t* active_mask, int32_t num_entries,
+                       const MaviSourceEntry* entries, const MaviSpawnBox* boxes, const double* spawn_xy,
+                       const int32_t* chunk_rc) {
+    if (!s || replica < 0 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    if (!s->is_rings) return fail(s, MAVI_ERR_UNSUPPORTED, "sources and sinks belong to the rings model");
+    if (num_entries < 0 || num_entries > MAVI_MAX_SOURCE_ENTRIES || (num_entries > 0 && !entries))
+        return fail(s, MAVI_ERR_INVALID_ARG, "num_entries must be in [0, %d]", MAVI_MAX_SOURCE_ENTRIES);
+    const DevRep& R = s->reps_h[replica];
+    int64_t nbox = 0, nchunk = 0;
+    for (int32_t e = 0; e < num_entries; e++) {
+        const MaviSourceEntry& E = entries[e];
+        if (E.kind == MAVI_SRC_SINK) {
+            if (E.geometry != MAVI_GEOM_RECTANGLE && E.geometry != MAVI_GEOM_CIRCLE)
+                return fail(s, MAVI_ERR_INVALID_ARG, "entry %d: a sink is a rectangle or a circle", e);
+        } else if (E.kind == MAVI_SRC_SOURCE) {
+            if (E.num_boxes < 1 || E.num_boxes > MAVI_MAX_SPAWN_BOXES)
+                return fail(s, MAVI_ERR_INVALID_ARG, "entry %d: 1..%d spawn boxes", e, MAVI_MAX_SPAWN_BOXES);
+            if (E.pol_mode != MAVI_SPAWN_POL_FIXED && E.pol_mode != MAVI_SPAWN_POL_RANDOM)
+                return fail(s, MAVI_ERR_INVALID_ARG, "entry %d: unknown spawn polarisation mode", e);
+            nbox += E.num_boxes;
+        } else {
+            return fail(s, MAVI_ERR_INVALID_ARG, "entry %d: unknown kind %d", e, E.kind);
+        }
+    }
+    if (nbox > 0 && (!boxes || !spawn_xy)) return fail(s, MAVI_ERR_INVALID_ARG, "spawn boxes and points required");
+    for (int64_t b = 0; b < nbox; b++) {
+        if (boxes[b].num_chunks < -1) return fail(s, MAVI_ERR_INVALID_ARG, "box %lld: num_chunks < -1", (long long)b);
+        nchunk += std::max(boxes[b].num_chunks, 0);
+    }
+    if (nchunk > 0 && !chunk_rc) return fail(s, MAVI_ERR_INVALID_ARG, "chunk lists required");
+    for (int64_t k = 0; k < nchunk; k++) {
+        const int32_t row = chunk_rc[2 * k], col = chunk_rc[2 * k + 1];
+        if (row < 0 || row >= R.rows || col < 0 || col >= R.cols)
+            return fail(s, MAVI_ERR_INVALID_ARG, "chunk (%d, %d) outside the %d x %d grid", row, col, R.rows, R.cols);
+    }
+    for (int64_t k = 0; k < 2 * nbox * R.nmax; k++)
+        if (!std::isfinite(spawn_xy[k])) return fail(s, MAVI_ERR_INVALID_ARG, "non-finite spawn position");
+    if (s->src_cfg.empty()) s->src_cfg.resize(s->R);
+    MaviSystem::SrcCfg& cfg = s->src_cfg[replica];
+    cfg.entries.assign(entries, entries + num_entries);
+    cfg.boxes.assign(boxes, boxes + nbox);
+    cfg.spawn_xy.assign(spawn_xy, spawn_xy + 2 * nbox * R.nmax);
+    cfg.chunk_rc.assign(chunk_rc, chunk_rc + 2 * nchunk);
+
+    Ctx& C = s->C;
+    if (!C.ring_active) {
+        // VarRingsIds of every replica: all active, uids 1..num_rings, ids identity
+        if (dalloc(s, &C.ring_active, s->total_rings) != cudaSuccess || dalloc(s, &C.ring_uid, s->total_rings) != cudaSuccess ||
+            dalloc(s, &C.ring_cms, s->total_rings) != cudaSuccess || dalloc(s, &C.src_ids, s->total_rings) != cudaSuccess ||
+            dalloc(s, &C.src_state, 2 * (int64_t)s->R) != cudaSuccess)
+            return fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for the rings ids");
+        std::vector<int32_t> act(s->total_rings, 1), uid(s->total_rings), ids(s->total_rings), st(2 * s->R);
+        for (int r = 0; r < s->R; r++) {
+            const DevRep& Q = s->reps_h[r];
+            for (int32_t k = 0; k < Q.num_rings; k++) { uid[Q.ring0 + k] = k + 1; ids[Q.ring0 + k] = k; }
+            st[2 * r] = Q.num_rings;
+            st[2 * r + 1] = Q.num_rings;
+        }
+        CUDA_TRY(s, cudaMemcpyAsync(C.ring_active, act.data(), sizeof(int32_t) * act.size(), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.ring_uid, uid.data(), sizeof(int32_t) * uid.size(), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.src_ids, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.src_state, st.data(), sizeof(int32_t) * st.size(), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemsetAsync(C.ring_cms, 0, sizeof(double2) * s->total_rings, s->stream));
+        CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    }
+    {
+        // this replica's mask (ActiveState), uids 1..num_rings and ids
+        // (calc_active_ids!: active rings ascending, the rest of 1:num_rings after)
+        const int32_t nr = R.num_rings;
+        std::vector<int32_t> act(nr), uid(nr), ids(nr), st(2);
+        int32_t na = 0;
+        for (int32_t k = 0; k < nr; k++) {
+            act[k] = active_mask ? (active_mask[k] != 0 ? 1 : 0) : 1;
+            uid[k] = k + 1;
+            ids[k] = k;
+        }
+        for (int32_t k = 0; k < nr; k++) if (act[k]) ids[na++] = k;
+        st[0] = na;
+        st[1] = nr;
+        CUDA_TRY(s, cudaMemcpyAsync(C.ring_active + R.ring0, act.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.ring_uid + R.ring0, uid.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.src_ids + R.ring0, ids.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaMemcpyAsync(C.src_state + 2 * replica, st.data(), sizeof(int32_t) * 2, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    }
+    int rc = upload_sources(s);
+    if (rc) return rc;
+    s->var_rings = true;
+    C.var_rings = 1;
+    drop_graph(s);
+    // chunk lists of the active set (pending histograms were of the old set)
+    s->counts_valid = false;
+    launch_rebin(s, false);
+    CUDA_TRY(s, cudaGetLastError());
+    return check_device_error(s);
+}
+
+int mavi_rings_active(MaviSystem* s, int32_t replica, int32_t* active_mask, int32_t* uids, int32_t* num_active) {
+    if (!s || replica < 0 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    if (!s->is_rings) return fail(s, MAVI_ERR_UNSUPPORTED, "rings ids belong to the rings model");
+    const DevRep& R = s->reps_h[replica];
+    const int32_t nr = R.num_rings;
+    if (!s->C.ring_active) {
+        for (int32_t k = 0; k < nr; k++) {
+            if (active_mask) active_mask[k] = 1;
+            if (uids) uids[k] = k + 1;
+        }
+        if (num_active) *num_active = nr;
+        return MAVI_OK;
+    }
+    int32_t st[2] = {0, 0};
+    if (active_mask)
+        CUDA_TRY(s, cudaMemcpyAsync(active_mask, s->C.ring_active + R.ring0, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, s->stream));
+    if (uids)
+        CUDA_TRY(s, cudaMemcpyAsync(uids, s->C.ring_uid + R.ring0, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(st, s->C.src_state + 2 * replica, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, s->stream));
+    int rc = check_device_error(s);   // waits for the copies
+    if (num_active) *num_active = st[0];
+    return rc;
 }
 
 int mavi_get_stats(MaviSystem* s, MaviStats* st) {

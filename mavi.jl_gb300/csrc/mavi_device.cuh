@@ -28,6 +28,27 @@ __device__ __forceinline__ void raise_error(DevError* e, int32_t code, int64_t s
     }
 }
 
+// A source or sink of the rings model (MaviSourceEntry plus the index of its
+// first spawn box in the handle's box array).
+struct SrcEntryD {
+    int32_t kind, num_boxes, pol_mode, geometry;
+    int32_t box0, _pad;
+    double pol, pad;
+    double length, height, bl_x, bl_y;
+    double radius, cx, cy;
+};
+
+// A spawn box: Source.bbox[i], its chunk list (global chunk indices
+// [chunk0, chunk0 + num_chunks) of the handle's list; num_chunks < 0: every
+// chunk of the replica), its nmax spawn points and, for a random
+// polarisation, its place in the step's noise (-1: fixed polarisation).
+struct SrcBoxD {
+    double bl_x, bl_y, length, height;
+    int32_t num_chunks, chunk0;
+    int64_t spawn0;
+    int64_t noise_idx;
+};
+
 // Per-replica descriptor, built on the host from MaviReplicaParams.
 struct DevRep {
     int64_t a0, na;        // range of this replica's particles in sorted order
@@ -38,6 +59,8 @@ struct DevRep {
     int32_t rows, cols, cap, periodic; // chunk grid; periodic stencil
     int32_t has_chunks;
     int32_t num_rings, nmax;
+    // sources and sinks of the rings model: entries [src_e0, src_e0 + src_ne)
+    int32_t src_e0, src_ne, src_has_sink, _src_pad;
     int32_t min_image;     // first space is PeriodicWalls on a RectangleCfg
     int32_t num_spaces;
     int32_t has_wall_forces;
@@ -79,6 +102,9 @@ struct DevRep {
     double ring_a0sq[MAVI_MAX_TYPES];
     float ring_ks_f[MAVI_MAX_TYPES], ring_ls_f[MAVI_MAX_TYPES], ring_kb_f[MAVI_MAX_TYPES];
     float ring_vo_f[MAVI_MAX_TYPES], ring_mu_f[MAVI_MAX_TYPES];
+    // mixed-form polarisation update: dt / relax_time (FP32) and sqrt(2 D dt)
+    float ring_dt_tau_f[MAVI_MAX_TYPES];
+    double ring_noise_amp[MAVI_MAX_TYPES];
     float dt_f;
     int32_t _pad3;
     double u2_d;           // u^2 in double (areas from integer units^2)
@@ -256,5 +282,30 @@ __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t id, uint
     Rand2 u = philox_uniform2(seed, id, step);
     return sqrt(-2.0 * log(u.a)) * cospi(2.0 * u.b);
 }
+
+// The same Philox counters with the Box-Muller transform in FP32 (24-bit
+// uniforms in (0, 1]): the mixed form's noise, a standard normal to FP32
+// precision without the FP64 logarithm and cosine.
+__device__ __forceinline__ float philox_normal_f(uint64_t seed, uint64_t id, uint64_t step) {
+    U4 c{(uint32_t)id, (uint32_t)(id >> 32), (uint32_t)step, (uint32_t)(step >> 32)};
+    U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const float a = ((float)(r.x >> 8) + 1.0f) * (1.0f / 16777216.0f);
+    const float b = ((float)(r.z >> 8) + 1.0f) * (1.0f / 16777216.0f);
+    return sqrtf(-2.0f * logf(a)) * cospif(2.0f * b);
+}
+
+// float -> double on the integer pipes (the conversion instruction runs on
+// the FP64 pipe, the scarce one on this GPU). Exact for normal floats; zero
+// and subnormal floats give a signed zero, infinities and NaN stay so.
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    const uint32_t sign = b & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    const uint32_t de = (e == 0xffu) ? 0x7ffu : e + 896u;   // rebias 127 -> 1023
+    const uint32_t hi = sign | (de << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
 
 }  // namespace mavi

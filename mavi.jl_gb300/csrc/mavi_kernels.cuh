@@ -76,7 +76,23 @@ struct Ctx {
     double nb_tol;
     int32_t *nb_count, *nb_list;
     double2 *ring_cs;          // (cos, sin) of the ring's polarisation angle
-    double2 *ring_vc;          // mean particle velocity of the ring in the last update
+    double2 *ring_vc;          // summed particle velocity of the ring in the last update
+    // the mixed form keeps both in FP32 (aliases of the same buffers)
+    float2 *ring_csf, *ring_vcf;
+    // variable number of rings (sources and sinks). var_rings: inactive rings'
+    // particles are parked in chunk `park` (after every real chunk), out of
+    // every stencil; the step's histogram is then taken by k_count after
+    // k_sources instead of inside k_rings.
+    int32_t var_rings;
+    int64_t park;
+    int32_t *ring_active, *ring_uid;   // per ring: VarRingsIds.mask, .uids
+    double2 *ring_cms;                 // per ring: RingsInfo.cms
+    int32_t *src_ids;                  // per ring slot: VarRingsIds.ids (replica-local, 0-based)
+    int32_t *src_state;                // per replica: num_active, max uid
+    const SrcEntryD *src_entries;
+    const SrcBoxD *src_boxes;
+    const double2 *src_spawn;
+    const int32_t *src_chunks;
     // descriptors
     const DevRep *reps;
     const MaviSpace *spaces;     // [replica][MAVI_MAX_SPACES]
@@ -261,10 +277,19 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
     int32_t cap = 1 << 30;
     if (valid) {
         const DevRep& R = C.reps[C.num_reps > 1 ? C.rep_out[s] : 0];
-        double2 p = C.pos_out[s];
-        const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
-        cell = bin_final<PREC>(C, R, s, p.x, p.y, guess);
-        cap = R.has_chunks ? R.cap : (1 << 30);
+        bool parked = false;
+        if (C.var_rings) {   // particles of inactive rings take no chunk (update_ids!)
+            const int32_t ring = (C.uid_out[s] - (int32_t)R.slot0) / R.nmax;
+            parked = C.ring_active[R.ring0 + ring] == 0;
+        }
+        if (parked) {
+            cell = C.park;
+        } else {
+            double2 p = C.pos_out[s];
+            const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
+            cell = bin_final<PREC>(C, R, s, p.x, p.y, (guess == C.park && C.var_rings) ? -1 : guess);
+            cap = R.has_chunks ? R.cap : (1 << 30);
+        }
     }
     count_into_chunk(C, valid, s, cell, cap);
 }
@@ -1350,6 +1375,18 @@ k_pass(Ctx C, int32_t with_wall_forces) {
     int32_t rep = (valid && C.num_reps > 1) ? C.rep_cur[s] : 0;
     const DevRep& R = C.reps[rep];
     int32_t cell = valid ? C.cell_cur[s] : 0;
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        // particles of inactive rings (parked after every real chunk): zero
+        // force (clean_forces!), no neighbours, no pair terms
+        if (valid && C.var_rings && cell == C.park) {
+            if constexpr (PASS == kPassForce) {
+                if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(0.0, 0.0);
+                else C.ff[s] = make_float2(0.f, 0.f);
+                if (C.nb_mode) C.nb_count[C.uid_cur[s]] = 0;
+            }
+            valid = false;
+        }
+    }
     const double2* P = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
     // own FP64 position, loaded early so its latency overlaps the gather
     const double2 p = valid ? P[s] : make_double2(0.0, 0.0);
@@ -1361,13 +1398,17 @@ k_pass(Ctx C, int32_t with_wall_forces) {
                                stage[threadIdx.x >> 5], acc);
     }
     if (valid) {
-        double fx = (double)acc.gx(), fy = (double)acc.gy();
+        // FP32 sums widen on the integer pipes (f32_to_f64_bits), not the FP64 one
+        double fx, fy;
+        if constexpr (PREC == kPrecFP64) { fx = acc.gx(); fy = acc.gy(); }
+        else { fx = f32_to_f64_bits(acc.gx()); fy = f32_to_f64_bits(acc.gy()); }
         bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
         if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
         const double dt = R.dt;
         if constexpr (PASS == kPassForce) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
-            else C.ff[s] = make_float2((float)fx, (float)fy);
+            else if (walls_f) C.ff[s] = make_float2((float)fx, (float)fy);
+            else C.ff[s] = make_float2(acc.gx(), acc.gy());
             if constexpr (DYN == MAVI_DYN_RINGS) {
                 if (C.nb_mode) C.nb_count[C.uid_cur[s]] = acc.nb;
             }
@@ -1403,8 +1444,8 @@ k_pass(Ctx C, int32_t with_wall_forces) {
                     y = __dadd_rn(y, __dmul_rn(fy, R.mdt));
                 } else {
                     // FP32 displacement (relative error 6e-8 of a step), FP64 position
-                    x = __dadd_rn(x, (double)(acc.gx() * R.mdt_f));
-                    y = __dadd_rn(y, (double)(acc.gy() * R.mdt_f));
+                    x = __dadd_rn(x, f32_to_f64_bits(acc.gx() * R.mdt_f));
+                    y = __dadd_rn(y, f32_to_f64_bits(acc.gy() * R.mdt_f));
                 }
             } else if constexpr (PASS == kPassSzabo || PASS == kPassRTP) {
                 int32_t uid = C.uid_cur[s];
@@ -1477,7 +1518,10 @@ __device__ __forceinline__ void ring_vc_store(const Ctx& C, int64_t g, int lane,
         vcx += __shfl_xor_sync(0xffffffffu, vcx, o);
         vcy += __shfl_xor_sync(0xffffffffu, vcy, o);
     }
-    if (lane == 0) C.ring_vc[g] = make_double2((double)vcx, (double)vcy);
+    if (lane == 0) {
+        if constexpr (std::is_same<V, double>::value) C.ring_vc[g] = make_double2(vcx, vcy);
+        else C.ring_vcf[g] = make_float2(vcx, vcy);
+    }
 }
 
 #ifndef MAVI_RINGS_MIN_BLOCKS
@@ -1497,6 +1541,21 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     const int32_t rl = (int32_t)(g - R.ring0);
     const int t = C.ring_types[g] - 1;
     const int32_t n = rc.num_particles[t];
+    if (C.var_rings && C.ring_active[g] == 0) {
+        // inactive ring: positions carried over unchanged, no forces
+        if (do_update) {
+            for (int p = lane; p < n; p += 32) {
+                const int32_t s = C.slot_of[(int32_t)R.slot0 + rl * R.nmax + p];
+                C.pos_out[s] = C.pos_cur[s];
+                C.uid_out[s] = C.uid_cur[s];
+                C.rep_out[s] = rep;
+            }
+        }
+        return;
+    }
+    // with sources and sinks the active set changes before the next chunk
+    // update, so the histogram is taken afterwards (k_count)
+    const bool fused_count = !C.var_rings;
     double2* P = sp_[w];
     int32_t* S = ss_[w];
     for (int p = lane; p < n; p += 32) {
@@ -1513,18 +1572,16 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     };
     // overdamped active update parameters; (cos, sin) of the polarisation
     // come from k_ring_pol (one thread per ring, not one warp)
-    double pc = 0.0, ps = 0.0;
-    if (do_update) {
-        const double2 cs = C.ring_cs[g];
-        pc = cs.x;
-        ps = cs.y;
-    }
-    const double vo = rc.vo[t], mu = rc.mobility[t], dt = R.dt;
     // the mixed form sums the ring's velocity and forms the position
     // increment in FP32 (FP64 only for x += increment); FP64 form: all double
     using V = typename std::conditional<PREC == kPrecFP64, double, float>::type;
+    V pc = 0, ps = 0;
+    if (do_update) {
+        if constexpr (PREC == kPrecFP64) { const double2 cs = C.ring_cs[g]; pc = cs.x; ps = cs.y; }
+        else { const float2 cs = C.ring_csf[g]; pc = cs.x; ps = cs.y; }
+    }
+    const double vo = rc.vo[t], mu = rc.mobility[t], dt = R.dt;
     V vcx = 0, vcy = 0;
-    const V pcv = (V)pc, psv = (V)ps;
     // pair + wall forces, then the overdamped active update of particle p
     // returns the chunk of the updated position (binning fused here: the
     // histogram of the next step is taken in this kernel)
@@ -1552,17 +1609,20 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             x = __dadd_rn(xc.x, __dmul_rn(vx, dt));
             y = __dadd_rn(xc.y, __dmul_rn(vy, dt));
         } else {
-            const float vx = fmaf(R.ring_vo_f[t], pcv, R.ring_mu_f[t] * fx);
-            const float vy = fmaf(R.ring_vo_f[t], psv, R.ring_mu_f[t] * fy);
+            const float vx = fmaf(R.ring_vo_f[t], pc, R.ring_mu_f[t] * fx);
+            const float vy = fmaf(R.ring_vo_f[t], ps, R.ring_mu_f[t] * fy);
             vcx += vx; vcy += vy;
-            x = __dadd_rn(xc.x, (double)(vx * R.dt_f));
-            y = __dadd_rn(xc.y, (double)(vy * R.dt_f));
+            x = __dadd_rn(xc.x, f32_to_f64_bits(vx * R.dt_f));
+            y = __dadd_rn(xc.y, f32_to_f64_bits(vy * R.dt_f));
         }
         double dvx = 0, dvy = 0;
-        apply_walls(C, rep, R, rc.inter_dist_eq[t][t] * 0.5, x, y, dvx, dvy, false);
-        const int32_t cur = C.cell_cur[s];
-        int64_t nc = bin_fast<PREC>(C, R, s, x, y, cur);
-        if (nc < 0) nc = bin_final<PREC>(C, R, s, x, y, cur);
+        if (R.has_walls) apply_walls(C, rep, R, rc.inter_dist_eq[t][t] * 0.5, x, y, dvx, dvy, false);
+        int64_t nc = 0;
+        if (fused_count) {
+            const int32_t cur = C.cell_cur[s];
+            nc = bin_fast<PREC>(C, R, s, x, y, cur);
+            if (nc < 0) nc = bin_final<PREC>(C, R, s, x, y, cur);
+        }
         C.pos_out[s] = make_double2(x, y);
         C.uid_out[s] = C.uid_cur[s];
         C.rep_out[s] = rep;
@@ -1654,7 +1714,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             }
             int64_t nc = 0;
             if (act) nc = finish(p, P[p], fx, fy, near_wall);
-            if (do_update) count_into_chunk(C, act, S[p], nc, cap);
+            if (do_update && fused_count) count_into_chunk(C, act, S[p], nc, cap);
             ring_vc_store(C, g, lane, do_update, vcx, vcy);
             return;
         }
@@ -1744,7 +1804,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         }
         int64_t nc = 0;
         if (act) nc = finish(p, xc, (V)fx, (V)fy);
-        if (do_update) count_into_chunk(C, act, S[p], nc, cap);
+        if (do_update && fused_count) count_into_chunk(C, act, S[p], nc, cap);
     } else {
         for (int base = 0; base < n; base += 32) {
             const int p = base + lane;
@@ -1793,7 +1853,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             }
             nc = finish(p, xc, (V)fx, (V)fy);
             }
-            if (do_update) count_into_chunk(C, act, act ? S[p] : 0, nc, cap);
+            if (do_update && fused_count) count_into_chunk(C, act, act ? S[p] : 0, nc, cap);
         }
     }
     ring_vc_store(C, g, lane, do_update, vcx, vcy);
@@ -1805,36 +1865,277 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
 // Polarisation of each ring (src/rings/integration.jl:340-351), one thread
 // per ring: theta += asin(p x v_mean / |v_mean|) / tau dt + sqrt(2 D dt) xi,
 // then (cos, sin) of the new angle for the next step. With update == 0 it
-// only refreshes (cos, sin) (after an upload).
-static __global__ void k_ring_pol(Ctx C, int64_t total_rings, int32_t update) {
+// only refreshes (cos, sin) (after an upload). The mixed form takes the
+// deterministic increment and (cos, sin) in FP32 (the angle, reduced to
+// [-pi, pi] in FP64, stays an FP64 sum); the FP64 transcendental functions
+// dominate this kernel otherwise.
+template <int PREC>
+__global__ void k_ring_pol(Ctx C, int64_t total_rings, int32_t update) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total_rings) return;
+    if (update && C.var_rings && C.ring_active[g] == 0) return;   // update! runs over active rings
     double theta = C.ring_pol[g];
     if (update) {
         const int32_t rep = C.ring_rep[g];
         const DevRep& R = C.reps[rep];
         const MaviRingsCfg& rc = C.rcfg[rep];
         const int t = C.ring_types[g] - 1;
-        const double2 vs = C.ring_vc[g], cs = C.ring_cs[g];
         const int32_t n = rc.num_particles[t];
-        const double2 vc = make_double2(vs.x / n, vs.y / n);
-        const double dt = R.dt;
-        const double speed = sqrt(vc.x * vc.x + vc.y * vc.y);
-        double cr = 0.0;
-        if (speed != 0) {
-            cr = (cs.x * vc.y - cs.y * vc.x) / speed;
-            if (fabs(cr) > 1) cr = jsign(cr);
+        if constexpr (PREC == kPrecFP64) {
+            const double2 vs = C.ring_vc[g], cs = C.ring_cs[g];
+            const double2 vc = make_double2(vs.x / n, vs.y / n);
+            const double dt = R.dt;
+            const double speed = sqrt(vc.x * vc.x + vc.y * vc.y);
+            double cr = 0.0;
+            if (speed != 0) {
+                cr = (cs.x * vc.y - cs.y * vc.x) / speed;
+                if (fabs(cr) > 1) cr = jsign(cr);
+            }
+            double nz;
+            if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (g - R.ring0)];
+            else nz = philox_normal(C.seed, (uint64_t)g, (uint64_t)(C.d_step[0] - 1));
+            const double d_theta = 1 / rc.relax_time[t] * asin(cr) * dt + sqrt(2 * rc.rot_diff[t] * dt) * nz;
+            theta = theta + d_theta;
+        } else {
+            const float2 vs = C.ring_vcf[g], cs = C.ring_csf[g];
+            const float inv_n = 1.0f / (float)n;
+            const float vx = vs.x * inv_n, vy = vs.y * inv_n;
+            const float speed = sqrtf(vx * vx + vy * vy);
+            float cr = 0.0f;
+            if (speed != 0.0f) {
+                cr = (cs.x * vy - cs.y * vx) / speed;
+                if (fabsf(cr) > 1.0f) cr = copysignf(1.0f, cr);
+            }
+            double nz;
+            if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (g - R.ring0)];
+            else nz = f32_to_f64_bits(philox_normal_f(C.seed, (uint64_t)g, (uint64_t)(C.d_step[0] - 1)));
+            const double det = f32_to_f64_bits(asinf(cr) * R.ring_dt_tau_f[t]);
+            theta = fma(R.ring_noise_amp[t], nz, theta + det);
         }
-        double nz;
-        if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (g - R.ring0)];
-        else nz = philox_normal(C.seed, (uint64_t)g, (uint64_t)(C.d_step[0] - 1));
-        const double d_theta = 1 / rc.relax_time[t] * asin(cr) * dt + sqrt(2 * rc.rot_diff[t] * dt) * nz;
-        theta = theta + d_theta;
         C.ring_pol[g] = theta;
     }
-    double sn, cn;
-    sincos(theta, &sn, &cn);
-    C.ring_cs[g] = make_double2(cn, sn);
+    if constexpr (PREC == kPrecFP64) {
+        double sn, cn;
+        sincos(theta, &sn, &cn);
+        C.ring_cs[g] = make_double2(cn, sn);
+    } else {
+        const double q = rint(theta * 0.15915494309189535);   // 1 / (2 pi)
+        const float r = (float)fma(-q, 6.283185307179586, theta);
+        float sn, cn;
+        sincosf(r, &sn, &cn);
+        C.ring_csf[g] = make_float2(cn, sn);
+    }
+}
+
+// ===========================================================================
+// Sources and sinks of the rings model: the head of step!
+// (src/rings/integration.jl:522-526) for every replica that has some, one
+// block per replica. It runs before the step's chunk update, so the chunk
+// lists it reads (start[], the slots in *_cur order) are the previous
+// update_chunks!'s, as the reference's ChunksChecker reads them; the current
+// positions are in pos_out (same slot order), the previous step's in pos_cur.
+// ===========================================================================
+constexpr int kSrcThreads = 256;
+
+// is_inside(point, ::RectangleCfg; pad) (src/configs.jl:89-93)
+__device__ __forceinline__ bool inside_rect(double x, double y, double blx, double bly, double len, double h,
+                                            double pad) {
+    const bool ix = (blx - pad <= x) && (x <= blx + len + pad);
+    const bool iy = (bly - pad <= y) && (y <= bly + h + pad);
+    return ix && iy;
+}
+
+// is_inside(point, sink geometry) with pad 0 (src/configs.jl:89-93, 165-168)
+__device__ __forceinline__ bool sink_inside(const SrcEntryD& E, double2 c) {
+    if (E.geometry == MAVI_GEOM_CIRCLE) {
+        const double dx = c.x - E.cx, dy = c.y - E.cy;
+        const double rp = E.radius + 0.0;
+        return dx * dx + dy * dy <= rp * rp;
+    }
+    return inside_rect(c.x, c.y, E.bl_x, E.bl_y, E.length, E.height, 0.0);
+}
+
+// update_cms! (src/rings/integration.jl:366-372) for one ring: the mean of the
+// ring's positions, or with periodic walls of its continuous positions, which
+// update_continuos_pos! (:118-138) formed from the previous step's positions.
+// Summed in particle order.
+__device__ __forceinline__ double2 ring_centre(const Ctx& C, const DevRep& R, int32_t ring, int32_t n) {
+    const int32_t u0 = (int32_t)R.slot0 + ring * R.nmax;
+    double sx, sy;
+    if (R.periodic) {
+        double2 prev = C.pos_cur[C.slot_of[u0]];
+        double cx = prev.x, cy = prev.y;
+        sx = cx; sy = cy;
+        for (int32_t p = 1; p < n; p++) {
+            const double2 q = C.pos_cur[C.slot_of[u0 + p]];
+            double dx = q.x - prev.x, dy = q.y - prev.y;
+            if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
+            cx = cx + dx; cy = cy + dy;
+            sx += cx; sy += cy;
+            prev = q;
+        }
+    } else {
+        const double2 q0 = C.pos_out[C.slot_of[u0]];
+        sx = q0.x; sy = q0.y;
+        for (int32_t p = 1; p < n; p++) {
+            const double2 q = C.pos_out[C.slot_of[u0 + p]];
+            sx += q.x; sy += q.y;
+        }
+    }
+    return make_double2(sx / n, sy / n);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kSrcThreads) k_sources(Ctx C) {
+    const int32_t rep = (int32_t)blockIdx.x;
+    const DevRep& R = C.reps[rep];
+    if (R.src_ne == 0) return;
+    __shared__ int32_t sh_num_active, sh_max_uid, sh_first, sh_hits;
+    __shared__ int32_t sh_flag[MAVI_MAX_SPAWN_BOXES];
+    __shared__ int smem[32];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int32_t nr = R.num_rings;
+    const MaviRingsCfg& rc = C.rcfg[rep];
+    int32_t* ids = C.src_ids + R.ring0;
+    int32_t* act = C.ring_active + R.ring0;
+    if (tid == 0) {
+        sh_num_active = C.src_state[2 * rep];
+        sh_max_uid = C.src_state[2 * rep + 1];
+        sh_hits = 0;
+    }
+    __syncthreads();
+    if (R.src_has_sink) {
+        const int32_t na = sh_num_active;
+        for (int32_t k = tid; k < na; k += nthr) {
+            const int32_t ring = ids[k];
+            const int32_t n = rc.num_particles[C.ring_types[R.ring0 + ring] - 1];
+            C.ring_cms[R.ring0 + ring] = ring_centre(C, R, ring, n);
+        }
+    }
+    __syncthreads();
+    for (int32_t e = 0; e < R.src_ne; e++) {
+        const SrcEntryD& E = C.src_entries[R.src_e0 + e];
+        if (E.kind == MAVI_SRC_SINK) {
+            // process_sink! (src/rings/sources.jl:253-260) over the view
+            // ids[1:num_active] taken when the loop starts; every hit
+            // decrements num_active (remove_ring!, src/rings/states.jl:176-180)
+            const int32_t L = sh_num_active;
+            int hits = 0;
+            for (int32_t k = tid; k < L; k += nthr) {
+                const int32_t ring = ids[k];
+                if (sink_inside(E, C.ring_cms[R.ring0 + ring])) { act[ring] = 0; hits++; }
+            }
+            if (hits) atomicAdd(&sh_hits, hits);
+            __syncthreads();
+            if (tid == 0) { sh_num_active -= sh_hits; sh_hits = 0; }
+            __syncthreads();
+            continue;
+        }
+        // process_source! (src/rings/sources.jl:226-239): which boxes are empty
+        // (update_area_empty!, :193-224), all before any ring is added
+        const int32_t nb = E.num_boxes;
+        for (int32_t b = tid; b < nb; b += nthr) sh_flag[b] = 0;
+        __syncthreads();
+        for (int32_t b = 0; b < nb; b++) {
+            const SrcBoxD& B = C.src_boxes[E.box0 + b];
+            bool occ = false;
+            if (B.num_chunks < 0) {
+                // PosChecker: the active particles of the last update_ids!
+                const int32_t lo = C.start[R.c0], hi = C.start[R.c0 + (int64_t)R.rows * R.cols];
+                for (int32_t q = lo + tid; q < hi && !occ; q += nthr) {
+                    const double2 x = C.pos_out[q];
+                    occ = inside_rect(x.x, x.y, B.bl_x, B.bl_y, B.length, B.height, E.pad);
+                }
+            } else {
+                for (int32_t k = tid; k < B.num_chunks && !occ; k += nthr) {
+                    const int32_t c = C.src_chunks[B.chunk0 + k];
+                    for (int32_t q = C.start[c]; q < C.start[c + 1] && !occ; q++) {
+                        const double2 x = C.pos_out[q];
+                        occ = inside_rect(x.x, x.y, B.bl_x, B.bl_y, B.length, B.height, E.pad);
+                    }
+                }
+            }
+            if (occ) sh_flag[b] = 1;
+        }
+        __syncthreads();
+        for (int32_t b = 0; b < nb; b++) {
+            if (sh_flag[b]) continue;   // block-uniform
+            const SrcBoxD& B = C.src_boxes[E.box0 + b];
+            // add_ring! (src/rings/states.jl:162-174): the first inactive slot
+            if (tid == 0) sh_first = 0x7fffffff;
+            __syncthreads();
+            for (int32_t k = tid; k < nr; k += nthr)
+                if (act[k] == 0) { atomicMin(&sh_first, k); break; }
+            __syncthreads();
+            const int32_t ring = sh_first;
+            if (ring == 0x7fffffff) continue;   // no free slot: nothing added (block-uniform)
+            const int64_t g = R.ring0 + ring;
+            const int32_t n = rc.num_particles[C.ring_types[g] - 1];
+            for (int32_t p = tid; p < n; p += nthr)
+                C.pos_out[C.slot_of[(int32_t)R.slot0 + ring * R.nmax + p]] = C.src_spawn[B.spawn0 + p];
+            if (tid == 0) {
+                act[ring] = 1;
+                sh_max_uid += 1;
+                C.ring_uid[g] = sh_max_uid;
+                sh_num_active += 1;
+                double pol = E.pol;
+                if (E.pol_mode == MAVI_SPAWN_POL_RANDOM) {
+                    // get_spawn_pol (src/rings/sources.jl:23-24): rand() * 2 * pi
+                    double u;
+                    if (C.noise_mode == MAVI_NOISE_INJECTED) u = C.noise[B.noise_idx];
+                    else u = philox_uniform2(C.seed, (uint64_t)B.noise_idx + (1ull << 40), (uint64_t)C.d_step[0]).a - 0x1p-53;
+                    pol = u * 2.0 * 3.141592653589793;
+                }
+                C.ring_pol[g] = pol;
+                if constexpr (PREC == kPrecFP64) {
+                    double sn, cn;
+                    sincos(pol, &sn, &cn);
+                    C.ring_cs[g] = make_double2(cn, sn);
+                } else {
+                    const double q = rint(pol * 0.15915494309189535);
+                    const float r = (float)fma(-q, 6.283185307179586, pol);
+                    float sn, cn;
+                    sincosf(r, &sn, &cn);
+                    C.ring_csf[g] = make_float2(cn, sn);
+                }
+                // process_source! sets the new ring's centre: sum(rings_pos[1:n]) / n
+                double2 q0 = C.src_spawn[B.spawn0];
+                double sx = q0.x, sy = q0.y;
+                for (int32_t p = 1; p < n; p++) { const double2 q = C.src_spawn[B.spawn0 + p]; sx += q.x; sy += q.y; }
+                C.ring_cms[g] = make_double2(sx / n, sy / n);
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    // update_ids! (calc_active_ids!, src/rings/states.jl:200-219): active rings
+    // in ascending order; entries past the new count keep their old values
+    int32_t base = 0;
+    for (int32_t k0 = 0; k0 < nr; k0 += nthr) {
+        const int32_t k = k0 + tid;
+        const int a = (k < nr && act[k] != 0) ? 1 : 0;
+        int total;
+        const int ex = block_exclusive_scan(a, smem, total);
+        if (a) ids[base + ex] = k;
+        base += total;
+    }
+    if (tid == 0) {
+        C.src_state[2 * rep] = base;
+        C.src_state[2 * rep + 1] = sh_max_uid;
+    }
+}
+
+// *_out := *_cur (rings with sources and sinks, after a chunk update outside
+// the step): between steps their current state lives in *_out in the slot
+// order of *_cur, where k_sources reads it.
+static __global__ void k_out_from_cur(Ctx C) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C.M) return;
+    C.pos_out[s] = C.pos_cur[s];
+    C.uid_out[s] = C.uid_cur[s];
+    C.rep_out[s] = C.rep_cur[s];
+    C.cell_out[s] = C.cell_cur[s];
+    if (C.off_out) C.off_out[s] = C.off_cur[s];
 }
 
 static __global__ void k_gather_user(Ctx C, const double2* __restrict__ pos_user, const double2* __restrict__ vel_user,

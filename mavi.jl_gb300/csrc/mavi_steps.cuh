@@ -33,7 +33,7 @@ template <int PREC>
 void rings_terms(MaviSystem* s, int do_update) {
     unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
     k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update);
-    if (do_update) k_ring_pol<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
+    if (do_update) k_ring_pol<PREC><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
 }
 
 // The passes of one step after the chunk rebuild.
@@ -106,6 +106,14 @@ void forces_only(MaviSystem* s, int with_walls) {
     }
 }
 
+// Head of the rings step with sources and sinks: k_sources, then the
+// histogram of the (changed) active set for the step's chunk update.
+template <int PREC>
+void sources(MaviSystem* s) {
+    k_sources<PREC><<<(unsigned)s->R, kSrcThreads, 0, s->stream>>>(s->C);
+    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, 1);
+}
+
 template <int PREC>
 void forces_to_user(MaviSystem* s) {
     k_forces_to_user<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->f_user);
@@ -122,4 +130,5 @@ void forces_to_user(MaviSystem* s) {
     void forces_only_##SUFFIX(MaviSystem* s, int w) { steps::forces_only<PREC>(s, w); }      \
     void rings_terms_##SUFFIX(MaviSystem* s, int u) { steps::rings_terms<PREC>(s, u); }      \
     void forces_to_user_##SUFFIX(MaviSystem* s) { steps::forces_to_user<PREC>(s); }          \
+    void sources_##SUFFIX(MaviSystem* s) { steps::sources<PREC>(s); }                        \
     }

@@ -62,6 +62,19 @@ struct MaviSystem {
     int32_t max_chunk_count = 0;
     int64_t last_pairs = -1;
     std::string last_error;
+    // chunks the scan covers: Ctot, plus the parking chunk of rings handles
+    int64_t nscan = 0;
+    int64_t noise_base = 0;        // noise numbers per step without the spawn uniforms
+    // sources and sinks (rings): per replica, as passed to mavi_rings_sources
+    bool var_rings = false;
+    struct SrcCfg {
+        std::vector<MaviSourceEntry> entries;
+        std::vector<MaviSpawnBox> boxes;
+        std::vector<double> spawn_xy;
+        std::vector<int32_t> chunk_rc;
+    };
+    std::vector<SrcCfg> src_cfg;
+    void* src_buf[4] = {nullptr, nullptr, nullptr, nullptr};   // entries, boxes, spawn, chunks
 };
 
 namespace mavi {
@@ -158,5 +171,7 @@ void rings_terms_fp64(MaviSystem* s, int do_update);
 void rings_terms_mixed(MaviSystem* s, int do_update);
 void forces_to_user_fp64(MaviSystem* s);
 void forces_to_user_mixed(MaviSystem* s);
+void sources_fp64(MaviSystem* s);
+void sources_mixed(MaviSystem* s);
 
 }  // namespace mavi

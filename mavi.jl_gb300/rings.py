@@ -12,7 +12,7 @@ from typing import Any, Sequence
 import numpy as np
 
 from . import abi
-from .configs import HarmTruncCfg, IntCfg, ChunksCfg, CUDADevice, chunk_capacity
+from .configs import HarmTruncCfg, IntCfg, ChunksCfg, CUDADevice, CircleCfg, RectangleCfg, chunk_capacity
 from .system import System, TimeInfo
 
 
@@ -132,7 +132,7 @@ class RingsState:
     view sharing memory with it. ``types`` are 1-based per ring (or None)."""
     kind = abi.MAVI_STATE_RINGS
 
-    def __init__(self, rings_pos, pol, num_particles=None, types=None):
+    def __init__(self, rings_pos, pol, num_particles=None, types=None, active_state=None):
         rp = np.ascontiguousarray(np.asarray(rings_pos, dtype=np.float64))
         if rp.ndim != 3 or rp.shape[2] != 2:
             raise ValueError("rings_pos must have shape (num_rings, nmax, 2)")
@@ -145,6 +145,7 @@ class RingsState:
         self.num_particles = self.nmax if num_particles is None else num_particles
         self.types = None if types is None else np.ascontiguousarray(np.asarray(types, dtype=np.int32))
         self.vel = None
+        self.active_state = active_state
 
     def types_array(self):
         return self.types if self.types is not None else np.ones(self.num_rings, dtype=np.int32)
@@ -169,6 +170,128 @@ class NeighborsCfg:
     tol: float = 1.1
 
 
+# ---------------------------------------------------------------------------
+# variable number of rings: ActiveState, sources and sinks
+# (src/states.jl:14-20, src/rings/states.jl:20-40, src/rings/sources.jl)
+# ---------------------------------------------------------------------------
+class ActiveState:
+    """ActiveState(mask) (src/states.jl:14-20): which rings are active at the
+    start; a bool applies to every ring."""
+
+    def __init__(self, mask=True):
+        self.mask = mask
+
+    def get_active_mask(self, num_rings: int) -> np.ndarray:
+        if isinstance(self.mask, (bool, np.bool_)):
+            return np.full(num_rings, bool(self.mask))
+        m = np.asarray(self.mask, dtype=bool).reshape(-1)
+        if m.size != num_rings:
+            raise ValueError("the active mask needs one entry per ring")
+        return m
+
+
+@dataclass
+class SourceCfg:
+    """SourceCfg (src/rings/sources.jl:27-48): a ring spawn template
+    (``spawn_pos``, nmax points) repeated on a size[0] x size[1] grid of boxes
+    from ``bottom_left``; a ring is added to every box that holds no particle
+    (within ``pad``). ``spawn_pol`` is an angle or "random"."""
+    bottom_left: tuple
+    spawn_pos: object
+    spawn_pol: object = 0.0
+    pad: float = 0.0
+    offset: tuple = (0.0, 0.0)
+    size: tuple = (1, 1)
+
+
+@dataclass
+class SinkCfg:
+    """SinkCfg (src/rings/sources.jl:241-244): rings whose centre of mass lies
+    in ``geometry_cfg`` (RectangleCfg or CircleCfg) are removed."""
+    geometry_cfg: object
+
+
+def _rect_union(a, b):
+    """RectangleCfg + RectangleCfg (src/configs.jl:68-77): (bl_x, bl_y, length, height)."""
+    max_x = max(a[0] + a[2], b[0] + b[2])
+    max_y = max(a[1] + a[3], b[1] + b[3])
+    min_x = min(a[0], b[0])
+    min_y = min(a[1], b[1])
+    return (min_x, min_y, max_x - min_x, max_y - min_y)
+
+
+def _intersects(r1, r2):
+    """check_intersection(r1, r2) of two rectangles (src/configs.jl:79-87),
+    (bl_x, bl_y, length, height) each."""
+    x1 = r2[0] <= r1[0] <= r2[0] + r2[2]
+    x2 = r2[0] <= r1[0] + r1[2] <= r2[0] + r2[2]
+    y1 = r2[1] <= r1[1] <= r2[1] + r2[3]
+    y2 = r2[1] <= r1[1] + r1[3] <= r2[1] + r2[3]
+    return (x1 or x2) and (y1 or y2)
+
+
+def source_boxes(cfg: SourceCfg, chunk_grid=None):
+    """The fields of Source(cfg, ...) (src/rings/sources.jl:122-185), in FP64
+    with the reference's operation order: the spawn boxes (bl_x, bl_y, length,
+    height), their spawn points and, with a chunk grid (bl_x, bl_y, length,
+    height, rows, cols), the ChunksChecker's chunk lists ((row, col), 0-based);
+    without one, None (PosChecker)."""
+    sp = np.asarray(cfg.spawn_pos, dtype=np.float64).reshape(-1, 2)
+    pad = float(cfg.pad)
+    min_x, max_x = float(sp[:, 0].min()), float(sp[:, 0].max())
+    min_y, max_y = float(sp[:, 1].min()), float(sp[:, 1].max())
+    bbox_length = max_x - min_x + 2 * pad
+    bbox_height = max_y - min_y + 2 * pad
+    blx, bly = float(cfg.bottom_left[0]), float(cfg.bottom_left[1])
+    ox, oy = float(cfg.offset[0]), float(cfg.offset[1])
+    boxes, pads = [], []
+    for i in range(1, int(cfg.size[0]) + 1):
+        for j in range(1, int(cfg.size[1]) + 1):
+            bx = blx + ((i - 1) * bbox_length + i * ox)
+            by = bly + ((j - 1) * bbox_height + j * oy)
+            boxes.append((bx, by, bbox_length, bbox_height))
+            pads.append((bx - pad, by - pad, bbox_length + 2 * pad, bbox_height + 2 * pad))
+    spawns = []
+    for b in boxes:
+        dx = b[0] - min_x + pad
+        dy = b[1] - min_y + pad
+        spawns.append(np.stack([sp[:, 0] + dx, sp[:, 1] + dy], axis=1))
+    if chunk_grid is None:
+        return boxes, spawns, None
+    gblx, gbly, glen, ghei, rows, cols = chunk_grid
+    cl, ch = glen / cols, ghei / rows
+    glob = pads[0]
+    for r in pads[1:]:
+        glob = _rect_union(glob, r)
+    tlx, tly = gblx + 0.0, gbly + ghei
+    found, sx, ex = False, 0, 0
+    for i in range(1, cols + 1):
+        x1 = tlx + (i - 1) * cl
+        x2 = x1 + cl
+        if not found and x1 <= glob[0] <= x2:
+            found, sx = True, i
+        if found and x1 >= glob[0] + glob[2]:
+            ex = i - 1
+            break
+    found, sy, ey = False, 0, 0
+    for i in range(1, rows + 1):
+        y2 = tly - (i - 1) * ch
+        y1 = y2 - ch
+        if not found and y1 <= glob[1] + glob[3] <= y2:
+            found, sy = True, i
+        if found and y2 <= glob[1]:
+            ey = i - 1
+            break
+    lists = [[] for _ in pads]
+    for col in range(sx, ex + 1):
+        for row in range(sy, ey + 1):
+            rect = (tlx + (col - 1) * cl, tly - row * ch, cl, ch)   # get_chunk_rect (src/chunks.jl:50-59)
+            for k, bp in enumerate(pads):
+                if _intersects(rect, bp):
+                    lists[k].append((row - 1, col - 1))
+    return boxes, spawns, lists
+
+
 class RingsSystem(System):
     """RingsSystem (src/rings/rings.jl:231-291) on the GPU. With
     ``p_neighbors_cfg`` every pair pass also records the particle neighbour
@@ -176,11 +299,102 @@ class RingsSystem(System):
     is_rings = True
 
     def __init__(self, state: RingsState, space_cfg, dynamic_cfg: RingsCfg, int_cfg: IntCfg,
-                 time_info: TimeInfo | None = None, p_neighbors_cfg: NeighborsCfg | None = None):
+                 time_info: TimeInfo | None = None, p_neighbors_cfg: NeighborsCfg | None = None,
+                 source_cfg=None):
         super().__init__(state, space_cfg, dynamic_cfg, int_cfg, time_info)
         if dynamic_cfg.num_types > 1 and state.types is None:
             raise ValueError("DynamicCfg has multiple types, but state.types is nothing!")
         self.p_neighbors_cfg = p_neighbors_cfg
+        if source_cfg is not None and not isinstance(source_cfg, (list, tuple)):
+            source_cfg = [source_cfg]
+        self.source_cfg = None if source_cfg is None else list(source_cfg)
+        for c in self.source_cfg or []:
+            if not isinstance(c, (SourceCfg, SinkCfg)):
+                raise ValueError(f"Unknown source configuration type: {type(c).__name__}")
+            if isinstance(c, SourceCfg) and np.asarray(c.spawn_pos).reshape(-1, 2).shape[0] != state.nmax:
+                raise ValueError("spawn_pos needs one point per row of rings_pos (nmax)")
+
+    @property
+    def variable_rings(self) -> bool:
+        """VarRingsIds: an ActiveState was given or sources/sinks are configured."""
+        return self.source_cfg is not None or getattr(self.state, "active_state", None) is not None
+
+    def sources_abi(self):
+        """(active_mask, entries, boxes, spawn_xy, chunk_rc) for
+        mavi_rings_sources, or None without variable rings."""
+        if not self.variable_rings:
+            return None
+        st = self.state
+        a = getattr(st, "active_state", None)
+        mask = (a.get_active_mask(st.num_rings) if a is not None else np.ones(st.num_rings, bool)).astype(np.int32)
+        grid = None
+        cc = self.int_cfg.chunks_cfg
+        if cc is not None:
+            bb = self.space_cfg.bounding_box()
+            grid = (float(bb.bottom_left[0]), float(bb.bottom_left[1]), float(bb.length), float(bb.height),
+                    int(cc.num_rows), int(cc.num_cols))
+        cfgs = self.source_cfg or []
+        entries = (abi.MaviSourceEntry * max(len(cfgs), 1))()
+        boxes, spawn, chunks = [], [], []
+        for k, c in enumerate(cfgs):
+            e = entries[k]
+            if isinstance(c, SinkCfg):
+                e.kind = abi.MAVI_SRC_SINK
+                g = c.geometry_cfg
+                if isinstance(g, CircleCfg):
+                    e.geometry = abi.MAVI_GEOM_CIRCLE
+                    e.radius, e.cx, e.cy = float(g.radius), float(g.center[0]), float(g.center[1])
+                elif isinstance(g, RectangleCfg):
+                    e.geometry = abi.MAVI_GEOM_RECTANGLE
+                    e.length, e.height = float(g.length), float(g.height)
+                    e.bl_x, e.bl_y = float(g.bottom_left[0]), float(g.bottom_left[1])
+                else:
+                    raise ValueError("a sink geometry is a RectangleCfg or a CircleCfg")
+                continue
+            e.kind = abi.MAVI_SRC_SOURCE
+            random_pol = isinstance(c.spawn_pol, str)
+            if random_pol and c.spawn_pol != "random":
+                raise ValueError("spawn_pol is an angle or 'random'")
+            e.pol_mode = abi.MAVI_SPAWN_POL_RANDOM if random_pol else abi.MAVI_SPAWN_POL_FIXED
+            e.pol = 0.0 if random_pol else float(c.spawn_pol)
+            e.pad = float(c.pad)
+            bx, sp, lists = source_boxes(c, grid)
+            e.num_boxes = len(bx)
+            for q, b in enumerate(bx):
+                mb = abi.MaviSpawnBox()
+                mb.bl_x, mb.bl_y, mb.length, mb.height = b
+                mb.num_chunks = -1 if lists is None else len(lists[q])
+                boxes.append(mb)
+                spawn.append(sp[q])
+                if lists is not None:
+                    chunks.extend(lists[q])
+        nb = len(boxes)
+        box_arr = (abi.MaviSpawnBox * max(nb, 1))(*boxes)
+        spawn_xy = np.ascontiguousarray(np.concatenate(spawn).reshape(-1)) if spawn else np.zeros(2)
+        chunk_rc = np.ascontiguousarray(np.asarray(chunks, dtype=np.int32).reshape(-1)) if chunks else \
+            np.zeros(2, dtype=np.int32)
+        return mask, len(cfgs), entries, box_arr, spawn_xy, chunk_rc
+
+    def _configure_replica(self, h, replica: int):
+        """Handle hook: variable rings ids and sources/sinks of this replica."""
+        cfg = self.sources_abi()
+        if cfg is None:
+            return
+        mask, n, entries, boxes, spawn_xy, chunk_rc = cfg
+        h.check(h.lib.mavi_rings_sources(h.handle, replica, abi.as_iptr(mask), n, entries, boxes,
+                                         abi.as_dptr(spawn_xy), abi.as_iptr(chunk_rc)), "mavi_rings_sources")
+
+    def rings_ids(self):
+        """(active_mask[num_rings] bool, uids[num_rings], num_active) on the
+        device (VarRingsIds: mask, uids, num_active)."""
+        h = self._ensure()
+        nr = self.state.num_rings
+        mask = np.zeros(nr, dtype=np.int32)
+        uids = np.zeros(nr, dtype=np.int32)
+        na = C.c_int32()
+        h.check(h.lib.mavi_rings_active(h.handle, 0, abi.as_iptr(mask), abi.as_iptr(uids), C.byref(na)),
+                "mavi_rings_active")
+        return mask.astype(bool), uids, int(na.value)
 
     def _ensure(self, step_kind=None):
         fresh = self._handle is None

@@ -49,6 +49,21 @@ struct OracleSys {
     int64_t num_rings; int32_t nmax;
     double *cont_pos;           /* 2*n */
     double *areas;              /* num_rings */
+    /* VarRingsIds (src/rings/states.jl:20-40) and RingsInfo.cms */
+    int var_ids;
+    int32_t *mask, *uids;       /* num_rings */
+    int64_t *ids;               /* num_rings: active rings first (update_ids!) */
+    int64_t num_active;
+    double *cms;                /* 2*num_rings */
+    /* sources and sinks (src/rings/sources.jl), in the order of the tuple */
+    int32_t src_n;
+    MaviSourceEntry *src;
+    MaviSpawnBox *boxes;        /* all sources' spawn boxes, in order */
+    int64_t nbox;
+    double *spawn;              /* nmax points per box */
+    int32_t *chunk_rc;          /* (row, col) pairs, 0-based */
+    int64_t *box_chunk0;        /* per box: first pair in chunk_rc */
+    int64_t n_random;           /* boxes with a random spawn polarisation */
     /* time_info */
     int64_t num_steps; double time;
     int32_t err;
@@ -583,11 +598,17 @@ static inline int32_t ring_n(const OracleSys* s, int64_t ring) {
     return s->p.rings.num_particles[s->types[ring] - 1];
 }
 
+/* get_rings_ids (src/rings/states.jl:35-38, 52-53): the active rings,
+ * ascending; every ring without VarRingsIds. */
+static inline int64_t rings_count(const OracleSys* s) { return s->var_ids ? s->num_active : s->num_rings; }
+static inline int64_t ring_at(const OracleSys* s, int64_t k) { return s->var_ids ? s->ids[k] : k; }
+
 /* update_continuos_pos! (src/rings/integration.jl:118-138): periodic only. */
 static void update_continuos_pos(OracleSys* s) {
     const MaviSpace* sp = &s->p.spaces[0];
     int periodic = (sp->wall == MAVI_WALL_PERIODIC);
-    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+    for (int64_t k = 0; k < rings_count(s); k++) {
+        int64_t ring = ring_at(s, k);
         int64_t base = ring * s->nmax;
         for (int64_t i = 0; i < s->nmax; i++) {
             s->cont_pos[2 * (base + i)] = s->pos[2 * (base + i)];
@@ -618,7 +639,8 @@ static double calc_area(const double* rp, int32_t n) {
 static void rings_bonded_forces(OracleSys* s) {
     const MaviRingsCfg* rc = &s->p.rings;
     double* F = s->forces;
-    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+    for (int64_t kr = 0; kr < rings_count(s); kr++) {
+        int64_t ring = ring_at(s, kr);
         int t = s->types[ring] - 1;
         int32_t n = rc->num_particles[t];
         double k = rc->k_spring[t], l = rc->l_spring[t];
@@ -633,7 +655,8 @@ static void rings_bonded_forces(OracleSys* s) {
             F[2 * p2] -= f.x; F[2 * p2 + 1] -= f.y;
         }
     }
-    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+    for (int64_t kr = 0; kr < rings_count(s); kr++) {
+        int64_t ring = ring_at(s, kr);
         int t = s->types[ring] - 1;
         int32_t n = rc->num_particles[t];
         double area = calc_area(s->cont_pos + 2 * ring * s->nmax, n);
@@ -651,7 +674,8 @@ static void rings_bonded_forces(OracleSys* s) {
             F[2 * idx] -= fmod_ * a_deriv.x; F[2 * idx + 1] -= fmod_ * a_deriv.y;
         }
     }
-    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+    for (int64_t kr = 0; kr < rings_count(s); kr++) {
+        int64_t ring = ring_at(s, kr);
         int t = s->types[ring] - 1;
         int32_t n = rc->num_particles[t];
         double kb = rc->k_bend[t];
@@ -678,7 +702,8 @@ static void rings_bonded_forces(OracleSys* s) {
 static void rings_update(OracleSys* s, const double* noise) {
     const MaviRingsCfg* rc = &s->p.rings;
     double dt = s->p.dt;
-    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+    for (int64_t kr = 0; kr < rings_count(s); kr++) {
+        int64_t ring = ring_at(s, kr);
         int t = s->types[ring] - 1;
         int32_t n = rc->num_particles[t];
         double vo = rc->vo[t], relax_time = rc->relax_time[t], mu = rc->mobility[t], dr = rc->rot_diff[t];
@@ -702,6 +727,187 @@ static void rings_update(OracleSys* s, const double* noise) {
         double d_theta = 1 / relax_time * asin(cross) * dt + sqrt(2 * dr * dt) * noise[ring];
         s->pol[ring] += d_theta;
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* variable number of rings: sources and sinks (src/rings/sources.jl)        */
+/* ------------------------------------------------------------------------ */
+
+/* calc_active_ids! (src/rings/states.jl:200-219): ids and p_ids of the active
+ * rings in ascending order; entries of ids past the count keep their values. */
+static void update_ids(OracleSys* s) {
+    int64_t pointer = 0, p_pointer = 0;
+    for (int64_t ring = 0; ring < s->num_rings; ring++) {
+        if (!s->mask[ring]) continue;
+        s->ids[pointer++] = ring;
+        for (int32_t i = 0; i < ring_n(s, ring); i++) s->pids[p_pointer++] = ring * s->nmax + i;
+    }
+    s->num_active = pointer;
+    s->npids = p_pointer;
+}
+
+/* update_cms! (src/rings/integration.jl:366-372) with get_continuos_pos
+ * (src/rings/rings.jl:31-41): positions, or the continuous positions of the
+ * last update_continuos_pos! with periodic walls; summed in particle order. */
+static void update_cms(OracleSys* s) {
+    const double* src = (s->p.spaces[0].wall == MAVI_WALL_PERIODIC) ? s->cont_pos : s->pos;
+    for (int64_t k = 0; k < s->num_active; k++) {
+        int64_t ring = s->ids[k];
+        int32_t n = ring_n(s, ring);
+        const double* rp = src + 2 * ring * s->nmax;
+        double sx = rp[0], sy = rp[1];
+        for (int32_t i = 1; i < n; i++) { sx += rp[2 * i]; sy += rp[2 * i + 1]; }
+        s->cms[2 * ring] = sx / n;
+        s->cms[2 * ring + 1] = sy / n;
+    }
+}
+
+/* is_inside(point, ::RectangleCfg; pad) (src/configs.jl:89-93) */
+static int inside_rect(double x, double y, double blx, double bly, double len, double h, double pad) {
+    int ix = (blx - pad <= x) && (x <= blx + len + pad);
+    int iy = (bly - pad <= y) && (y <= bly + h + pad);
+    return ix && iy;
+}
+
+/* is_inside(point, sink geometry) (src/configs.jl:89-93, 165-168) */
+static int sink_inside(const MaviSourceEntry* e, double x, double y) {
+    if (e->geometry == MAVI_GEOM_CIRCLE) {
+        double dx = x - e->cx, dy = y - e->cy;
+        double rp = e->radius + 0.0;
+        return dx * dx + dy * dy <= rp * rp;
+    }
+    return inside_rect(x, y, e->bl_x, e->bl_y, e->length, e->height, 0.0);
+}
+
+/* update_sources! (src/rings/integration.jl:353-358): each sink and source in
+ * order. uniforms: one per random-polarisation box, in box order. */
+static void process_sources(OracleSys* s, const double* uniforms) {
+    int64_t b0 = 0, rnd = 0;
+    for (int32_t e = 0; e < s->src_n; e++) {
+        const MaviSourceEntry* E = &s->src[e];
+        if (E->kind == MAVI_SRC_SINK) {
+            /* process_sink! (src/rings/sources.jl:253-260): the view
+             * ids[1:num_active] is taken once; remove_ring! decrements num_active */
+            int64_t L = s->num_active;
+            for (int64_t k = 0; k < L; k++) {
+                int64_t ring = s->ids[k];
+                if (sink_inside(E, s->cms[2 * ring], s->cms[2 * ring + 1])) {
+                    s->mask[ring] = 0;
+                    s->num_active -= 1;
+                }
+            }
+            continue;
+        }
+        /* update_area_empty! (src/rings/sources.jl:193-224) for every box first */
+        int32_t nb = E->num_boxes;
+        int empty[MAVI_MAX_SPAWN_BOXES];
+        for (int32_t b = 0; b < nb; b++) {
+            const MaviSpawnBox* B = &s->boxes[b0 + b];
+            empty[b] = 1;
+            if (B->num_chunks < 0 || !s->has_chunks) {
+                /* PosChecker: active particle ids of the last update_ids! */
+                for (int64_t k = 0; k < s->npids && empty[b]; k++) {
+                    int64_t i = s->pids[k];
+                    if (inside_rect(s->pos[2 * i], s->pos[2 * i + 1], B->bl_x, B->bl_y, B->length, B->height, E->pad))
+                        empty[b] = 0;
+                }
+            } else {
+                /* ChunksChecker: the chunk lists of the last update_chunks! */
+                const int32_t* rc = s->chunk_rc + 2 * s->box_chunk0[b0 + b];
+                for (int32_t c = 0; c < B->num_chunks && empty[b]; c++) {
+                    int64_t ch = (int64_t)rc[2 * c + 1] * s->rows + rc[2 * c];
+                    for (int32_t q = 0; q < s->num_in_chunk[ch] && empty[b]; q++) {
+                        int64_t i = s->chunk_particles[ch * s->cap + q];
+                        if (inside_rect(s->pos[2 * i], s->pos[2 * i + 1], B->bl_x, B->bl_y, B->length, B->height,
+                                        E->pad))
+                            empty[b] = 0;
+                    }
+                }
+            }
+        }
+        /* process_source! (:226-239) */
+        for (int32_t b = 0; b < nb; b++) {
+            double pol = E->pol;
+            if (E->pol_mode == MAVI_SPAWN_POL_RANDOM) pol = uniforms[rnd++] * 2.0 * 3.141592653589793;
+            if (!empty[b]) continue;
+            /* add_ring! (src/rings/states.jl:162-174): the first inactive slot */
+            int64_t ring = -1;
+            for (int64_t i = 0; i < s->num_rings; i++)
+                if (!s->mask[i]) { ring = i; break; }
+            if (ring < 0) continue;
+            const double* sp = s->spawn + 2 * (b0 + b) * s->nmax;
+            memcpy(s->pos + 2 * ring * s->nmax, sp, sizeof(double) * 2 * s->nmax);
+            s->pol[ring] = pol;
+            s->mask[ring] = 1;
+            int32_t mu = s->uids[0];
+            for (int64_t i = 1; i < s->num_rings; i++) if (s->uids[i] > mu) mu = s->uids[i];
+            s->uids[ring] = mu + 1;
+            s->num_active += 1;
+            int32_t n = ring_n(s, ring);
+            double sx = sp[0], sy = sp[1];
+            for (int32_t i = 1; i < n; i++) { sx += sp[2 * i]; sy += sp[2 * i + 1]; }
+            s->cms[2 * ring] = sx / n;
+            s->cms[2 * ring + 1] = sy / n;
+        }
+        b0 += nb;
+    }
+}
+
+int32_t oracle_rings_sources(OracleSys* s, const int32_t* active_mask, int32_t num_entries,
+                             const MaviSourceEntry* entries, const MaviSpawnBox* boxes, const double* spawn_xy,
+                             const int32_t* chunk_rc) {
+    if (s->p.state_kind != MAVI_STATE_RINGS) return MAVI_ERR_UNSUPPORTED;
+    if (num_entries < 0 || num_entries > MAVI_MAX_SOURCE_ENTRIES) return MAVI_ERR_INVALID_ARG;
+    if (!s->mask) {
+        s->mask = (int32_t*)malloc(sizeof(int32_t) * s->num_rings);
+        s->uids = (int32_t*)malloc(sizeof(int32_t) * s->num_rings);
+        s->ids = (int64_t*)malloc(sizeof(int64_t) * s->num_rings);
+        s->cms = (double*)calloc(2 * s->num_rings, sizeof(double));
+    }
+    for (int64_t r = 0; r < s->num_rings; r++) {
+        s->mask[r] = active_mask ? (active_mask[r] != 0) : 1;
+        s->uids[r] = (int32_t)(r + 1);
+        s->ids[r] = r;
+    }
+    free(s->src); free(s->boxes); free(s->spawn); free(s->chunk_rc); free(s->box_chunk0);
+    s->src_n = num_entries;
+    s->src = (MaviSourceEntry*)malloc(sizeof(MaviSourceEntry) * (num_entries ? num_entries : 1));
+    if (num_entries) memcpy(s->src, entries, sizeof(MaviSourceEntry) * num_entries);
+    s->nbox = 0;
+    s->n_random = 0;
+    for (int32_t e = 0; e < num_entries; e++)
+        if (entries[e].kind == MAVI_SRC_SOURCE) {
+            if (entries[e].num_boxes < 1 || entries[e].num_boxes > MAVI_MAX_SPAWN_BOXES) return MAVI_ERR_INVALID_ARG;
+            s->nbox += entries[e].num_boxes;
+            if (entries[e].pol_mode == MAVI_SPAWN_POL_RANDOM) s->n_random += entries[e].num_boxes;
+        }
+    s->boxes = (MaviSpawnBox*)malloc(sizeof(MaviSpawnBox) * (s->nbox ? s->nbox : 1));
+    s->box_chunk0 = (int64_t*)malloc(sizeof(int64_t) * (s->nbox ? s->nbox : 1));
+    s->spawn = (double*)malloc(sizeof(double) * 2 * s->nmax * (s->nbox ? s->nbox : 1));
+    int64_t nchunk = 0;
+    for (int64_t b = 0; b < s->nbox; b++) {
+        s->boxes[b] = boxes[b];
+        s->box_chunk0[b] = nchunk;
+        if (boxes[b].num_chunks > 0) nchunk += boxes[b].num_chunks;
+    }
+    if (s->nbox) memcpy(s->spawn, spawn_xy, sizeof(double) * 2 * s->nmax * s->nbox);
+    s->chunk_rc = (int32_t*)malloc(sizeof(int32_t) * 2 * (nchunk ? nchunk : 1));
+    if (nchunk) memcpy(s->chunk_rc, chunk_rc, sizeof(int32_t) * 2 * nchunk);
+    s->var_ids = 1;
+    /* RingsSystem(): update_continuos_pos!, update_ids!, update_chunks_all!
+     * (src/rings/rings.jl:280-283) */
+    update_ids(s);
+    update_continuos_pos(s);
+    return oracle_update_chunks(s);
+}
+
+int32_t oracle_rings_active(OracleSys* s, int32_t* active_mask, int32_t* uids, int32_t* num_active) {
+    for (int64_t r = 0; r < s->num_rings; r++) {
+        if (active_mask) active_mask[r] = s->var_ids ? s->mask[r] : 1;
+        if (uids) uids[r] = s->var_ids ? s->uids[r] : (int32_t)(r + 1);
+    }
+    if (num_active) *num_active = (int32_t)rings_count(s);
+    return MAVI_OK;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -742,7 +948,7 @@ int64_t oracle_noise_count(OracleSys* s) {
     switch (s->p.step_kind) {
     case MAVI_STEP_SZABO: return s->n;
     case MAVI_STEP_RTP: return 2 * s->n;
-    case MAVI_STEP_RINGS: return s->num_rings;
+    case MAVI_STEP_RINGS: return s->num_rings + (s->var_ids ? s->n_random : 0);
     }
     return 0;
 }
@@ -798,6 +1004,11 @@ static int32_t step_once(OracleSys* s, int32_t fm, const double* noise) {
         update_time(s);
         return MAVI_OK;
     case MAVI_STEP_RINGS:                           /* src/rings/integration.jl:522-543 */
+        if (s->var_ids) {
+            update_cms(s);
+            process_sources(s, noise ? noise + s->num_rings : NULL);
+            update_ids(s);
+        }
         if ((st = oracle_update_chunks(s))) return st;
         update_continuos_pos(s);
         clean_forces(s);
@@ -1064,6 +1275,8 @@ void oracle_destroy(OracleSys* s) {
     free(s->pos); free(s->vel); free(s->pol); free(s->types); free(s->forces); free(s->slices);
     free(s->pids); free(s->chunk_particles); free(s->num_in_chunk); free(s->nbr); free(s->nbr_cnt);
     free(s->cont_pos); free(s->areas);
+    free(s->mask); free(s->uids); free(s->ids); free(s->cms);
+    free(s->src); free(s->boxes); free(s->spawn); free(s->chunk_rc); free(s->box_chunk0);
     free(s);
 }
 
@@ -1131,5 +1344,7 @@ int32_t oracle_struct_sizes(int64_t* out) {
     out[4] = (int64_t)sizeof(MaviOptions);
     out[5] = (int64_t)sizeof(MaviStats);
     out[6] = (int64_t)sizeof(MaviProfile);
-    return 7;
+    out[7] = (int64_t)sizeof(MaviSourceEntry);
+    out[8] = (int64_t)sizeof(MaviSpawnBox);
+    return 9;
 }

@@ -53,6 +53,12 @@ int32_t oracle_get_areas(OracleSys* s, double* areas);
 int64_t oracle_count_pairs(OracleSys* s);
 int32_t oracle_rings_neighbors(OracleSys* s, double tol, int32_t type_all, int32_t max_list, int32_t* counts,
                                int32_t* lists);
+/* Variable rings ids with sources and sinks, as mavi_rings_sources; the step's
+ * noise is num_rings normals then one uniform per random-polarisation box. */
+int32_t oracle_rings_sources(OracleSys* s, const int32_t* active_mask, int32_t num_entries,
+                             const MaviSourceEntry* entries, const MaviSpawnBox* boxes, const double* spawn_xy,
+                             const int32_t* chunk_rc);
+int32_t oracle_rings_active(OracleSys* s, int32_t* active_mask, int32_t* uids, int32_t* num_active);
 /* Julia float `div` as used by update_particle_chunk! (src/chunks.jl:129-130). */
 double  oracle_julia_div(double x, double y);
 /* update_particle_chunk! row/col (1-based, before bounds checks) for a point. */

@@ -56,6 +56,9 @@ def _load_lib():
         "oracle_count_pairs": (C.c_int64, [vp]),
         "oracle_rings_neighbors": (C.c_int32, [vp, C.c_double, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                                C.POINTER(C.c_int32)]),
+        "oracle_rings_sources": (C.c_int32, [vp, ip, C.c_int32, C.POINTER(abi.MaviSourceEntry),
+                                             C.POINTER(abi.MaviSpawnBox), dp, ip]),
+        "oracle_rings_active": (C.c_int32, [vp, ip, ip, ip]),
         "oracle_julia_div": (C.c_double, [C.c_double, C.c_double]),
         "oracle_chunk_of": (C.c_int32, [vp, C.c_double, C.c_double, lp, lp]),
         "oracle_struct_sizes": (C.c_int32, [lp]),
@@ -201,6 +204,27 @@ class OracleSystem:
     def count_pairs(self) -> int:
         return int(self.lib.oracle_count_pairs(self.h))
 
+    def rings_sources(self, mask, num_entries, entries, boxes, spawn_xy, chunk_rc):
+        """Variable rings ids with sources and sinks (the arguments of
+        mavi_rings_sources for this replica)."""
+        ip = C.POINTER(C.c_int32)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        sp = np.ascontiguousarray(spawn_xy, dtype=np.float64)
+        rc = np.ascontiguousarray(chunk_rc, dtype=np.int32)
+        self._ck(self.lib.oracle_rings_sources(self.h, None if m is None else m.ctypes.data_as(ip), int(num_entries),
+                                               entries, boxes, _dp(sp), rc.ctypes.data_as(ip)), "rings_sources")
+
+    def rings_ids(self):
+        """(active mask bool, uids, num_active)."""
+        nr = self.params.rings.num_rings
+        m = np.zeros(nr, dtype=np.int32)
+        u = np.zeros(nr, dtype=np.int32)
+        na = C.c_int32()
+        ip = C.POINTER(C.c_int32)
+        self._ck(self.lib.oracle_rings_active(self.h, m.ctypes.data_as(ip), u.ctypes.data_as(ip), C.byref(na)),
+                 "rings_active")
+        return m.astype(bool), u, int(na.value)
+
     def chunk_of(self, x, y):
         r, c = C.c_int64(), C.c_int64()
         st = self.lib.oracle_chunk_of(self.h, float(x), float(y), C.byref(r), C.byref(c))
@@ -215,7 +239,7 @@ def struct_sizes():
     out = (C.c_int64 * 16)()
     n = _load_lib().oracle_struct_sizes(out)
     names = ["MaviSpace", "MaviRingsCfg", "MaviDynamicCfg", "MaviReplicaParams", "MaviOptions", "MaviStats",
-             "MaviProfile"]
+             "MaviProfile", "MaviSourceEntry", "MaviSpawnBox"]
     return {names[k]: out[k] for k in range(n)}
 
 
@@ -236,4 +260,8 @@ def from_system(system, nthreads: int = 1, step_kind=None) -> OracleSystem:
     vel = getattr(st, "vel", None)
     pol = st.pol_array()
     types = st.types_array() if getattr(system, "is_rings", False) else None
-    return OracleSystem(p, st.pos, vel, pol, types, nthreads=nthreads)
+    o = OracleSystem(p, st.pos, vel, pol, types, nthreads=nthreads)
+    src = system.sources_abi() if hasattr(system, "sources_abi") else None
+    if src is not None:
+        o.rings_sources(*src)
+    return o
