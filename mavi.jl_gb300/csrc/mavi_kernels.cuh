@@ -824,8 +824,8 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
             else pair_term<DYN>(C, R, rep, me, P[j], uq, shx, shy, mi, acc);
         }
     };
-    if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224)
-        visit((int32_t)R.a0, (int32_t)(R.a0 + R.na), 0, 0, R.min_image);
+    if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224): its one chunk
+        visit(C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
         return;
     }
     int32_t lc = (int32_t)(cell - R.c0);
@@ -2176,6 +2176,7 @@ static __global__ void k_energy_terms(Ctx C, int32_t dyn, int32_t all_pairs, dou
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= C.M) return;
     const DevRep& R = C.reps[C.rep_cur[s]];
+    if (C.var_rings && C.cell_cur[s] == C.park) { ke_t[s] = 0.0; pe_t[s] = 0.0; return; }   // inactive ring
     double ke = 0;
     if (has_vel) { double2 v = C.vel_cur[s]; ke = v.x * v.x + v.y * v.y; }
     ke_t[s] = ke;
@@ -2196,7 +2197,8 @@ static __global__ void k_energy_terms(Ctx C, int32_t dyn, int32_t all_pairs, dou
         }
     };
     if (all_pairs || !R.has_chunks) {
-        visit((int32_t)R.a0, (int32_t)(R.a0 + R.na));
+        // the replica's chunked particles (parked ones, of inactive rings, follow every chunk)
+        visit(C.start[R.c0], C.start[R.c0 + (int64_t)R.rows * R.cols]);
     } else {
         int64_t lc = C.cell_cur[s] - R.c0;
         int32_t row = (int32_t)(lc % R.rows), col = (int32_t)(lc / R.rows);
@@ -2242,7 +2244,8 @@ static __global__ void k_pair_count(Ctx C, unsigned long long* __restrict__ tota
     unsigned long long c = 0;
     if (s < C.M) {
         const DevRep& R = C.reps[C.rep_cur[s]];
-        if (!R.has_chunks) c = R.na - 1;
+        if (C.var_rings && C.cell_cur[s] == C.park) c = 0;
+        else if (!R.has_chunks) c = C.start[R.c0 + 1] - C.start[R.c0] - 1;
         else {
             int64_t lc = C.cell_cur[s] - R.c0;
             int32_t row = (int32_t)(lc % R.rows), col = (int32_t)(lc / R.rows);

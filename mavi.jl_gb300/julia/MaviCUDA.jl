@@ -23,6 +23,9 @@ using Mavi.Configs: DeviceMode, RectangleCfg, CircleCfg, LinesCfg, RigidWalls, P
     SlipperyWalls, PotentialWalls, ManyWalls, ManyGeometries, HarmTruncCfg, LenJonesCfg, SzaboCfg,
     RunTumbleCfg, has_chunks
 using Mavi.States: SecondLawState, SelfPropelledState
+import Mavi.Rings
+const RC = Mavi.Rings.Configs
+const RS = Mavi.Rings.Sources
 
 const libmavi = get(ENV, "MAVI_CUDA_LIB", joinpath(@__DIR__, "..", "lib", "libmavi_cuda.so"))
 
@@ -36,6 +39,8 @@ const WALL_RIGID, WALL_PERIODIC, WALL_SLIPPERY, WALL_POTENTIAL = Int32.(0:3)
 const PREC_FP64, PREC_MIXED = Int32(0), Int32(1)
 const NOISE_DEVICE, NOISE_INJECTED = Int32(0), Int32(1)
 const MAX_SPACES, MAX_LINES, MAX_TYPES = 4, 16, 4
+const SRC_SOURCE, SRC_SINK = Int32(0), Int32(1)
+const SPAWN_POL_FIXED, SPAWN_POL_RANDOM = Int32(0), Int32(1)
 
 # ---- C structs (same field order and types as the header) -------------------
 struct CSpace
@@ -76,6 +81,18 @@ struct CReplicaParams
     spaces::NTuple{MAX_SPACES, CSpace}
     dyn::CDynamicCfg
     rings::CRingsCfg
+end
+
+struct CSourceEntry
+    kind::Int32; num_boxes::Int32; pol_mode::Int32; geometry::Int32
+    pol::Float64; pad::Float64
+    length::Float64; height::Float64; bl_x::Float64; bl_y::Float64
+    radius::Float64; cx::Float64; cy::Float64
+end
+
+struct CSpawnBox
+    bl_x::Float64; bl_y::Float64; length::Float64; height::Float64
+    num_chunks::Int32; _pad0::Int32
 end
 
 struct COptions
@@ -157,7 +174,34 @@ function cdynamic(cfg)
                                            cfg.relax_time, cfg.k_adh, cfg.r_eq, cfg.r_max, cfg.rot_diff, z)
     cfg isa RunTumbleCfg && return CDynamicCfg(DYN_RUN_TUMBLE, 0, z, z, z, z, cfg.sigma, cfg.epsilon,
                                                cfg.vo, 1.0, z, z, z, z, z, cfg.tumble_rate)
-    error("unsupported dynamic config $(typeof(cfg)) (rings: use the Python host API or extend this shim)")
+    cfg isa RC.RingsCfg && return CDynamicCfg(DYN_RINGS, 0, z, z, z, z, z, z, z, 1.0, z, z, z, z, z, z)
+    error("unsupported dynamic config $(typeof(cfg))")
+end
+
+# RingsCfg (src/rings/configs.jl:95-163) for the state's rings: per-type
+# vectors (a scalar applies to every type) and the InteractionMatrix as four
+# row-major MAX_TYPES x MAX_TYPES matrices.
+_tup4(v, T) = ntuple(k -> k <= length(v) ? T(v[k]) : zero(T), MAX_TYPES)
+function crings(cfg, st)
+    nt = cfg.num_types
+    nmax, nr = size(st.rings_pos)
+    np = st.num_particles
+    nps = np isa AbstractVector ? np : fill(np, nt)
+    finder = cfg.interaction_finder
+    inter(a, b) = finder isa RC.InteractionMatrix ? finder.matrix[a, b] : finder
+    flat = zeros(4 * MAX_TYPES * MAX_TYPES)
+    for a in 1:nt, b in 1:nt
+        it = inter(a, b)
+        k = (a - 1) * MAX_TYPES + (b - 1)
+        flat[1 + k] = it.k_rep
+        flat[1 + MAX_TYPES^2 + k] = it.k_atr
+        flat[1 + 2 * MAX_TYPES^2 + k] = it.dist_eq
+        flat[1 + 3 * MAX_TYPES^2 + k] = it.dist_max
+    end
+    pt(x) = _tup4(x isa AbstractVector ? x : fill(x, nt), Float64)
+    CRingsCfg(Int32(nt), Int32(nr), Int32(nmax), Int32(0), _tup4(nps, Int32),
+              pt(cfg.p0), pt(cfg.relax_time), pt(cfg.vo), pt(cfg.mobility), pt(cfg.rot_diff), pt(cfg.k_area),
+              pt(cfg.k_spring), pt(cfg.l_spring), ntuple(_ -> 0.0, MAX_TYPES), Tuple(flat))
 end
 
 const ZRINGS = CRingsCfg(0, 0, 0, 0, ntuple(_ -> Int32(0), MAX_TYPES), ntuple(_ -> ntuple(_ -> 0.0, MAX_TYPES), 9)...,
@@ -165,6 +209,7 @@ const ZRINGS = CRingsCfg(0, 0, 0, 0, ntuple(_ -> Int32(0), MAX_TYPES), ntuple(_ 
 
 function step_kind(system)
     cfg = system.dynamic_cfg
+    cfg isa RC.RingsCfg && return STEP_RINGS
     cfg isa SzaboCfg && return STEP_SZABO
     cfg isa RunTumbleCfg && return STEP_RTP
     return STEP_NEWTON
@@ -175,10 +220,16 @@ function replica_params(system, kind=step_kind(system))
     sp, nsp = cspaces(system.space_cfg)
     cc = system.int_cfg.chunks_cfg
     cols, rows = has_chunks(system.int_cfg) ? (Int32(cc.num_cols), Int32(cc.num_rows)) : (Int32(0), Int32(0))
-    sk = st isa SecondLawState ? STATE_SECOND_LAW : STATE_SELF_PROPELLED
+    rings = st isa Rings.RingsState
+    sk = rings ? STATE_RINGS : st isa SecondLawState ? STATE_SECOND_LAW : STATE_SELF_PROPELLED
     CReplicaParams(length(st.pos), sk, kind, nsp, cols, rows, 0, system.int_cfg.dt, sp,
-                   cdynamic(system.dynamic_cfg), ZRINGS)
+                   cdynamic(system.dynamic_cfg), rings ? crings(system.dynamic_cfg, st) : ZRINGS)
 end
+
+# pointers of the state arrays the ABI takes (velocities, polarisations)
+_vel_ptr(st) = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
+_pol_ptr(st) = st isa SelfPropelledState ? pointer(st.pol_angle) :
+               st isa Rings.RingsState ? pointer(st.pol) : Ptr{Float64}(C_NULL)
 
 # ---- handles -------------------------------------------------------------------
 mutable struct Handle
@@ -206,30 +257,91 @@ function handle!(system)
                    dev.device, 1, 0, -1)   # gather: autotuned
     params = Ref(replica_params(system))
     st = system.state
-    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
-    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    vel, pol = _vel_ptr(st), _pol_ptr(st)
+    types = st isa Rings.RingsState && !isnothing(st.types) ? Int32.(st.types) : Int32[]
     out = Ref{Ptr{Cvoid}}(C_NULL)
-    GC.@preserve st begin
+    GC.@preserve st types begin
         check(ccall((:mavi_create, libmavi), Cint,
                     (Ref{COptions}, Int32, Ref{CReplicaParams}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
                      Ptr{Int32}, Ref{Ptr{Cvoid}}),
-                    opt, 1, params, pointer(st.pos), vel, pol, C_NULL, out), "mavi_create")
+                    opt, 1, params, pointer(st.pos), vel, pol,
+                    isempty(types) ? Ptr{Int32}(C_NULL) : pointer(types), out), "mavi_create")
     end
     h = Handle(out[])
     finalizer(x -> ccall((:mavi_destroy, libmavi), Cint, (Ptr{Cvoid},), x.ptr), h)
     HANDLES[system] = h
+    st isa Rings.RingsState && configure_sources!(system, h.ptr)
     return h.ptr
+end
+
+"""
+Variable rings ids and the system's sources and sinks (VarRingsIds,
+src/rings/states.jl:20-40; `system.info.sources`, src/rings/rings.jl:162-186)
+passed to `mavi_rings_sources`, from the reference's own `Source` / `Sink`
+objects: boxes (`bbox`), spawn points (`bbox_spawn_pos`) and chunk lists
+(`checker.ids`) are the ones the reference computed.
+"""
+function configure_sources!(system, h)
+    st = system.state
+    ids = st.rings_ids
+    ids isa Rings.States.VarRingsIds || return
+    mask = Int32.(ids.mask)
+    entries, boxes, spawn, rc = CSourceEntry[], CSpawnBox[], Float64[], Int32[]
+    srcs = system.info.sources
+    for s in (isnothing(srcs) ? () : srcs)
+        if s isa RS.Sink
+            g = s.cfg.geometry_cfg
+            if g isa CircleCfg
+                push!(entries, CSourceEntry(SRC_SINK, 0, 0, GEOM_CIRCLE, 0, 0, 0, 0, 0, 0,
+                                            g.radius, g.center[1], g.center[2]))
+            else
+                push!(entries, CSourceEntry(SRC_SINK, 0, 0, GEOM_RECTANGLE, 0, 0, g.length, g.height,
+                                            g.bottom_left[1], g.bottom_left[2], 0, 0, 0))
+            end
+            continue
+        end
+        random = s.cfg.spawn_pol isa RS.RandomPol
+        nb = length(s.bbox)
+        push!(entries, CSourceEntry(SRC_SOURCE, nb, random ? SPAWN_POL_RANDOM : SPAWN_POL_FIXED, 0,
+                                    random ? 0.0 : Float64(s.cfg.spawn_pol), Float64(s.cfg.pad),
+                                    0, 0, 0, 0, 0, 0, 0))
+        for i in 1:nb
+            b = s.bbox[i]
+            lst = s.checker isa RS.ChunksChecker ? s.checker.ids[i] : nothing
+            push!(boxes, CSpawnBox(b.bottom_left[1], b.bottom_left[2], b.length, b.height,
+                                   isnothing(lst) ? -1 : length(lst), 0))
+            for p in s.bbox_spawn_pos[i]
+                push!(spawn, p[1], p[2])
+            end
+            isnothing(lst) || for c in lst
+                push!(rc, Int32(c[1] - 1), Int32(c[2] - 1))
+            end
+        end
+    end
+    GC.@preserve mask entries boxes spawn rc check(
+        ccall((:mavi_rings_sources, libmavi), Cint,
+              (Ptr{Cvoid}, Int32, Ptr{Int32}, Int32, Ptr{CSourceEntry}, Ptr{CSpawnBox}, Ptr{Float64}, Ptr{Int32}),
+              h, 0, mask, length(entries), entries, boxes, spawn, rc), "mavi_rings_sources", h)
 end
 
 "Copy the GPU state and the time back into `system` (user particle order)."
 function sync!(system)
     h = handle!(system)
     st = system.state
-    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
-    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    vel, pol = _vel_ptr(st), _pol_ptr(st)
     GC.@preserve st check(ccall((:mavi_download_state, libmavi), Cint,
                                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
                                 h, pointer(st.pos), vel, pol), "mavi_download_state", h)
+    if st isa Rings.RingsState && st.rings_ids isa Rings.States.VarRingsIds
+        ids = st.rings_ids
+        nr = length(ids.mask)
+        mask, uids, na = zeros(Int32, nr), zeros(Int32, nr), Ref{Int32}(0)
+        check(ccall((:mavi_rings_active, libmavi), Cint, (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Int32}, Ref{Int32}),
+                    h, 0, mask, uids, na), "mavi_rings_active", h)
+        ids.mask .= mask .!= 0
+        ids.uids .= uids
+        Mavi.States.update_ids!(st)          # ids, p_ids, counts (calc_active_ids!)
+    end
     n, t = Ref{Int64}(0), Ref{Float64}(0)
     check(ccall((:mavi_get_time, libmavi), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Float64}), h, n, t),
           "mavi_get_time", h)
@@ -242,8 +354,7 @@ end
 function upload!(system)
     h = handle!(system)
     st = system.state
-    vel = st isa SecondLawState ? pointer(st.vel) : Ptr{SVector{2,Float64}}(C_NULL)
-    pol = st isa SelfPropelledState ? pointer(st.pol_angle) : Ptr{Float64}(C_NULL)
+    vel, pol = _vel_ptr(st), _pol_ptr(st)
     GC.@preserve st check(ccall((:mavi_upload_state, libmavi), Cint,
                                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
                                 h, pointer(st.pos), vel, pol), "mavi_upload_state", h)
@@ -276,6 +387,12 @@ end
 # get_step_function(::StandardSys, system) (src/integration.jl:539-548) dispatches on
 # the dynamic config; a CUDA device mode takes precedence.
 function Mavi.Integration.get_step_function(t::Mavi.Systems.StandardSys, system::Mavi.Systems.System{
+        T, ND, NT, S, W, G, D, <:Mavi.Configs.IntCfg{<:Number, <:Any, CUDADevice}}) where {T, ND, NT, S, W, G, D}
+    return gpu_step!
+end
+
+# the rings step (get_step_function(::RingsSys, system), src/rings/integration.jl:545)
+function Mavi.Integration.get_step_function(t::Rings.RingsSys, system::Mavi.Systems.System{
         T, ND, NT, S, W, G, D, <:Mavi.Configs.IntCfg{<:Number, <:Any, CUDADevice}}) where {T, ND, NT, S, W, G, D}
     return gpu_step!
 end

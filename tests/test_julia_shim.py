@@ -19,6 +19,8 @@ PAIRS = {
     "CDynamicCfg": ("MaviDynamicCfg", None),
     "CReplicaParams": ("MaviReplicaParams", None),
     "COptions": ("MaviOptions", None),
+    "CSourceEntry": ("MaviSourceEntry", None),
+    "CSpawnBox": ("MaviSpawnBox", None),
 }
 
 
