@@ -714,6 +714,12 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     int32_t* ring_types_d = nullptr;
     int32_t* ring_rep_d = nullptr;
     if (s->is_rings) {
+        // packed ring identity per slot when every replica fits the packing
+        bool fits = true;
+        for (const DevRep& R : s->reps_h) fits = fits && R.nmax <= kRingKeyMaxNmax && R.num_rings <= kRingKeyMaxRings;
+        int32_t* rkey_d = nullptr;
+        if (fits) { ALLOC(C.rinfo_cur, M); ALLOC(rkey_d, N); }
+        C.rkey_user = rkey_d;
         ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings);
         ALLOC(ring_rep_d, s->total_rings); ALLOC(C.ring_cs, s->total_rings); ALLOC(C.ring_vc, s->total_rings);
     }
@@ -772,6 +778,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     // identity user order over active slots
     std::vector<int32_t> uid_h(M), rep_h(M);
     std::vector<int32_t> types_all, ring_rep_h;
+    std::vector<int32_t> rkey_h(C.rkey_user ? N : 0, 0);
     {
         int64_t k = 0;
         const int32_t* tc = ring_types;
@@ -786,6 +793,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
                     for (int i = 0; i < p.rings.num_particles[t - 1]; i++) {
                         uid_h[k] = (int32_t)(R.slot0 + (int64_t)q * p.rings.nmax + i);
                         rep_h[k] = r;
+                        // ring_key: replica-local ring, index in the ring, 0-based type
+                        if (!rkey_h.empty()) rkey_h[uid_h[k]] = (q << 12) | (i << 2) | (t - 1);
                         k++;
                     }
                 }
@@ -800,6 +809,9 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         }
     }
     CUDA_TRY(s, cudaMemcpyAsync(reps_d, s->reps_h.data(), sizeof(DevRep) * s->R, cudaMemcpyHostToDevice, s->stream));
+    if (!rkey_h.empty())
+        CUDA_TRY(s, cudaMemcpyAsync(const_cast<int32_t*>(C.rkey_user), rkey_h.data(), sizeof(int32_t) * N,
+                                    cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(cxu_d, cxu_h.data(), sizeof(double) * cxu_h.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(cyu_d, cyu_h.data(), sizeof(double) * cyu_h.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(spaces_d, spaces_h.data(), sizeof(MaviSpace) * spaces_h.size(), cudaMemcpyHostToDevice, s->stream));
