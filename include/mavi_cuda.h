@@ -378,6 +378,12 @@ int mavi_rings_sources(MaviSystem* sys, int32_t replica, const int32_t* active_m
 int mavi_rings_active(MaviSystem* sys, int32_t replica, int32_t* active_mask, int32_t* uids,
                       int32_t* num_active);
 
+/* Ring areas of one replica (num_rings doubles): RingsInfo.areas, which
+ * area_forces! sets (src/rings/integration.jl:140-160) — calc_area of the
+ * continuous positions of the last force evaluation, computed on demand in
+ * FP64. Entries of inactive rings are computed from their parked positions. */
+int mavi_rings_areas(MaviSystem* sys, int32_t replica, double* areas);
+
 int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
 /* Device-time profiling (and reset of the accumulated profile). on: 0 off,
  * 1 per kernel kind and whole step (an event pair around every launch group),

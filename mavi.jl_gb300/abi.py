@@ -214,6 +214,7 @@ SIGNATURES = {
     "mavi_rings_sources": (C.c_int, [_vp, C.c_int32, _ip, C.c_int32, C.POINTER(MaviSourceEntry),
                                      C.POINTER(MaviSpawnBox), _dp, _ip]),
     "mavi_rings_active": (C.c_int, [_vp, C.c_int32, _ip, _ip, _ip]),
+    "mavi_rings_areas": (C.c_int, [_vp, C.c_int32, _dp]),
     "mavi_chunk_lists_noalloc": (C.c_int, [C.POINTER(MaviReplicaParams), _vp, C.c_int64, _vp, _vp, _vp,
                                            C.c_char_p, C.c_int32]),
 }

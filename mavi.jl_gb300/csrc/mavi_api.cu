@@ -720,6 +720,9 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         int32_t* rkey_d = nullptr;
         if (fits) { ALLOC(C.rinfo_cur, M); ALLOC(rkey_d, N); }
         C.rkey_user = rkey_d;
+        // user-order state and force of the rings update
+        ALLOC(C.pos_u, N); ALLOC(C.cell_u, N);
+        if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.off_u, N); ALLOC(C.ff_u, N); } else { ALLOC(C.fd_u, N); }
         ALLOC(C.ring_pol, s->total_rings); ALLOC(C.ring_area, s->total_rings); ALLOC(ring_types_d, s->total_rings);
         ALLOC(ring_rep_d, s->total_rings); ALLOC(C.ring_cs, s->total_rings); ALLOC(C.ring_vc, s->total_rings);
     }
@@ -1320,6 +1323,17 @@ int mavi_rings_active(MaviSystem* s, int32_t replica, int32_t* active_mask, int3
     int rc = check_device_error(s);   // waits for the copies
     if (num_active) *num_active = st[0];
     return rc;
+}
+
+int mavi_rings_areas(MaviSystem* s, int32_t replica, double* areas) {
+    if (!s || !areas || replica < 0 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    if (!s->is_rings) return fail(s, MAVI_ERR_UNSUPPORTED, "ring areas belong to the rings model");
+    const DevRep& R = s->reps_h[replica];
+    if (R.num_rings == 0) return MAVI_OK;
+    k_ring_areas<<<nblocks(R.num_rings), kBlock, 0, s->stream>>>(s->C, R.ring0, R.num_rings, s->C.ring_area);
+    CUDA_TRY(s, cudaGetLastError());
+    CUDA_TRY(s, cudaMemcpyAsync(areas, s->C.ring_area, sizeof(double) * R.num_rings, cudaMemcpyDeviceToHost, s->stream));
+    return check_device_error(s);   // waits for the copy
 }
 
 int mavi_get_stats(MaviSystem* s, MaviStats* st) {

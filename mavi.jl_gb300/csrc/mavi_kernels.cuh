@@ -63,6 +63,14 @@ struct Ctx {
     int32_t *count, *start, *src_of, *slot_of;
     int32_t *key_of, *cell_at;   // per claimed slot: user id and chunk of its particle
     int32_t *rinfo_cur;          // rings: packed ring identity per sorted slot (ring_key), or null
+    // rings: the current state and the pair force in user-slot order, where a
+    // ring's particles are contiguous, so that k_rings reads them coalesced
+    // and without the slot map (null for other models)
+    double2 *pos_u;
+    int2 *off_u;
+    int32_t *cell_u;
+    float2 *ff_u;
+    double2 *fd_u;
     const int32_t *rkey_user;    // the same per user slot (fixed at creation)
     int32_t *tile_sum;   // chunk counts per scan tile, accumulated with the histogram
     int64_t ntiles;
@@ -218,11 +226,14 @@ __device__ __forceinline__ void count_into_chunk(const Ctx& C, bool valid, int64
 // particle's current chunk or -1.
 template <int PREC>
 __device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int64_t s, double x, double y,
-                                            int64_t guess_cell) {
+                                            int64_t guess_cell, int32_t uw = -1) {
+    // uw >= 0: the offset also goes to the user-order copy (rings)
     if (!R.has_chunks) {
         if constexpr (PREC == kPrecMixed) {
             double tx = __dsub_rn(x, R.bb_blx), ty = __dadd_rn(__dadd_rn(-y, R.bb_bly), R.bb_h);
-            C.off_out[s] = fixed_offset(R, 0, 0, tx, ty);
+            const int2 o = fixed_offset(R, 0, 0, tx, ty);
+            C.off_out[s] = o;
+            if (uw >= 0) C.off_u[uw] = o;
         }
         return R.c0;
     }
@@ -238,7 +249,11 @@ __device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int6
     bool finite;
     bin_position(R, x, y, grow, gcol, has_guess, row, col, tx, ty, finite);
     int64_t cell = checked_cell(R, row, col, finite, C.err, s);
-    if constexpr (PREC == kPrecMixed) C.off_out[s] = fixed_offset(R, row, col, tx, ty);
+    if constexpr (PREC == kPrecMixed) {
+        const int2 o = fixed_offset(R, row, col, tx, ty);
+        C.off_out[s] = o;
+        if (uw >= 0) C.off_u[uw] = o;
+    }
     return cell;
 }
 
@@ -250,7 +265,7 @@ __device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int6
 // checks are skipped. Returns -1 when the exact path is needed.
 template <int PREC>
 __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64_t s, double x, double y,
-                                           int32_t cell) {
+                                           int32_t cell, int32_t uw = -1) {
     if (!R.has_chunks) return -1;
     int32_t lc = (int32_t)(cell - R.c0);
     int32_t col = lc / R.rows, row = lc - col * R.rows;
@@ -261,7 +276,10 @@ __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64
     // two-sided tests: a position many chunks away (a periodic wrap) saturates
     // the conversion, and abs(INT_MIN) would pass a one-sided test
     if (ix > 1 - R.half_sx_i && ix < R.half_sx_i - 1 && iy > 1 - R.half_sy_i && iy < R.half_sy_i - 1) {
-        if constexpr (PREC == kPrecMixed) C.off_out[s] = make_int2(ix, iy);
+        if constexpr (PREC == kPrecMixed) {
+            C.off_out[s] = make_int2(ix, iy);
+            if (uw >= 0) C.off_u[uw] = make_int2(ix, iy);
+        }
         return cell;
     }
     return -1;
@@ -284,13 +302,18 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
             const int32_t ring = (C.uid_out[s] - (int32_t)R.slot0) / R.nmax;
             parked = C.ring_active[R.ring0 + ring] == 0;
         }
+        const double2 p = C.pos_out[s];
+        const int32_t uw = C.pos_u ? C.uid_out[s] : -1;   // rings: the user-order copy too
         if (parked) {
             cell = C.park;
         } else {
-            double2 p = C.pos_out[s];
             const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
-            cell = bin_final<PREC>(C, R, s, p.x, p.y, (guess == C.park && C.var_rings) ? -1 : guess);
+            cell = bin_final<PREC>(C, R, s, p.x, p.y, (guess == C.park && C.var_rings) ? -1 : guess, uw);
             cap = R.has_chunks ? R.cap : (1 << 30);
+        }
+        if (uw >= 0) {
+            C.pos_u[uw] = p;
+            C.cell_u[uw] = (int32_t)cell;
         }
     }
     count_into_chunk(C, valid, s, cell, cap);
@@ -1439,9 +1462,10 @@ k_pass(Ctx C, int32_t with_wall_forces) {
         // force (clean_forces!), no neighbours, no pair terms
         if (valid && C.var_rings && cell == C.park) {
             if constexpr (PASS == kPassForce) {
-                if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(0.0, 0.0);
-                else C.ff[s] = make_float2(0.f, 0.f);
-                if (C.nb_mode) C.nb_count[C.uid_cur[s]] = 0;
+                const int32_t u = C.uid_cur[s];
+                if constexpr (PREC == kPrecFP64) C.fd_u[u] = make_double2(0.0, 0.0);
+                else C.ff_u[u] = make_float2(0.f, 0.f);
+                if (C.nb_mode) C.nb_count[u] = 0;
             }
             valid = false;
         }
@@ -1464,13 +1488,16 @@ k_pass(Ctx C, int32_t with_wall_forces) {
         bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
         if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
         const double dt = R.dt;
-        if constexpr (PASS == kPassForce) {
+        if constexpr (PASS == kPassForce && DYN == MAVI_DYN_RINGS) {
+            // rings: the force in user order, where k_rings reads a ring's particles together
+            const int32_t u = C.uid_cur[s];
+            if constexpr (PREC == kPrecFP64) C.fd_u[u] = make_double2(fx, fy);
+            else C.ff_u[u] = make_float2(acc.gx(), acc.gy());
+            if (C.nb_mode) C.nb_count[u] = acc.nb;
+        } else if constexpr (PASS == kPassForce) {
             if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
             else if (walls_f) C.ff[s] = make_float2((float)fx, (float)fy);
             else C.ff[s] = make_float2(acc.gx(), acc.gy());
-            if constexpr (DYN == MAVI_DYN_RINGS) {
-                if (C.nb_mode) C.nb_count[C.uid_cur[s]] = acc.nb;
-            }
         } else if constexpr (PASS == kPassVerlet1) {
             // update_verlet! (src/integration.jl:415-431), first half
             double2 v = C.vel_cur[s];
@@ -1604,9 +1631,10 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         // inactive ring: positions carried over unchanged, no forces
         if (do_update) {
             for (int p = lane; p < n; p += 32) {
-                const int32_t s = C.slot_of[(int32_t)R.slot0 + rl * R.nmax + p];
-                C.pos_out[s] = C.pos_cur[s];
-                C.uid_out[s] = C.uid_cur[s];
+                const int32_t u = (int32_t)R.slot0 + rl * R.nmax + p;
+                const int32_t s = C.slot_of[u];
+                C.pos_out[s] = C.pos_u[u];
+                C.uid_out[s] = u;
                 C.rep_out[s] = rep;
             }
         }
@@ -1617,11 +1645,10 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     const bool fused_count = !C.var_rings;
     double2* P = sp_[w];
     int32_t* S = ss_[w];
+    const int32_t u0 = (int32_t)R.slot0 + rl * R.nmax;   // user slot of particle 0 (contiguous ring)
     for (int p = lane; p < n; p += 32) {
-        int32_t uid = (int32_t)R.slot0 + rl * R.nmax + p;
-        int32_t s = C.slot_of[uid];
-        S[p] = s;
-        P[p] = C.pos_cur[s];
+        S[p] = C.slot_of[u0 + p];
+        P[p] = C.pos_u[u0 + p];
     }
     __syncwarp();
     auto diff = [&](double2 a, double2 b) {
@@ -1646,9 +1673,9 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     // histogram of the next step is taken in this kernel)
     const int32_t cap = R.has_chunks ? R.cap : (1 << 30);
     auto finish = [&](int p, double2 xc, V fx, V fy, bool near_wall = true) -> int64_t {
-        int32_t s = S[p];
-        if constexpr (PREC == kPrecFP64) { double2 f = C.fd[s]; fx += f.x; fy += f.y; }
-        else { float2 f = C.ff[s]; fx += f.x; fy += f.y; }
+        const int32_t s = S[p], u = u0 + p;
+        if constexpr (PREC == kPrecFP64) { double2 f = C.fd_u[u]; fx += f.x; fy += f.y; }
+        else { float2 f = C.ff_u[u]; fx += f.x; fy += f.y; }
         if (R.has_wall_forces && near_wall) {
             double wx = 0.0, wy = 0.0;
             add_wall_forces(C, rep, R, xc.x, xc.y, wx, wy);
@@ -1656,8 +1683,8 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             fy += (V)wy;
         }
         if (!do_update) {
-            if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
-            else C.ff[s] = make_float2(fx, fy);
+            if constexpr (PREC == kPrecFP64) C.fd_u[u] = make_double2(fx, fy);
+            else C.ff_u[u] = make_float2(fx, fy);
             return 0;
         }
         double x, y;
@@ -1678,12 +1705,14 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         if (R.has_walls) apply_walls(C, rep, R, rc.inter_dist_eq[t][t] * 0.5, x, y, dvx, dvy, false);
         int64_t nc = 0;
         if (fused_count) {
-            const int32_t cur = C.cell_cur[s];
-            nc = bin_fast<PREC>(C, R, s, x, y, cur);
-            if (nc < 0) nc = bin_final<PREC>(C, R, s, x, y, cur);
+            const int32_t cur = C.cell_u[u];
+            nc = bin_fast<PREC>(C, R, s, x, y, cur, u);
+            if (nc < 0) nc = bin_final<PREC>(C, R, s, x, y, cur, u);
+            C.pos_u[u] = make_double2(x, y);
+            C.cell_u[u] = (int32_t)nc;
         }
         C.pos_out[s] = make_double2(x, y);
-        C.uid_out[s] = C.uid_cur[s];
+        C.uid_out[s] = u;
         C.rep_out[s] = rep;
         return nc;
     };
@@ -1702,9 +1731,8 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             const bool act = lane < n;
             const int p = act ? lane : 0;
             const int pp = p == n - 1 ? 0 : p + 1, pm = p == 0 ? n - 1 : p - 1;
-            const int32_t sp = S[p];
-            const int2 off = C.off_cur[sp];
-            const int32_t lc = C.cell_cur[sp] - (int32_t)R.c0;
+            const int2 off = C.off_u[u0 + p];
+            const int32_t lc = C.cell_u[u0 + p] - (int32_t)R.c0;
             const int32_t col = lc / R.rows, row = lc - col * R.rows;
             const long long X = (long long)col * R.sx_u + off.x;
             const long long Y = -(long long)row * R.sy_u + off.y;
@@ -1735,11 +1763,6 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             const long long d2a_c = d2a > (__int128)INT64_MAX ? INT64_MAX
                                   : (d2a < (__int128)INT64_MIN ? INT64_MIN : (long long)d2a);
             const float fa = i64_to_f32(d2a_c) * R.ring_karea_f[t];
-            if (lane == 0) {
-                const double a2d = fma((double)(long long)(a2 >> 64), 18446744073709551616.0,
-                                       (double)(unsigned long long)a2);
-                C.ring_area[g] = a2d * R.u2_d * 0.5;
-            }
             const float uf = R.u_f;
             const float bxf = i64_to_f32(bx) * uf, byf = i64_to_f32(by) * uf;
             const float L = sqrtf(bxf * bxf + byf * byf);
@@ -1808,7 +1831,6 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) area2 += __shfl_xor_sync(0xffffffffu, area2, o);
     const double area = area2 / 2.0;
-    if (lane == 0) C.ring_area[g] = area;
     const double k_s = rc.k_spring[t], l_s = rc.l_spring[t];
     const double fmod_area = rc.k_area[t] * (area - R.ring_a0sq[t]);
     const double kb = rc.k_bend[t];
@@ -2197,6 +2219,38 @@ static __global__ void k_out_from_cur(Ctx C) {
     if (C.off_out) C.off_out[s] = C.off_cur[s];
 }
 
+// Ring areas on demand (RingsInfo.areas, set by area_forces!,
+// src/rings/integration.jl:140-160): calc_area (:103-116) of the continuous
+// positions (update_continuos_pos!, :118-138: cumulative differences with
+// periodic walls, the positions themselves otherwise) of the last force
+// evaluation (the *_cur state), FP64, summed in particle order.
+static __global__ void k_ring_areas(Ctx C, int64_t ring0, int64_t nrings, double* __restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nrings) return;
+    const int64_t g = ring0 + k;
+    const DevRep& R = C.reps[C.ring_rep[g]];
+    const int32_t rl = (int32_t)(g - R.ring0);
+    const int32_t n = C.rcfg[C.ring_rep[g]].num_particles[C.ring_types[g] - 1];
+    const int32_t u0 = (int32_t)R.slot0 + rl * R.nmax;
+    const double2 c0 = C.pos_cur[C.slot_of[u0]];
+    double2 prev = c0, cprev = c0;
+    double area = 0.0;
+    for (int32_t i = 1; i < n; i++) {
+        const double2 q = C.pos_cur[C.slot_of[u0 + i]];
+        double2 c = q;
+        if (R.periodic) {
+            double dx = q.x - prev.x, dy = q.y - prev.y;
+            if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
+            c = make_double2(cprev.x + dx, cprev.y + dy);
+        }
+        area += cprev.x * c.y - cprev.y * c.x;
+        prev = q;
+        cprev = c;
+    }
+    area += cprev.x * c0.y - cprev.y * c0.x;
+    out[k] = area / 2.0;
+}
+
 static __global__ void k_gather_user(Ctx C, const double2* __restrict__ pos_user, const double2* __restrict__ vel_user,
                               const double* __restrict__ pol_user) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2223,6 +2277,11 @@ __global__ void k_forces_to_user(Ctx C, double2* __restrict__ f_user) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= C.M) return;
     int32_t u = C.uid_cur[s];
+    if (C.pos_u) {   // rings keep the force in user order
+        if constexpr (PREC == kPrecFP64) f_user[u] = C.fd_u[u];
+        else { float2 f = C.ff_u[u]; f_user[u] = make_double2(f.x, f.y); }
+        return;
+    }
     if constexpr (PREC == kPrecFP64) f_user[u] = C.fd[s];
     else { float2 f = C.ff[s]; f_user[u] = make_double2(f.x, f.y); }
 }

@@ -332,6 +332,11 @@ function sync!(system)
     GC.@preserve st check(ccall((:mavi_download_state, libmavi), Cint,
                                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
                                 h, pointer(st.pos), vel, pol), "mavi_download_state", h)
+    if st isa Rings.RingsState
+        # RingsInfo.areas of the last force evaluation
+        check(ccall((:mavi_rings_areas, libmavi), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}),
+                    h, 0, system.info.areas), "mavi_rings_areas", h)
+    end
     if st isa Rings.RingsState && st.rings_ids isa Rings.States.VarRingsIds
         ids = st.rings_ids
         nr = length(ids.mask)

@@ -384,6 +384,14 @@ class RingsSystem(System):
         h.check(h.lib.mavi_rings_sources(h.handle, replica, abi.as_iptr(mask), n, entries, boxes,
                                          abi.as_dptr(spawn_xy), abi.as_iptr(chunk_rc)), "mavi_rings_sources")
 
+    def areas(self) -> np.ndarray:
+        """RingsInfo.areas (src/rings/integration.jl:140-160): ring areas at
+        the last force evaluation."""
+        h = self._ensure()
+        out = np.zeros(self.state.num_rings)
+        h.check(h.lib.mavi_rings_areas(h.handle, 0, abi.as_dptr(out)), "mavi_rings_areas")
+        return out
+
     def rings_ids(self):
         """(active_mask[num_rings] bool, uids[num_rings], num_active) on the
         device (VarRingsIds: mask, uids, num_active)."""

@@ -122,6 +122,9 @@ def test_rings(mg, orc, factory, precision):
     tol = 1e-8 if precision == "fp64" else 1e-3
     assert np.max(np.abs(s.state.pos[active] - p[active])) < tol
     assert np.max(np.abs(s.state.pol - pol)) < tol
+    # RingsInfo.areas: the areas of the last step's force evaluation
+    a, ra = s.areas(), ref.areas(s.state.num_rings)
+    assert np.max(np.abs(a - ra) / np.abs(ra)) < (1e-10 if precision == "fp64" else 1e-5)
     s.close()
 
 
