@@ -27,15 +27,16 @@ static void launch_count(MaviSystem* s) {
 
 // update_chunks! (src/chunks.jl:150-161): chunk lists from the histogram of the
 // *_out state: scan -> scatter -> per-chunk order + permutation into *_cur.
-// The scan clears the counts and the scatter the tile sums, so the histogram
-// of the next step starts from zero without memset launches.
+// The scatter takes the counts back to zero as it hands out the places in
+// each chunk, and clears the tile sums, so the histogram of the next step
+// starts from zero without memset launches.
 static void launch_rebin(MaviSystem* s, bool advance) {
     if (!s->counts_valid) launch_count(s);
     record_begin(s, MAVI_KERNEL_BIN_SCAN);
     if (s->tile_offs)   // many tiles: their offsets first, in one block
         k_tile_offsets<<<1, kTileScanThreads, 0, s->stream>>>(s->C.tile_sum, s->ntiles, s->tile_offs);
     k_scan<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->nscan, s->C.tile_sum, s->C.start,
-                                                               s->C.d_step, advance ? 1 : 0, s->tile_offs);
+                                                               s->C.d_step, advance ? 1 : 0, s->tile_offs, 0);
     record_end(s, MAVI_KERNEL_BIN_SCAN);
     record_begin(s, MAVI_KERNEL_BIN_SCATTER);
     k_scatter<<<nblocks(std::max(s->M, s->ntiles)), kBlock, 0, s->stream>>>(s->C);
@@ -702,7 +703,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         if (s->prec == MAVI_PREC_MIXED) { ALLOC(C.fold_f, M); } else { ALLOC(C.fold_d, M); }
     }
     ALLOC(C.uid_cur, M); ALLOC(C.uid_out, M); ALLOC(C.rep_cur, M); ALLOC(C.rep_out, M);
-    ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.rank, M); ALLOC(C.src_of, M);
+    ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.src_of, M);
     ALLOC(C.key_of, M); ALLOC(C.cell_at, M);
     if (s->ntiles > kScanDirectTiles) ALLOC(s->tile_offs, s->ntiles);
     // no chunk guess before the first histogram

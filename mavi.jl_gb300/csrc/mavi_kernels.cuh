@@ -59,7 +59,7 @@ struct Ctx {
     double2 *fold_d; // Verlet F(t), FP64 form
     float2 *fold_f;  // Verlet F(t), mixed form
     int32_t *uid_cur, *uid_out, *rep_cur, *rep_out;
-    int32_t *cell_cur, *cell_out, *rank;
+    int32_t *cell_cur, *cell_out;
     int32_t *count, *start, *src_of, *slot_of;
     int32_t *key_of, *cell_at;   // per claimed slot: user id and chunk of its particle
     int32_t *rinfo_cur;          // rings: packed ring identity per sorted slot (ring_key), or null
@@ -201,25 +201,20 @@ __device__ __forceinline__ bool edge_chunk(const DevRep& R, int64_t row, int64_t
 // by all 32 lanes of the warp.
 __device__ __forceinline__ void count_into_chunk(const Ctx& C, bool valid, int64_t s, int64_t cell,
                                                  int32_t cap) {
+    // a fire-and-forget add (no rank returned: nothing waits on the atomic);
+    // each particle takes its place in the chunk later, in k_scatter
+    (void)cap;
     const unsigned full = 0xffffffffu;
     int key = valid ? (int)cell : -1;
     unsigned peers = __match_any_sync(full, key);
     int lane = threadIdx.x & 31;
-    int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (valid && lane == leader) base = atomicAdd(&C.count[cell], __popc(peers));
-    base = __shfl_sync(full, base, leader);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&C.count[cell], __popc(peers));
     // scan-tile totals: one atomic per warp and tile (consecutive particles
     // share a tile; per-particle atomics on one address would serialise)
     int tkey = valid ? (int)(cell / kScanTile) : -1;
     unsigned tpeers = __match_any_sync(full, tkey);
     if (valid && lane == __ffs(tpeers) - 1) atomicAdd(&C.tile_sum[tkey], __popc(tpeers));
-    if (valid) {
-        int r = base + __popc(peers & ((1u << lane) - 1u));
-        C.cell_out[s] = (int32_t)cell;
-        C.rank[s] = r;
-        if (r >= cap) raise_error(C.err, MAVI_ERR_CHUNK_OVERFLOW, s, cell);
-    }
+    if (valid) C.cell_out[s] = (int32_t)cell;
 }
 
 // Chunk (and mixed-form offset) of a final position; `guess_cell` is the
@@ -350,10 +345,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total
 }
 
 // Single-kernel exclusive scan: the histogram already accumulated each tile's
-// total, so every block sums the tiles before its own, scans its tile and
-// (clear) zeroes the counts it consumed, so the next histogram starts from
-// zero. (Clearing only the occupied chunks in k_permute instead measured
-// slower on a sparse 14 M-chunk grid: nearly every 32-byte sector holds one.)
+// total, so every block sums the tiles before its own and scans its tile;
+// with clear it zeroes the counts it consumed (the chunk update instead lets
+// k_scatter take them back to zero as it hands out the places).
 // With tile_offs (the exclusive scan of the tile totals, from k_tile_offsets)
 // a block reads its offset instead of summing the totals before it, which
 // grows quadratically with the number of tiles.
@@ -430,15 +424,25 @@ static __global__ void __launch_bounds__(kTileScanThreads) k_tile_offsets(const 
 }
 
 // ===========================================================================
-// scatter: each particle claims start[cell] + rank
+// scatter: each particle claims a place in its chunk. The scan left the
+// counts in place; taking them back down one claim at a time hands out the
+// places 0..count-1 (in no particular order: k_permute orders each chunk) and
+// leaves the counts at zero for the next histogram.
 // ===========================================================================
 static __global__ void k_scatter(Ctx C) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < C.ntiles) C.tile_sum[s] = 0;   // k_scan has consumed the tile sums
     if (s >= C.M) return;
-    int32_t c = C.cell_out[s];
-    int32_t dst = C.start[c] + C.rank[s];
-    // ranks are < count[c] by construction, so dst stays inside [start[c], start[c+1])
+    const int32_t c = C.cell_out[s];
+    const int32_t r = atomicSub(&C.count[c], 1) - 1;
+    const int32_t b = C.start[c];
+    if (r == 0 && c != C.park) {
+        // chunk capacity (src/chunks.jl:32-34; the reference's BoundsError), once per chunk
+        const DevRep& R = C.reps[C.num_reps > 1 ? C.rep_out[s] : 0];
+        if (R.has_chunks && C.start[c + 1] - b > R.cap) raise_error(C.err, MAVI_ERR_CHUNK_OVERFLOW, s, c);
+    }
+    const int32_t dst = b + r;
+    // places are < count[c], so dst stays inside [start[c], start[c+1])
     C.src_of[dst] = (int32_t)s;
     C.key_of[dst] = C.uid_out[s];
     C.cell_at[dst] = c;
