@@ -253,7 +253,12 @@ int mavi_destroy(MaviSystem* sys);
 
 /* Advance every replica `num_steps` steps with the replica's step function
  * (get_step_function, src/integration.jl:537-548; rings src/rings/integration.jl:545),
- * replacing `run_system(system; num_steps)` (src/run_system.jl:7-23). */
+ * replacing `run_system(system; num_steps)` (src/run_system.jl:7-23). The steps
+ * are enqueued on the handle's stream and the call returns without waiting;
+ * a device error of these steps (the reference's BoundsError on a particle
+ * leaving the grid or overfilling a chunk) is returned by the next call that
+ * waits for results (mavi_download_state, mavi_calc_forces, mavi_get_chunks,
+ * mavi_energies, mavi_update_chunks, mavi_rings_*). */
 int mavi_step(MaviSystem* sys, int64_t num_steps);
 
 /* update_chunks! for every replica (src/chunks.jl:150-161). */
@@ -279,7 +284,7 @@ int mavi_calc_forces(MaviSystem* sys, int32_t include_walls, double* forces_out)
  * mavi_upload_state returns once the copy and the chunk histogram of the new
  * state are queued on the handle's stream: from page-locked host memory the
  * copy may still be in flight, so the arrays must not change before the next
- * call on this handle that returns results (mavi_step, mavi_download_state,
+ * call on this handle that waits for results (mavi_download_state,
  * mavi_calc_forces, ...); a state outside the chunk grid is reported by that
  * call. mavi_download_state waits for its copies. */
 int mavi_upload_state(MaviSystem* sys, const double* pos, const double* vel,

@@ -16,12 +16,14 @@ using namespace mavi;
 // ---------------------------------------------------------------------------
 // launch sequences shared by both precisions
 // ---------------------------------------------------------------------------
-static void launch_count(MaviSystem* s) {
+// Histogram of the *_out state; with src, the positions are first gathered
+// from that user-order buffer (an upload).
+static void launch_count(MaviSystem* s, const double2* src = nullptr) {
     record_begin(s, MAVI_KERNEL_BIN_COUNT);
-    cudaMemsetAsync(s->C.count, 0, sizeof(int32_t) * s->nscan, s->stream);
-    cudaMemsetAsync(s->C.tile_sum, 0, sizeof(int32_t) * s->ntiles, s->stream);
-    if (s->prec == MAVI_PREC_FP64) count_fp64(s, 2);
-    else count_mixed(s, 2);
+    k_zero_counts<<<nblocks(std::max(s->nscan, s->ntiles)), kBlock, 0, s->stream>>>(s->C.count, s->nscan,
+                                                                                  s->C.tile_sum, s->ntiles);
+    if (s->prec == MAVI_PREC_FP64) count_fp64(s, 2, src);
+    else count_mixed(s, 2, src);
     record_end(s, MAVI_KERNEL_BIN_COUNT);
 }
 
@@ -866,10 +868,12 @@ int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const
         if (s->prec == MAVI_PREC_MIXED) k_ring_pol<kPrecMixed><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
         else k_ring_pol<kPrecFP64><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 0);
     }
-    k_gather_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, (s->has_vel && vel) ? s->vel_user : nullptr,
-                                                           (s->has_pol && pol) ? s->pol_user : nullptr);
+    const double2* vel_src = (s->has_vel && vel) ? s->vel_user : nullptr;
+    const double* pol_src = (s->has_pol && pol) ? s->pol_user : nullptr;
+    if (vel_src || pol_src)
+        k_gather_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, nullptr, vel_src, pol_src);
     s->counts_valid = false;
-    launch_count(s);
+    launch_count(s, s->pos_user);   // positions gathered inside the histogram
     s->counts_valid = true;
     if (s->var_rings) launch_rebin(s, false);   // chunk lists of the uploaded state
     CUDA_TRY(s, cudaGetLastError());
@@ -963,7 +967,7 @@ int mavi_step(MaviSystem* s, int64_t nsteps) {
         if (s->profiling) s->prof.steps += 1;
     }
     CUDA_TRY(s, cudaGetLastError());
-    return check_device_error(s);
+    return MAVI_OK;   // enqueued: device errors of these steps surface at the next synchronising call
 }
 
 int mavi_update_chunks(MaviSystem* s) {

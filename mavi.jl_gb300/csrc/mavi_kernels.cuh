@@ -284,8 +284,10 @@ __device__ __forceinline__ int64_t bin_fast(const Ctx& C, const DevRep& R, int64
 // the rings step). The guess of the exact binning: use_guess 1 = the slot's
 // chunk in the *_cur order (rings step), 2 = the chunk the slot's particle
 // had at the last histogram (after an upload; -1 before the first one).
+// src != null: the positions are first gathered from the user-order upload
+// buffer into pos_out (an upload's gather fused into its histogram).
 template <int PREC>
-__global__ void k_count(Ctx C, int32_t use_guess) {
+__global__ void k_count(Ctx C, int32_t use_guess, const double2* __restrict__ src) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = s < C.M;
     int64_t cell = 0;
@@ -297,13 +299,19 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
             const int32_t ring = (C.uid_out[s] - (int32_t)R.slot0) / R.nmax;
             parked = C.ring_active[R.ring0 + ring] == 0;
         }
-        const double2 p = C.pos_out[s];
-        const int32_t uw = C.pos_u ? C.uid_out[s] : -1;   // rings: the user-order copy too
+        const int32_t us = (src || C.pos_u) ? C.uid_out[s] : -1;
+        const double2 p = src ? src[us] : C.pos_out[s];
+        if (src) C.pos_out[s] = p;
+        const int32_t uw = C.pos_u ? us : -1;   // rings: the user-order copy too
         if (parked) {
             cell = C.park;
         } else {
-            const int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
-            cell = bin_final<PREC>(C, R, s, p.x, p.y, (guess == C.park && C.var_rings) ? -1 : guess, uw);
+            int64_t guess = use_guess == 1 ? (int64_t)C.cell_cur[s] : (use_guess == 2 ? (int64_t)C.cell_out[s] : -1);
+            if (guess == C.park) guess = -1;
+            // the fixed-point fast path first (a guess is the particle's chunk at
+            // the last histogram), the exact Julia formula when it cannot decide
+            cell = guess >= 0 ? bin_fast<PREC>(C, R, s, p.x, p.y, (int32_t)guess, uw) : -1;
+            if (cell < 0) cell = bin_final<PREC>(C, R, s, p.x, p.y, guess, uw);
             cap = R.has_chunks ? R.cap : (1 << 30);
         }
         if (uw >= 0) {
@@ -312,6 +320,15 @@ __global__ void k_count(Ctx C, int32_t use_guess) {
         }
     }
     count_into_chunk(C, valid, s, cell, cap);
+}
+
+// Chunk counts and scan-tile totals to zero in one launch (a histogram
+// replaced before a chunk update consumed it, e.g. by an upload).
+static __global__ void k_zero_counts(int32_t* __restrict__ count, int64_t n, int32_t* __restrict__ tile_sum,
+                                     int64_t ntiles) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) count[i] = 0;
+    if (i < ntiles) tile_sum[i] = 0;
 }
 
 // ===========================================================================
@@ -2260,7 +2277,7 @@ static __global__ void k_gather_user(Ctx C, const double2* __restrict__ pos_user
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= C.M) return;
     int32_t u = C.uid_out[s];
-    C.pos_out[s] = pos_user[u];
+    if (pos_user) C.pos_out[s] = pos_user[u];
     if (vel_user) C.vel_out[s] = vel_user[u];
     if (pol_user) C.pol_out[s] = pol_user[u];
 }

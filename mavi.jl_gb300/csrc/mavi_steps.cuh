@@ -17,8 +17,8 @@ void sort_permute(MaviSystem* s) {
 }
 
 template <int PREC>
-void count(MaviSystem* s, int use_guess) {
-    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, use_guess);
+void count(MaviSystem* s, int use_guess, const double2* src) {
+    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, use_guess, src);
 }
 
 template <int PREC, int DYN, int PASS>
@@ -111,7 +111,7 @@ void forces_only(MaviSystem* s, int with_walls) {
 template <int PREC>
 void sources(MaviSystem* s) {
     k_sources<PREC><<<(unsigned)s->R, kSrcThreads, 0, s->stream>>>(s->C);
-    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, 1);
+    k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, 1, nullptr);
 }
 
 template <int PREC>
@@ -125,7 +125,7 @@ void forces_to_user(MaviSystem* s) {
 #define MAVI_DEFINE_STEPS(SUFFIX, PREC)                                                      \
     namespace mavi {                                                                         \
     void sort_permute_##SUFFIX(MaviSystem* s) { steps::sort_permute<PREC>(s); }              \
-    void count_##SUFFIX(MaviSystem* s, int g) { steps::count<PREC>(s, g); }                  \
+    void count_##SUFFIX(MaviSystem* s, int g, const double2* src) { steps::count<PREC>(s, g, src); } \
     void step_body_##SUFFIX(MaviSystem* s) { steps::step_body_dispatch<PREC>(s); }           \
     void forces_only_##SUFFIX(MaviSystem* s, int w) { steps::forces_only<PREC>(s, w); }      \
     void rings_terms_##SUFFIX(MaviSystem* s, int u) { steps::rings_terms<PREC>(s, u); }      \

@@ -160,8 +160,8 @@ inline void collect_step_time(MaviSystem* s, int used) {
 
 // Per-precision launch sequences (mavi_steps_fp64.cu / mavi_steps_mixed.cu).
 void sort_permute_fp64(MaviSystem* s);
-void count_fp64(MaviSystem* s, int use_guess);
-void count_mixed(MaviSystem* s, int use_guess);
+void count_fp64(MaviSystem* s, int use_guess, const double2* src);
+void count_mixed(MaviSystem* s, int use_guess, const double2* src);
 void sort_permute_mixed(MaviSystem* s);
 void step_body_fp64(MaviSystem* s);
 void step_body_mixed(MaviSystem* s);
