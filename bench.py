@@ -259,22 +259,23 @@ def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
         if step_kind == abi.MAVI_STEP_NEWTON:
             # pass 1: r x, v, uid, rep, cell, (off) ; w x', F(t), (off')
             p1 = (16 + 16 + 4 + 4 + 4 + off) + (16 + (8 if mixed else 16) + off)
-            # pass 2: r x', v, F(t), (off') ; w x, v, uid, rep, cell, rank, (off)
-            p2 = (16 + 16 + (8 if mixed else 16) + 4 + 4 + 4 + off) + (16 + 16 + 4 + 4 + 4 + 4 + off)
+            # pass 2: r x', v, F(t), (off') ; w x, v, uid, rep, cell, (off)
+            p2 = (16 + 16 + (8 if mixed else 16) + 4 + 4 + 4 + off) + (16 + 16 + 4 + 4 + 4 + off)
             return p1 + p2
-        # final pass: r x, (v), uid, rep, cell, (off); w x, (v), uid, rep, cell, rank, (off)
-        return (16 + vel + 4 + 4 + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
+        # final pass: r x, (v), uid, rep, cell, (off); w x, (v), uid, rep, cell, (off)
+        return (16 + vel + 4 + 4 + 4 + off) + (16 + vel + 4 + 4 + 4 + off)
     if kind == "bin_sort":
         # r src_of, cell_at, key_of, x, (v), rep, (off); w x, (v), uid, rep, cell, slot_of, (off)
         return (4 + 4 + 4 + 16 + vel + 4 + off) + (16 + vel + 4 + 4 + 4 + 4 + off)
     if kind == "bin_scatter":
-        return 4 + 4 + 4 + 4 + 4 + 4   # r cell, rank, uid; w src_of, key_of, cell_at
+        return 4 + 4 + 4 + 4 + 4       # r cell, uid; w src_of, key_of, cell_at (the count atomics hit L2)
     if kind == "bin_scan":
         return 0                  # per chunk, not per particle (counted in the chunk term)
     if kind == "update" and step_kind == abi.MAVI_STEP_RINGS:
-        # k_rings: r slot_of, x, (off), cell, F, uid; w x', (off'), uid, rep, cell, rank
+        # k_rings, user order: r slot_of, x, (off), cell, F; w x', (off'), cell' (user order
+        # copy) and x', (off'), uid, rep, cell (sorted order, for the chunk update)
         f = 8 if mixed else 16
-        return (4 + 16 + off + 4 + f + 4) + (16 + off + 4 + 4 + 4 + 4)
+        return (4 + 16 + off + 4 + f) + (16 + off + 4) + (16 + off + 4 + 4 + 4)
     return 0
 
 

@@ -302,6 +302,17 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
             // margins far above the float rounding of the test (relative 1e-7)
             R.wall_lo2_u = (float)(lo * R.inv_u * lo * R.inv_u * (1.0 - 1e-4));
             R.wall_hi2_u = (float)(hi * R.inv_u * hi * R.inv_u * (1.0 + 1e-4));
+            // the FP32 wall force of the mixed form: radius^2 in units^2 as an
+            // integer (its rounding, <= 0.5 units^2, moves the wall by ~1e-11 units)
+            const long double Ru = (long double)sp.radius * (long double)R.inv_u;
+            const __int128 R2 = (__int128)(Ru * Ru + 0.5L);
+            R.wall_R2_hi = (long long)(R2 >> 64);
+            R.wall_R2_lo = (unsigned long long)R2;
+            R.wall_Ru_f = (float)Ru;
+            R.wall_krep_f = (float)sp.pot_params[0];
+            R.wall_katr_f = (float)sp.pot_params[1];
+            R.wall_deq_f = (float)sp.pot_params[2];
+            R.wall_dmax_f = (float)sp.pot_params[3];
         }
     }
     R.sx_u = std::llround(R.chunk_l / u);
@@ -1017,8 +1028,8 @@ int mavi_calc_forces(MaviSystem* s, int32_t include_walls, double* forces_out) {
     if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, include_walls);
     else forces_only_mixed(s, include_walls);
     if (s->is_rings) {
-        if (s->prec == MAVI_PREC_FP64) rings_terms_fp64(s, 0);
-        else rings_terms_mixed(s, 0);
+        if (s->prec == MAVI_PREC_FP64) rings_terms_fp64(s, 0, include_walls);
+        else rings_terms_mixed(s, 0, include_walls);
     }
     CUDA_TRY(s, cudaMemsetAsync(s->f_user, 0, sizeof(double2) * s->Nslots, s->stream));
     if (s->prec == MAVI_PREC_FP64) forces_to_user_fp64(s);

@@ -59,6 +59,11 @@ struct DevRep {
     int32_t rows, cols, cap, periodic; // chunk grid; periodic stencil
     int32_t has_chunks;
     int32_t num_rings, nmax;
+    // mixed-form circle wall force (the pre-checked PotentialWalls circle):
+    // radius^2 in units^2 (128-bit) and in units, HarmTrunc constants
+    long long wall_R2_hi;
+    unsigned long long wall_R2_lo;
+    float wall_Ru_f, wall_krep_f, wall_katr_f, wall_deq_f, wall_dmax_f, _wall_pad;
     // sources and sinks of the rings model: entries [src_e0, src_e0 + src_ne)
     int32_t src_e0, src_ne, src_has_sink, _src_pad;
     int32_t min_image;     // first space is PeriodicWalls on a RectangleCfg

@@ -1293,6 +1293,31 @@ __device__ __forceinline__ double proc_dist(int mode, double dist, double flag) 
     return dist;
 }
 
+// Mixed form: the force of the pre-checked PotentialWalls circle (truncated
+// harmonic potential; inside or repulsion mode) on a particle at the exact
+// integer displacement (wx, wy) from the centre, in FP32. signed_pos
+// (src/configs.jl:154-163) gives dist - R and the wall vector dr (1 - R/dist);
+// dist - R comes from the exact integer r^2 - R^2 divided by (dist + R), so it
+// keeps FP32 relative accuracy next to the wall; process_dist and
+// potential_force (src/configs.jl:259-261, 354-368) follow.
+__device__ __forceinline__ void wall_circle_f32(const DevRep& R, long long wx, long long wy, float wxf, float wyf,
+                                                float& fx, float& fy) {
+    const __int128 r2 = (__int128)wx * wx + (__int128)wy * wy;
+    const __int128 R2 = (__int128)(((unsigned __int128)(unsigned long long)R.wall_R2_hi << 64) | R.wall_R2_lo);
+    const __int128 dd = r2 - R2;
+    const long long d64 = dd > (__int128)INT64_MAX ? INT64_MAX : (dd < (__int128)INT64_MIN ? INT64_MIN : (long long)dd);
+    const float dist_u = sqrtf(fmaf(wxf, wxf, wyf * wyf));
+    const float sd_u = i64_to_f32(d64) / (dist_u + R.wall_Ru_f);    // dist - R, units
+    const float sd = sd_u * R.u_f;
+    const float d = R.wall_precheck == 1 ? -sd : fabsf(sd);         // inside: -(dist - R)
+    if (d > R.wall_dmax_f) return;
+    const float k = d < R.wall_deq_f ? R.wall_krep_f : R.wall_katr_f;
+    const float fm = -k * (d / R.wall_deq_f - 1.0f);
+    const float sc = fm / d * (sd_u / dist_u) * R.u_f;              // times dr (units -> length)
+    fx += sc * wxf;
+    fy += sc * wyf;
+}
+
 static __device__ __forceinline__ void add_wall_forces(const Ctx& C, int32_t rep, const DevRep& R, double x, double y,
                                 double& fx, double& fy) {
     const MaviSpace* sps = C.spaces + (int64_t)rep * MAVI_MAX_SPACES;
@@ -1636,7 +1661,8 @@ __device__ __forceinline__ void ring_vc_store(const Ctx& C, int64_t g, int lane,
 #endif
 template <int PREC>
 __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_rings(Ctx C, int64_t total_rings,
-                                                                                 int32_t do_update) {
+                                                                                 int32_t do_update,
+                                                                                 int32_t with_walls) {
     __shared__ double2 sp_[kRingWarps][kRingMax];
     __shared__ int32_t ss_[kRingWarps][kRingMax];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1697,7 +1723,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         const int32_t s = S[p], u = u0 + p;
         if constexpr (PREC == kPrecFP64) { double2 f = C.fd_u[u]; fx += f.x; fy += f.y; }
         else { float2 f = C.ff_u[u]; fx += f.x; fy += f.y; }
-        if (R.has_wall_forces && near_wall) {
+        if (R.has_wall_forces && near_wall && with_walls) {
             double wx = 0.0, wy = 0.0;
             add_wall_forces(C, rep, R, xc.x, xc.y, wx, wy);
             fx += (V)wx;
@@ -1808,12 +1834,17 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
                 fx += kbt * (dcax - dcbx) - kbt * nax + kbt * pbx;
                 fy += kbt * (dcay - dcby) - kbt * nay + kbt * pby;
             }
-            // PotentialWalls circle: float test in units, exact FP64 only near the wall
+            // PotentialWalls circle: float test in units, then the wall force in
+            // FP32 on the exact integer displacement (the FP64 one, with its
+            // square root and divisions, was most of this kernel's FP64 work)
             bool near_wall = true;
             if (R.wall_precheck) {
-                const float wx = i64_to_f32(X - R.wall_cx_u), wy = i64_to_f32(Y - R.wall_cy_u);
+                const long long wxl = X - R.wall_cx_u, wyl = Y - R.wall_cy_u;
+                const float wx = i64_to_f32(wxl), wy = i64_to_f32(wyl);
                 const float r2 = fmaf(wx, wx, wy * wy);
                 near_wall = !(r2 < R.wall_lo2_u) && !(R.wall_precheck == 2 && r2 > R.wall_hi2_u);
+                if (near_wall && act && with_walls) wall_circle_f32(R, wxl, wyl, wx, wy, fx, fy);
+                near_wall = false;
             }
             int64_t nc = 0;
             if (act) nc = finish(p, P[p], fx, fy, near_wall);

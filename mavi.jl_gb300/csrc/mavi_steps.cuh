@@ -29,10 +29,11 @@ void pass(MaviSystem* s, int with_walls) {
     else k_pass<PREC, DYN, PASS, false, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
 }
 
+// with_walls: calc_walls_forces! (the step always includes it)
 template <int PREC>
-void rings_terms(MaviSystem* s, int do_update) {
+void rings_terms(MaviSystem* s, int do_update, int with_walls) {
     unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
-    k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update);
+    k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
     if (do_update) k_ring_pol<PREC><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
 }
 
@@ -75,7 +76,7 @@ void step_body(MaviSystem* s) {
             pass<PREC, DYN, kPassForce>(s, 0);
             record_end(s, MAVI_KERNEL_FORCE);
             record_begin(s, MAVI_KERNEL_UPDATE);
-            rings_terms<PREC>(s, 1);    // ring terms, update, walls, binning and the histogram
+            rings_terms<PREC>(s, 1, 1);    // ring terms, wall forces, update, walls, binning, histogram
             record_end(s, MAVI_KERNEL_UPDATE);
         }
         break;
@@ -128,7 +129,7 @@ void forces_to_user(MaviSystem* s) {
     void count_##SUFFIX(MaviSystem* s, int g, const double2* src) { steps::count<PREC>(s, g, src); } \
     void step_body_##SUFFIX(MaviSystem* s) { steps::step_body_dispatch<PREC>(s); }           \
     void forces_only_##SUFFIX(MaviSystem* s, int w) { steps::forces_only<PREC>(s, w); }      \
-    void rings_terms_##SUFFIX(MaviSystem* s, int u) { steps::rings_terms<PREC>(s, u); }      \
+    void rings_terms_##SUFFIX(MaviSystem* s, int u, int w) { steps::rings_terms<PREC>(s, u, w); } \
     void forces_to_user_##SUFFIX(MaviSystem* s) { steps::forces_to_user<PREC>(s); }          \
     void sources_##SUFFIX(MaviSystem* s) { steps::sources<PREC>(s); }                        \
     }

@@ -167,8 +167,8 @@ void step_body_fp64(MaviSystem* s);
 void step_body_mixed(MaviSystem* s);
 void forces_only_fp64(MaviSystem* s, int with_walls);
 void forces_only_mixed(MaviSystem* s, int with_walls);
-void rings_terms_fp64(MaviSystem* s, int do_update);
-void rings_terms_mixed(MaviSystem* s, int do_update);
+void rings_terms_fp64(MaviSystem* s, int do_update, int with_walls);
+void rings_terms_mixed(MaviSystem* s, int do_update, int with_walls);
 void forces_to_user_fp64(MaviSystem* s);
 void forces_to_user_mixed(MaviSystem* s);
 void sources_fp64(MaviSystem* s);

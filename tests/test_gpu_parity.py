@@ -388,6 +388,39 @@ def test_rings_in_circular_container(mg, orc, precision):
     s.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rings_container_wall_forces(mg, orc, precision):
+    """Rings pressed against the PotentialWalls circle: calc_walls_forces!
+    appears in the forces only when asked for (the step always includes it),
+    and matches the oracle (the mixed form evaluates it in FP32 on the exact
+    integer displacement from the centre)."""
+    from mavi_gb300 import workloads
+    systems, _ = workloads.rings_batch(num_replicas=1, rings_min=80, rings_max=80, precision=precision)
+    s = systems[0]
+    s.int_cfg.device.noise = "injected"
+    st = s.state
+    Rc = s.space_cfg.geometry_cfg.radius
+    cms = st.rings_pos.mean(axis=1)
+    # move the three outermost rings outwards until their outer particles sit
+    # 0.1-0.3 inside the circle (the wall potential reaches 0.5 in)
+    for q in np.argsort(-np.hypot(cms[:, 0], cms[:, 1]))[:3]:
+        c = cms[q] / np.hypot(*cms[q])
+        far = (st.rings_pos[q] @ c).max()
+        st.rings_pos[q] += c * (Rc - 0.1 - 0.2 * (q % 2) - far)
+    ref = orc.from_system(s)
+    fw, f = s.calc_forces(include_walls=True), s.calc_forces(include_walls=False)
+    rw, r = ref.forces(include_walls=True), ref.forces(include_walls=False)
+    touched = np.hypot(*(rw - r).T) > 0
+    assert touched.sum() >= 3
+    assert np.array_equal(np.hypot(*(fw - f).T) > 0, touched)
+    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_force_err(f, r) < tol and rel_force_err(fw, rw) < tol
+    # the wall term itself, against its own scale
+    assert rel_force_err(fw - f, rw - r) < (1e-12 if precision == "fp64" else 1e-5)
+    ref.close()
+    s.close()
+
+
 @pytest.mark.parametrize("kind,potential", [("slippery", None), ("potential", "harm"), ("potential", "lj")])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_line_walls(mg, orc, kind, potential, precision):
