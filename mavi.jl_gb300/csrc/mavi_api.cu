@@ -287,6 +287,10 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
     R.u_f = (float)u;
     R.u2_f = (float)(u * u);
     R.u2_d = u * u;
+    // centre of chunk (0, 0): the origin of the integer coordinates
+    // (col * sx + offset, -row * sy + offset) in units
+    R.cx0 = R.bb_blx + 0.5 * R.chunk_l;
+    R.cy0 = R.bb_bly + R.bb_h - 0.5 * R.chunk_h;
     // float pre-check of a single PotentialWalls circle with the truncated
     // harmonic potential (the wall force vanishes away from the circle)
     R.wall_precheck = 0;
@@ -325,8 +329,6 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
     R.sy_i = (int32_t)R.sy_u;
     R.half_sx_i = R.sx_i / 2;
     R.half_sy_i = R.sy_i / 2;
-    R.cx0 = R.bb_blx + 0.5 * R.chunk_l;
-    R.cy0 = R.bb_bly + R.bb_h - 0.5 * R.chunk_h;
     // the minimum image only matters for |dr| > L/2 with dr <= ~2 chunks,
     // i.e. grids of < 6 chunks per side, whose box fits int32 units
     const long long lim = (1ll << 31) - 1;
