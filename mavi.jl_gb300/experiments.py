@@ -62,6 +62,10 @@ def _snapshot(system):
         v = getattr(st, name, None)
         if isinstance(v, np.ndarray):
             snap[name] = v.copy()
+    if getattr(system, "variable_rings", False):
+        # which rings are active (the rings serializer keeps the mask and
+        # rebuilds the ids on load, src/rings/serder.jl:85)
+        snap["active_mask"] = system.rings_ids()[0].astype(np.int8)
     return snap
 
 
@@ -86,6 +90,9 @@ def _restore(system, snap):
     for name in ("vel", "pol", "pol_angle", "rings_pos"):
         if name in snap and isinstance(getattr(st, name, None), np.ndarray):
             getattr(st, name)[...] = snap[name]
+    if "active_mask" in snap:
+        from .rings import ActiveState
+        st.active_state = ActiveState(np.asarray(snap["active_mask"]).astype(bool))
     system.time_info.time = snap["time"]
     system.time_info.num_steps = snap["num_steps"]
 

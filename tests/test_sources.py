@@ -264,3 +264,26 @@ def test_sources_with_device_noise_run(mg):
     s.run(300)
     m, u, na = s.rings_ids()
     assert na >= 20 and u.max() >= 38 and m.sum() == na
+
+
+@pytest.mark.gpu
+def test_experiment_checkpoint_keeps_the_active_rings(mg, tmp_path):
+    """A checkpoint of a system with sources and sinks keeps which rings are
+    active; a resumed run starts from that mask."""
+    ex = mg.experiments
+    s = channel(mg, random_pol=False)
+    s.int_cfg.device.noise = "device"
+    exp = ex.Experiment(ex.ExperimentCfg(tf=2.0, root=str(tmp_path / "a"), checkpoint_cfg=ex.CheckpointCfg(1.0)),
+                        ex.DelayedCfg(0.5), s)
+    ex.run_experiment(exp)
+    s.close()
+    s2 = channel(mg, random_pol=False)
+    s2.int_cfg.device.noise = "device"
+    ex.load_experiment(tmp_path / "a", s2, ex.DelayedCfg(0.5))
+    import json
+    info = json.loads((tmp_path / "a" / "checkpoint" / "checkpoint_info.json").read_text())
+    saved = np.load(tmp_path / "a" / "checkpoint" / info["last_used"] / "sys_state" / "state.npz")["active_mask"]
+    m, _, na = s2.rings_ids()
+    assert np.array_equal(m, saved.astype(bool)) and na == int(saved.sum())
+    assert not m[30:36].any()            # the sink had removed the right column
+    s2.close()
