@@ -287,3 +287,42 @@ def test_experiment_checkpoint_keeps_the_active_rings(mg, tmp_path):
     assert np.array_equal(m, saved.astype(bool)) and na == int(saved.sum())
     assert not m[30:36].any()            # the sink had removed the right column
     s2.close()
+
+
+@pytest.mark.gpu
+def test_sources_in_a_batch_of_replicas(mg, orc):
+    """Two replicas with sources and sinks in one handle: each replica's head
+    of step runs in its own block; the step's noise holds every replica's
+    ring normals first, then every replica's spawn uniforms."""
+    a = channel(mg, random_pol=True)
+    b = channel(mg, random_pol=True)
+    b.state.pol[:] = 0.4                                     # the second replica drifts another way
+    batch = mg.SystemBatch([a, b], device=mg.CUDADevice(precision="fp64", noise="injected"))
+    oa, ob = orc.from_system(a), orc.from_system(b)
+    nr = a.state.num_rings
+    rng = np.random.default_rng(21)
+    for _ in range(4):
+        k = 100
+        za = rng.standard_normal((k, nr + 1))
+        zb = rng.standard_normal((k, nr + 1))
+        za[:, nr] = rng.random(k)
+        zb[:, nr] = rng.random(k)
+        # batch layout per step: [a rings][b rings][a spawn][b spawn]
+        z = np.concatenate([za[:, :nr], zb[:, :nr], za[:, nr:], zb[:, nr:]], axis=1).reshape(-1)
+        batch.run(k, noise=z)
+        oa.step(k, orc.SEQUENTIAL, za.reshape(-1))
+        ob.step(k, orc.SEQUENTIAL, zb.reshape(-1))
+        for s_, o in ((a, oa), (b, ob)):
+            pos, _, pol = o.state()
+            assert np.max(np.abs(s_.state.pos - pos)) < 1e-8
+            assert np.max(np.abs(s_.state.pol - pol)) < 1e-8
+    h = batch.handle
+    import ctypes as C
+    for r, o in enumerate((oa, ob)):
+        m = np.zeros(nr, dtype=np.int32)
+        u = np.zeros(nr, dtype=np.int32)
+        na = C.c_int32()
+        h.check(h.lib.mavi_rings_active(h.handle, r, mg.abi.as_iptr(m), mg.abi.as_iptr(u), C.byref(na)), "active")
+        mo, uo, nao = o.rings_ids()
+        assert np.array_equal(m.astype(bool), mo) and np.array_equal(u, uo) and na.value == nao
+    batch.close()
