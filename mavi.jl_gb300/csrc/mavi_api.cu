@@ -35,8 +35,9 @@ static void launch_count(MaviSystem* s, const double2* src = nullptr) {
 static void launch_rebin(MaviSystem* s, bool advance) {
     if (!s->counts_valid) launch_count(s);
     record_begin(s, MAVI_KERNEL_BIN_SCAN);
-    if (s->tile_offs)   // many tiles: their offsets first, in one block
-        k_tile_offsets<<<1, kTileScanThreads, 0, s->stream>>>(s->C.tile_sum, s->ntiles, s->tile_offs);
+    if (s->tile_offs)   // many tiles: their offsets inside groups of tiles first, a block per group
+        k_tile_offsets<<<(unsigned)((s->ntiles + kTileScanThreads - 1) / kTileScanThreads), kTileScanThreads, 0,
+                         s->stream>>>(s->C.tile_sum, s->ntiles, s->tile_offs);
     k_scan<<<(unsigned)s->ntiles, kScanThreads, 0, s->stream>>>(s->C.count, s->nscan, s->C.tile_sum, s->C.start,
                                                                s->C.d_step, advance ? 1 : 0, s->tile_offs, 0);
     record_end(s, MAVI_KERNEL_BIN_SCAN);
@@ -720,7 +721,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     ALLOC(C.uid_cur, M); ALLOC(C.uid_out, M); ALLOC(C.rep_cur, M); ALLOC(C.rep_out, M);
     ALLOC(C.cell_cur, M); ALLOC(C.cell_out, M); ALLOC(C.src_of, M);
     ALLOC(C.key_of, M); ALLOC(C.cell_at, M);
-    if (s->ntiles > kScanDirectTiles) ALLOC(s->tile_offs, s->ntiles);
+    if (s->ntiles > kScanDirectTiles)   // offsets inside groups + one total per group
+        ALLOC(s->tile_offs, s->ntiles + (s->ntiles + kTileScanThreads - 1) / kTileScanThreads);
     // no chunk guess before the first histogram
     if (cudaMemset(C.cell_out, 0xff, sizeof(int32_t) * M) != cudaSuccess)
         return bail(fail(s, MAVI_ERR_CUDA, "cudaMemset failed for cell_out"));

@@ -33,6 +33,7 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;                          // one int4 per thread
 constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
 constexpr int64_t kScanDirectTiles = 512;  // above this, tile offsets come from k_tile_offsets
+constexpr int kTileScanThreads = 1024;     // tiles per group of k_tile_offsets
 constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
 
 // Fixed-point parameters of the pair laws of one (type, type) pair, in units
@@ -365,16 +366,22 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total
 // total, so every block sums the tiles before its own and scans its tile;
 // with clear it zeroes the counts it consumed (the chunk update instead lets
 // k_scatter take them back to zero as it hands out the places).
-// With tile_offs (the exclusive scan of the tile totals, from k_tile_offsets)
-// a block reads its offset instead of summing the totals before it, which
-// grows quadratically with the number of tiles.
+// With tile_offs (each tile's offset inside its group of kTileScanThreads
+// tiles, and at tile_offs[ntiles + g] the total of group g, from
+// k_tile_offsets) a block adds the totals of the groups before its own to its
+// offset instead of summing every tile before it, which grows quadratically
+// with the number of tiles.
 static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int32_t* __restrict__ tile_sum,
                               int32_t* __restrict__ start, int64_t* d_step, int32_t advance,
                               const int32_t* __restrict__ tile_offs = nullptr, int32_t clear = 1) {
     __shared__ int smem[32];
     int tile_off;
     if (tile_offs) {
-        tile_off = tile_offs[blockIdx.x];
+        const int64_t ntiles = gridDim.x, grp = (int64_t)blockIdx.x / kTileScanThreads;
+        int pre = 0;
+        for (int64_t gi = threadIdx.x; gi < grp; gi += blockDim.x) pre += tile_offs[ntiles + gi];
+        block_exclusive_scan(pre, smem, tile_off);
+        tile_off += tile_offs[blockIdx.x];
     } else {
         int pre = 0;
         for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
@@ -411,33 +418,19 @@ static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int3
     }
 }
 
-// Exclusive scan of the tile totals in one block (grids with many tiles):
-// each thread takes kTileScanItems consecutive totals per round.
-constexpr int kTileScanThreads = 1024;
-constexpr int kTileScanItems = 16;
+// Offsets of the tile totals inside groups of kTileScanThreads tiles, one
+// block per group (grids with many tiles): tile_offs[t] = exclusive scan
+// within the group, tile_offs[ntiles + g] = the group's total.
 static __global__ void __launch_bounds__(kTileScanThreads) k_tile_offsets(const int32_t* __restrict__ tile_sum,
                                                                           int64_t ntiles,
                                                                           int32_t* __restrict__ tile_offs) {
     __shared__ int smem[32];
-    int carry = 0;
-    for (int64_t b0 = 0; b0 < ntiles; b0 += (int64_t)kTileScanThreads * kTileScanItems) {
-        const int64_t t0 = b0 + (int64_t)threadIdx.x * kTileScanItems;
-        int v[kTileScanItems];
-        int sum = 0;
-#pragma unroll
-        for (int k = 0; k < kTileScanItems; k++) {
-            v[k] = (t0 + k < ntiles) ? tile_sum[t0 + k] : 0;
-            sum += v[k];
-        }
-        int total;
-        int ex = block_exclusive_scan(sum, smem, total) + carry;
-#pragma unroll
-        for (int k = 0; k < kTileScanItems; k++) {
-            if (t0 + k < ntiles) tile_offs[t0 + k] = ex;
-            ex += v[k];
-        }
-        carry += total;
-    }
+    const int64_t t = (int64_t)blockIdx.x * kTileScanThreads + threadIdx.x;
+    const int v = t < ntiles ? tile_sum[t] : 0;
+    int total;
+    const int ex = block_exclusive_scan(v, smem, total);
+    if (t < ntiles) tile_offs[t] = ex;
+    if (threadIdx.x == 0) tile_offs[ntiles + blockIdx.x] = total;
 }
 
 // ===========================================================================
