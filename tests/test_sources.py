@@ -326,3 +326,43 @@ def test_sources_in_a_batch_of_replicas(mg, orc):
         mo, uo, nao = o.rings_ids()
         assert np.array_equal(m.astype(bool), mo) and np.array_equal(u, uo) and na.value == nao
     batch.close()
+
+
+# ---------------------------------------------------------------------------
+# host encoding for mavi_rings_sources (no GPU)
+# ---------------------------------------------------------------------------
+def test_sources_abi_encoding(mg, orc):
+    R = mg.rings
+    s = channel(mg, random_pol=True)
+    s.source_cfg.append(R.SinkCfg(mg.CircleCfg(2.0, (5.0, 6.0))))
+    mask, n, entries, boxes, spawn_xy, chunk_rc = s.sources_abi()
+    abi = mg.abi
+    assert n == 4 and mask.dtype == np.int32 and mask.sum() == 30
+    kinds = [entries[k].kind for k in range(n)]
+    assert kinds == [abi.MAVI_SRC_SINK, abi.MAVI_SRC_SOURCE, abi.MAVI_SRC_SOURCE, abi.MAVI_SRC_SINK]
+    assert entries[0].geometry == abi.MAVI_GEOM_RECTANGLE and entries[3].geometry == abi.MAVI_GEOM_CIRCLE
+    assert (entries[3].radius, entries[3].cx, entries[3].cy) == (2.0, 5.0, 6.0)
+    assert entries[1].pol_mode == abi.MAVI_SPAWN_POL_FIXED and entries[2].pol_mode == abi.MAVI_SPAWN_POL_RANDOM
+    assert entries[1].num_boxes == 1 and entries[2].num_boxes == 1
+    # one spawn template of nmax points per box, the boxes' chunk lists concatenated
+    assert spawn_xy.size == 2 * 2 * s.state.nmax
+    assert chunk_rc.size == 2 * (boxes[0].num_chunks + boxes[1].num_chunks)
+    # the oracle takes the same encoding; its step noise grows by the random box
+    o = orc.from_system(s)
+    assert o.noise_count() == s.state.num_rings + 1
+
+
+def test_sources_reject_bad_configuration(mg):
+    R = mg.rings
+    s = rings_normal(mg)
+    with pytest.raises(ValueError):
+        R.RingsSystem(s.state, s.space_cfg, s.dynamic_cfg, s.int_cfg,
+                      source_cfg=R.SourceCfg(bottom_left=(0.0, 0.0), spawn_pos=np.zeros((3, 2))))
+    with pytest.raises(ValueError):
+        R.RingsSystem(s.state, s.space_cfg, s.dynamic_cfg, s.int_cfg, source_cfg="not a source")
+    with pytest.raises(ValueError):
+        R.ActiveState(np.ones(5, bool)).get_active_mask(36)
+    bad = rings_normal(mg)
+    bad.source_cfg = [R.SourceCfg(bottom_left=(1.0, 1.0), spawn_pos=bad.state.rings_pos[14].copy(), spawn_pol="spin")]
+    with pytest.raises(ValueError):
+        bad.sources_abi()
