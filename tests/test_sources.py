@@ -366,3 +366,49 @@ def test_sources_reject_bad_configuration(mg):
     bad.source_cfg = [R.SourceCfg(bottom_left=(1.0, 1.0), spawn_pos=bad.state.rings_pos[14].copy(), spawn_pol="spin")]
     with pytest.raises(ValueError):
         bad.sources_abi()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sources_in_the_circular_container(mg, orc, precision):
+    """Sources and sinks with the PotentialWalls circle of the rings workloads
+    (no minimum image; the mixed form's integer ring geometry and FP32 wall
+    force) and a quarter of the rings parked at the start."""
+    from mavi_gb300 import workloads
+    R = mg.rings
+    systems, _ = workloads.rings_batch(num_replicas=1, rings_min=80, rings_max=80, precision=precision)
+    s = systems[0]
+    s.int_cfg.device.noise = "injected"
+    st = s.state
+    nr = st.num_rings
+    cms = st.rings_pos.mean(axis=1)
+    mask = np.ones(nr, bool)
+    mask[::4] = False
+    st.active_state = R.ActiveState(mask)
+    q = int(np.argmin(np.hypot(cms[:, 0], cms[:, 1])))          # the most central ring, parked
+    mask[q] = False
+    tpl = st.rings_pos[q]
+    pad = 0.05
+    src = R.SourceCfg(bottom_left=(tpl[:, 0].min() - pad, tpl[:, 1].min() - pad), spawn_pos=tpl.copy(),
+                      spawn_pol=0.7, pad=pad)
+    far = int(np.argmax(cms[:, 0]))
+    sink = R.SinkCfg(mg.CircleCfg(6.0, (float(cms[far, 0]), float(cms[far, 1]))))
+    s.source_cfg = [src, sink]
+    o = orc.from_system(s)
+    rng = np.random.default_rng(31)
+    tol = 1e-8 if precision == "fp64" else 1e-3
+    for _ in range(2):
+        z = rng.standard_normal(o.noise_count() * 100)
+        s.run(100, noise=z)
+        o.step(100, orc.SEQUENTIAL, z)
+        m, u, na = s.rings_ids()
+        mo, uo, nao = o.rings_ids()
+        assert np.array_equal(m, mo) and np.array_equal(u, uo) and na == nao
+        pos, _, pol = o.state()
+        real = np.array([k % st.nmax < st.ring_num_particles(k // st.nmax) for k in range(s.num_slots)])
+        assert np.max(np.abs(s.state.pos[real] - pos[real])) < tol
+        assert np.max(np.abs(s.state.pol - pol)) < tol
+    assert u.max() > nr                   # the source spawned
+    assert not m[far]                     # the sink removed the ring it covers
+    o.close()
+    s.close()
