@@ -313,8 +313,10 @@ function configure_sources!(system, h)
             for p in s.bbox_spawn_pos[i]
                 push!(spawn, p[1], p[2])
             end
-            isnothing(lst) || for c in lst
-                push!(rc, Int32(c[1] - 1), Int32(c[2] - 1))
+            if !isnothing(lst)
+                for c in lst
+                    push!(rc, Int32(c[1] - 1), Int32(c[2] - 1))
+                end
             end
         end
     end
