@@ -389,6 +389,35 @@ int mavi_rings_active(MaviSystem* sys, int32_t replica, int32_t* active_mask, in
  * FP64. Entries of inactive rings are computed from their parked positions. */
 int mavi_rings_areas(MaviSystem* sys, int32_t replica, double* areas);
 
+/* Invasion (src/rings/rings.jl:89-93): a particle of ring `invasor` that lies
+ * inside the polygon of ring `invaded`. 1-based ring ids and the particle's
+ * 1-based scalar index (to_scalar_idx, src/rings/states.jl:137-140). */
+typedef struct MaviInvasion {
+    int32_t invasor, invaded, p_id;
+    int32_t _pad0;
+} MaviInvasion;
+
+/* Invasion detection of one replica: InvasionsCfg(steps_to_update) and the
+ * ring chunks ChunksCfg(num_cols, num_rows) of RingsIntCfg
+ * (src/rings/configs.jl:334-350). enable = 0 turns it off. num_cols == 0 and
+ * num_rows == 0: no ring chunks (check_invasions!(system, ::Nothing),
+ * src/rings/integration.jl:497-507). The call stands for the system's
+ * construction: last_check becomes the replica's step count and
+ * update_invasions! runs once (src/rings/rings.jl:276-284). From then on every
+ * step whose num_steps - last_check >= steps_to_update runs check_invasions!
+ * at the point of step! the reference does (after sources, sinks and
+ * update_ids!, before the forces; src/rings/integration.jl:522-530). A step
+ * that checks waits for the device once to collect the list. */
+int mavi_rings_invasions_config(MaviSystem* sys, int32_t replica, int32_t enable, int64_t steps_to_update,
+                                int32_t num_cols, int32_t num_rows);
+/* InvasionsInfo of one replica (src/rings/rings.jl:95-100): the list in the
+ * order the reference pushes it (with ring chunks the list of the last check;
+ * without them every check's list appended, as the reference never empties
+ * it there) and last_check. Copies min(count, capacity) entries; *count is
+ * the list's length. Waits for the device. */
+int mavi_rings_invasions(MaviSystem* sys, int32_t replica, MaviInvasion* out, int64_t capacity, int64_t* count,
+                         int64_t* last_check);
+
 int mavi_get_stats(MaviSystem* sys, MaviStats* stats);
 /* Device-time profiling (and reset of the accumulated profile). on: 0 off,
  * 1 per kernel kind and whole step (an event pair around every launch group),

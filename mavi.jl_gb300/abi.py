@@ -176,10 +176,15 @@ class MaviSpawnBox(C.Structure):
     ]
 
 
+class MaviInvasion(C.Structure):
+    _fields_ = [("invasor", C.c_int32), ("invaded", C.c_int32), ("p_id", C.c_int32), ("_pad0", C.c_int32)]
+
+
 STRUCTS = {
     "MaviSpace": MaviSpace, "MaviRingsCfg": MaviRingsCfg, "MaviDynamicCfg": MaviDynamicCfg,
     "MaviReplicaParams": MaviReplicaParams, "MaviOptions": MaviOptions, "MaviStats": MaviStats,
     "MaviProfile": MaviProfile, "MaviSourceEntry": MaviSourceEntry, "MaviSpawnBox": MaviSpawnBox,
+    "MaviInvasion": MaviInvasion,
 }
 
 # Exported entry points and their signatures (restype, argtypes).
@@ -215,6 +220,9 @@ SIGNATURES = {
                                      C.POINTER(MaviSpawnBox), _dp, _ip]),
     "mavi_rings_active": (C.c_int, [_vp, C.c_int32, _ip, _ip, _ip]),
     "mavi_rings_areas": (C.c_int, [_vp, C.c_int32, _dp]),
+    "mavi_rings_invasions_config": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+    "mavi_rings_invasions": (C.c_int, [_vp, C.c_int32, C.POINTER(MaviInvasion), C.c_int64,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "mavi_chunk_lists_noalloc": (C.c_int, [C.POINTER(MaviReplicaParams), _vp, C.c_int64, _vp, _vp, _vp,
                                            C.c_char_p, C.c_int32]),
 }

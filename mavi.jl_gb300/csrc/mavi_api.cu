@@ -54,7 +54,9 @@ static void launch_rebin(MaviSystem* s, bool advance) {
 }
 
 // One whole step; its last kernel leaves the histogram for the next step.
-static void launch_step(MaviSystem* s) {
+// `due`: replicas whose invasion check falls on this step (eager steps only;
+// the check waits for the device).
+static int launch_step(MaviSystem* s, const std::vector<int32_t>* due = nullptr) {
     if (s->profiling) {
         cudaEventRecordWithFlags(s->ev.step_a, s->stream, cudaEventRecordExternal);
         s->ev.step_used = 1;
@@ -68,11 +70,18 @@ static void launch_step(MaviSystem* s) {
         record_end(s, MAVI_KERNEL_BIN_COUNT);
         s->counts_valid = true;
     }
+    if (due && !due->empty()) {
+        // update_invasions! (src/rings/integration.jl:529-530): after the
+        // sources, sinks and update_ids!, before the chunk update and forces
+        int rc = run_invasions(s, *due, s->var_rings);
+        if (rc) return rc;
+    }
     launch_rebin(s, true);
     if (s->prec == MAVI_PREC_FP64) step_body_fp64(s);
     else step_body_mixed(s);
     if (s->profiling) cudaEventRecordWithFlags(s->ev.step_b, s->stream, cudaEventRecordExternal);
     s->counts_valid = !s->var_rings;
+    return MAVI_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -402,6 +411,9 @@ static void fill_fix_pairs(const MaviReplicaParams& p, const DevRep& R, FixPair*
     }
 }
 
+static int check_device_error(MaviSystem* s);
+int mavi::device_error_status(MaviSystem* s) { return check_device_error(s); }
+
 static int check_device_error(MaviSystem* s) {
     DevError e{};
     CUDA_TRY(s, cudaMemcpyAsync(&e, s->C.err, sizeof(DevError), cudaMemcpyDeviceToHost, s->stream));
@@ -436,7 +448,7 @@ static int ensure_graph(MaviSystem* s) {
     for (int k = 0; k < MAVI_NUM_KERNEL_KINDS; k++) s->ev.used[k] = 0;
     CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     s->counts_valid = true;
-    launch_step(s);
+    (void)launch_step(s);
     cudaError_t e = cudaStreamEndCapture(s->stream, &s->graph);
     if (e != cudaSuccess) return fail(s, MAVI_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     CUDA_TRY(s, cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
@@ -956,19 +968,25 @@ int mavi_step(MaviSystem* s, int64_t nsteps) {
         int rc = ensure_graph(s);
         if (rc) return rc;
     }
+    std::vector<int32_t> due;
     for (int64_t k = 0; k < nsteps; k++) {
+        // update_invasions! (src/rings/integration.jl:511-520): which replicas check on this step
+        due.clear();
+        for (int32_t r = 0; r < (int32_t)s->inv.size(); r++)
+            if (s->inv[r].on && s->num_steps[r] - s->inv[r].last_check >= s->inv[r].steps) due.push_back(r);
         if (injected) {
             CUDA_TRY(s, cudaMemcpyAsync(s->noise_cur, s->noise_queue + s->noise_queue_pos * s->noise_count,
                                         sizeof(double) * s->noise_count, cudaMemcpyDeviceToDevice, s->stream));
             s->noise_queue_pos++;
         }
-        if (s->graph_exec) {
+        if (s->graph_exec && due.empty()) {
             CUDA_TRY(s, cudaGraphLaunch(s->graph_exec, s->stream));
             s->counts_valid = !s->var_rings;
             collect_profile(s, s->graph_ev_used);
             collect_step_time(s, s->graph_step_used);
         } else {
-            launch_step(s);
+            int rc = launch_step(s, &due);
+            if (rc) return rc;
             CUDA_TRY(s, cudaGetLastError());
             collect_profile(s, s->ev.used);
             collect_step_time(s, s->ev.step_used);

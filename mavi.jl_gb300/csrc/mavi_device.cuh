@@ -65,7 +65,8 @@ struct DevRep {
     unsigned long long wall_R2_lo;
     float wall_Ru_f, wall_krep_f, wall_katr_f, wall_deq_f, wall_dmax_f, _wall_pad;
     // sources and sinks of the rings model: entries [src_e0, src_e0 + src_ne)
-    int32_t src_e0, src_ne, src_has_sink, _src_pad;
+    // inv_cms: the step's k_sources keeps RingsInfo.cms for invasion detection
+    int32_t src_e0, src_ne, src_has_sink, inv_cms;
     int32_t min_image;     // first space is PeriodicWalls on a RectangleCfg
     int32_t num_spaces;
     int32_t has_wall_forces;

@@ -2130,7 +2130,7 @@ __global__ void __launch_bounds__(kSrcThreads) k_sources(Ctx C) {
         sh_hits = 0;
     }
     __syncthreads();
-    if (R.src_has_sink) {
+    if (R.src_has_sink || R.inv_cms) {
         const int32_t na = sh_num_active;
         for (int32_t k = tid; k < na; k += nthr) {
             const int32_t ring = ids[k];

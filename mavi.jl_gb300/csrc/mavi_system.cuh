@@ -75,6 +75,27 @@ struct MaviSystem {
     };
     std::vector<SrcCfg> src_cfg;
     void* src_buf[4] = {nullptr, nullptr, nullptr, nullptr};   // entries, boxes, spawn, chunks
+    // invasion detection (rings), per replica
+    struct InvCfg {
+        bool on = false;
+        int64_t steps = 0, last_check = 0;
+        int32_t cols = 0, rows = 0;          // ring chunks; 0 x 0: none
+        int64_t chunk0 = 0;                  // first ring chunk in the shared arrays
+        double blx = 0, bly = 0, len = 0, h = 0, cl = 0, ch = 0;
+        std::vector<MaviInvasion> list;
+    };
+    std::vector<InvCfg> inv;
+    struct InvBuffers {
+        double2* cont = nullptr;             // continuous ring positions, user order
+        double* bb = nullptr;                // per ring: xmin, xmax, ymin, ymax
+        int32_t *chunk_of = nullptr, *rank = nullptr, *list = nullptr;   // per ring
+        int32_t *count = nullptr, *start = nullptr, *nbr = nullptr;      // per ring chunk (nbr: 4 each)
+        int32_t* num_ids = nullptr;          // per replica: rings in get_rings_ids
+        void* reps = nullptr;                // the replicas of one check
+        void* rec = nullptr;                 // records of one check
+        int32_t* nrec = nullptr;
+        int64_t rec_cap = 0, nch = 0;
+    } invb;
 };
 
 namespace mavi {
@@ -173,5 +194,10 @@ void forces_to_user_fp64(MaviSystem* s);
 void forces_to_user_mixed(MaviSystem* s);
 void sources_fp64(MaviSystem* s);
 void sources_mixed(MaviSystem* s);
+// check_invasions! for the listed replicas (mavi_invasions.cu); waits for the
+// device. from_sources: the step's k_sources left RingsInfo.cms.
+int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sources);
+// waits for the stream and turns a device error flag into a status (mavi_api.cu)
+int device_error_status(MaviSystem* s);
 
 }  // namespace mavi

@@ -117,9 +117,40 @@ def get_ring_radius(p_radius: float, num_particles: int) -> float:
     return (p_radius * 2) / (2 * (1 - math.cos(2 * math.pi / num_particles))) ** .5
 
 
-def RingsIntCfg(dt: float, p_chunks_cfg: ChunksCfg | None = None, device: CUDADevice | None = None) -> IntCfg:
-    """RingsIntCfg (src/rings/configs.jl:575-582)."""
-    return IntCfg(dt=dt, chunks_cfg=p_chunks_cfg, device=device or CUDADevice())
+@dataclass
+class InvasionsCfg:
+    """InvasionsCfg(steps_to_update) (src/rings/configs.jl:334-336)."""
+    steps_to_update: int
+
+
+@dataclass
+class IntCfgExtra:
+    """IntCfgExtra(r_chunks_cfg, invasions_cfg) (src/rings/configs.jl:338-341)."""
+    r_chunks_cfg: ChunksCfg | None = None
+    invasions_cfg: InvasionsCfg | None = None
+
+
+def RingsIntCfg(dt: float, p_chunks_cfg: ChunksCfg | None = None, r_chunks_cfg: ChunksCfg | None = None,
+                invasions_cfg: InvasionsCfg | None = None, device: CUDADevice | None = None) -> IntCfg:
+    """RingsIntCfg (src/rings/configs.jl:344-350)."""
+    return IntCfg(dt=dt, chunks_cfg=p_chunks_cfg, device=device or CUDADevice(),
+                  extra=IntCfgExtra(r_chunks_cfg, invasions_cfg))
+
+
+@dataclass(frozen=True)
+class Invasion:
+    """Invasion (src/rings/rings.jl:89-93): particle p_id (1-based scalar
+    index) of ring invasor (1-based) inside ring invaded."""
+    invasor: int
+    invaded: int
+    p_id: int
+
+
+@dataclass
+class InvasionsInfo:
+    """InvasionsInfo(list, last_check) (src/rings/rings.jl:95-100)."""
+    list: list
+    last_check: int
 
 
 # ---------------------------------------------------------------------------
@@ -375,14 +406,41 @@ class RingsSystem(System):
             np.zeros(2, dtype=np.int32)
         return mask, len(cfgs), entries, box_arr, spawn_xy, chunk_rc
 
+    def invasions_abi(self):
+        """(enable, steps_to_update, num_cols, num_rows) for
+        mavi_rings_invasions_config, or None without an InvasionsCfg."""
+        extra = getattr(self.int_cfg, "extra", None)
+        inv = getattr(extra, "invasions_cfg", None)
+        if inv is None:
+            return None
+        rc = getattr(extra, "r_chunks_cfg", None)
+        return (1, int(inv.steps_to_update), int(rc.num_cols) if rc is not None else 0,
+                int(rc.num_rows) if rc is not None else 0)
+
     def _configure_replica(self, h, replica: int):
-        """Handle hook: variable rings ids and sources/sinks of this replica."""
+        """Handle hook: variable rings ids and sources/sinks of this replica,
+        then invasion detection (constructed last, as RingsSystem does)."""
         cfg = self.sources_abi()
-        if cfg is None:
-            return
-        mask, n, entries, boxes, spawn_xy, chunk_rc = cfg
-        h.check(h.lib.mavi_rings_sources(h.handle, replica, abi.as_iptr(mask), n, entries, boxes,
-                                         abi.as_dptr(spawn_xy), abi.as_iptr(chunk_rc)), "mavi_rings_sources")
+        if cfg is not None:
+            mask, n, entries, boxes, spawn_xy, chunk_rc = cfg
+            h.check(h.lib.mavi_rings_sources(h.handle, replica, abi.as_iptr(mask), n, entries, boxes,
+                                             abi.as_dptr(spawn_xy), abi.as_iptr(chunk_rc)), "mavi_rings_sources")
+        inv = self.invasions_abi()
+        if inv is not None:
+            h.check(h.lib.mavi_rings_invasions_config(h.handle, replica, *inv), "mavi_rings_invasions_config")
+
+    def invasions(self) -> InvasionsInfo:
+        """RingsInfo.invasions: the list of the last check (every check's,
+        appended, without ring chunks) and last_check."""
+        h = self._batch.handle if getattr(self, "_batch", None) is not None else self._ensure()
+        k = h.systems.index(self)
+        n, last = C.c_int64(), C.c_int64()
+        h.check(h.lib.mavi_rings_invasions(h.handle, k, None, 0, C.byref(n), C.byref(last)), "mavi_rings_invasions")
+        out = (abi.MaviInvasion * max(n.value, 1))()
+        h.check(h.lib.mavi_rings_invasions(h.handle, k, out, n.value, C.byref(n), C.byref(last)),
+                "mavi_rings_invasions")
+        return InvasionsInfo([Invasion(out[q].invasor, out[q].invaded, out[q].p_id) for q in range(n.value)],
+                             int(last.value))
 
     def areas(self) -> np.ndarray:
         """RingsInfo.areas (src/rings/integration.jl:140-160): ring areas at

@@ -64,6 +64,15 @@ struct OracleSys {
     int32_t *chunk_rc;          /* (row, col) pairs, 0-based */
     int64_t *box_chunk0;        /* per box: first pair in chunk_rc */
     int64_t n_random;           /* boxes with a random spawn polarisation */
+    /* invasions (src/rings/rings.jl:86-100) and the ring chunks of
+     * RingsInfo.r_chunks (:189-204) */
+    int inv_on;
+    int64_t inv_steps, inv_last;
+    int32_t rrows, rcols;
+    double r_blx, r_bly, r_len, r_h, r_cl, r_ch;
+    int32_t *rnbr, *rnbr_cnt, *rcount, *rstart, *rlist;
+    MaviInvasion *inv;
+    int64_t inv_n, inv_cap;
     /* time_info */
     int64_t num_steps; double time;
     int32_t err;
@@ -250,47 +259,52 @@ static int64_t periodic_get_id(int64_t x, int64_t num_t) {
     return x;
 }
 
-static void add_nbr(OracleSys* s, int64_t row1, int64_t col1, int64_t nrow1, int64_t ncol1) {
-    int64_t c = (col1 - 1) * s->rows + (row1 - 1);
-    int64_t nc = (ncol1 - 1) * s->rows + (nrow1 - 1);
-    s->nbr[c * 4 + s->nbr_cnt[c]] = (int32_t)nc;
-    s->nbr_cnt[c] += 1;
+static void add_nbr(int64_t rows, int32_t* nbr, int32_t* cnt, int64_t row1, int64_t col1, int64_t nrow1,
+                    int64_t ncol1) {
+    int64_t c = (col1 - 1) * rows + (row1 - 1);
+    int64_t nc = (ncol1 - 1) * rows + (nrow1 - 1);
+    nbr[c * 4 + cnt[c]] = (int32_t)nc;
+    cnt[c] += 1;
 }
 
-/* get_neighbors: periodic (src/chunks.jl:61-87) and open (:89-118). */
-static int build_neighbors(OracleSys* s, int periodic) {
-    int64_t R = s->rows, C = s->cols;
-    memset(s->nbr_cnt, 0, sizeof(int32_t) * R * C);
+/* get_neighbors: periodic (src/chunks.jl:61-87) and open (:89-118), 0-based
+ * column-major chunk ids. An open grid of one column and several rows indexes
+ * column 0 (a BoundsError in the reference). */
+static int neighbor_table(int64_t R, int64_t C, int periodic, int32_t* nbr, int32_t* cnt) {
+    memset(cnt, 0, sizeof(int32_t) * R * C);
     if (periodic) {
         for (int64_t i = 1; i <= R; i++)
             for (int64_t j = 1; j <= C; j++) {
-                add_nbr(s, i, j, periodic_get_id(i + 1, R), periodic_get_id(j, C));
-                add_nbr(s, i, j, periodic_get_id(i + 1, R), periodic_get_id(j + 1, C));
-                add_nbr(s, i, j, periodic_get_id(i, R), periodic_get_id(j + 1, C));
-                add_nbr(s, i, j, periodic_get_id(i - 1, R), periodic_get_id(j + 1, C));
+                add_nbr(R, nbr, cnt, i, j, periodic_get_id(i + 1, R), periodic_get_id(j, C));
+                add_nbr(R, nbr, cnt, i, j, periodic_get_id(i + 1, R), periodic_get_id(j + 1, C));
+                add_nbr(R, nbr, cnt, i, j, periodic_get_id(i, R), periodic_get_id(j + 1, C));
+                add_nbr(R, nbr, cnt, i, j, periodic_get_id(i - 1, R), periodic_get_id(j + 1, C));
             }
         return MAVI_OK;
     }
-    if (C < 2) return MAVI_ERR_UNSUPPORTED; /* reference indexes column 0 (BoundsError) */
+    if (C < 2 && R > 1) return MAVI_ERR_UNSUPPORTED;
     for (int64_t i = 1; i <= R - 1; i++) {
-        int64_t c1 = (1 - 1) * R + (i - 1);
-        s->nbr_cnt[c1] = 0;
-        add_nbr(s, i, 1, i + 1, 1);
-        add_nbr(s, i, 1, i + 1, 2);
-        add_nbr(s, i, 1, i, 2);
+        add_nbr(R, nbr, cnt, i, 1, i + 1, 1);
+        add_nbr(R, nbr, cnt, i, 1, i + 1, 2);
+        add_nbr(R, nbr, cnt, i, 1, i, 2);
         for (int64_t j = 2; j <= C - 1; j++) {
-            add_nbr(s, i, j, i + 1, j - 1);
-            add_nbr(s, i, j, i + 1, j);
-            add_nbr(s, i, j, i + 1, j + 1);
-            add_nbr(s, i, j, i, j + 1);
+            add_nbr(R, nbr, cnt, i, j, i + 1, j - 1);
+            add_nbr(R, nbr, cnt, i, j, i + 1, j);
+            add_nbr(R, nbr, cnt, i, j, i + 1, j + 1);
+            add_nbr(R, nbr, cnt, i, j, i, j + 1);
         }
         int64_t cl = (C - 1) * R + (i - 1);
-        s->nbr_cnt[cl] = 0;    /* neighbors[i, num_cols] is assigned, not appended */
-        add_nbr(s, i, C, i + 1, C - 1);
-        add_nbr(s, i, C, i + 1, C);
+        cnt[cl] = 0;    /* neighbors[i, num_cols] is assigned, not appended */
+        add_nbr(R, nbr, cnt, i, C, i + 1, C - 1);
+        add_nbr(R, nbr, cnt, i, C, i + 1, C);
     }
-    for (int64_t j = 1; j <= C - 1; j++) add_nbr(s, R, j, R, j + 1);
+    for (int64_t j = 1; j <= C - 1; j++) add_nbr(R, nbr, cnt, R, j, R, j + 1);
     return MAVI_OK;
+}
+
+static int build_neighbors(OracleSys* s, int periodic) {
+    if (!periodic && s->cols < 2) return MAVI_ERR_UNSUPPORTED; /* reference indexes column 0 (BoundsError) */
+    return neighbor_table(s->rows, s->cols, periodic, s->nbr, s->nbr_cnt);
 }
 
 /* update_particle_chunk! index computation (src/chunks.jl:120-142). */
@@ -751,8 +765,8 @@ static void update_ids(OracleSys* s) {
  * last update_continuos_pos! with periodic walls; summed in particle order. */
 static void update_cms(OracleSys* s) {
     const double* src = (s->p.spaces[0].wall == MAVI_WALL_PERIODIC) ? s->cont_pos : s->pos;
-    for (int64_t k = 0; k < s->num_active; k++) {
-        int64_t ring = s->ids[k];
+    for (int64_t k = 0; k < rings_count(s); k++) {
+        int64_t ring = ring_at(s, k);
         int32_t n = ring_n(s, ring);
         const double* rp = src + 2 * ring * s->nmax;
         double sx = rp[0], sy = rp[1];
@@ -911,6 +925,185 @@ int32_t oracle_rings_active(OracleSys* s, int32_t* active_mask, int32_t* uids, i
 }
 
 /* ------------------------------------------------------------------------ */
+/* invasions (src/rings/integration.jl:378-520)                              */
+/* ------------------------------------------------------------------------ */
+
+/* point_line_intersect (:378-418): does the ray from p towards +x cross the
+ * edge a-b? */
+static int point_line_intersect(double px, double py, const double* a, const double* b) {
+    double dx = b[0] - a[0];
+    double dy = b[1] - a[1];
+    if (dx == 0) {
+        double x_inter = a[0];
+        int check1 = x_inter > px;
+        double y1 = a[1], y2 = b[1];
+        if (dy < 0) { y1 = b[1]; y2 = a[1]; }
+        int check2 = (y1 < py) && (py < y2);
+        return check1 & check2;
+    }
+    if (dy == 0) return 0;
+    double c = dy * a[0] - dx * a[1];
+    double x_inter = (c + dx * py) / dy;
+    int check1 = x_inter > px;
+    double y1 = a[1], y2 = b[1];
+    if (dy < 0) { y1 = b[1]; y2 = a[1]; }
+    double x1 = a[0], x2 = b[0];
+    if (dx < 0) { x1 = b[0]; x2 = a[0]; }
+    int check2 = ((x1 < x_inter) && (x_inter < x2)) & ((y1 < py) && (py < y2));
+    return check1 & check2;
+}
+
+/* ring_points (src/rings/rings.jl:31-43): continuous positions with
+ * periodic walls, positions otherwise. */
+static const double* ring_points(const OracleSys* s, int64_t ring) {
+    const double* src = (s->p.spaces[0].wall == MAVI_WALL_PERIODIC) ? s->cont_pos : s->pos;
+    return src + 2 * ring * s->nmax;
+}
+
+static void push_invasion(OracleSys* s, int64_t invasor, int64_t invaded, int64_t pi) {
+    if (s->inv_n == s->inv_cap) {
+        s->inv_cap = s->inv_cap ? 2 * s->inv_cap : 64;
+        s->inv = (MaviInvasion*)realloc(s->inv, sizeof(MaviInvasion) * s->inv_cap);
+    }
+    MaviInvasion m;
+    memset(&m, 0, sizeof(m));
+    m.invasor = (int32_t)(invasor + 1);
+    m.invaded = (int32_t)(invaded + 1);
+    m.p_id = (int32_t)(invasor * s->nmax + pi + 1);   /* to_scalar_idx (src/rings/states.jl:137-140) */
+    s->inv[s->inv_n++] = m;
+}
+
+/* polygons_intersect (:420-441) pushed as find_invasions! does (:443-470):
+ * the points of ring a inside ring b, ascending. */
+static void push_inside(OracleSys* s, int64_t a, int64_t b) {
+    const double* pa = ring_points(s, a);
+    const double* pb = ring_points(s, b);
+    int32_t na = ring_n(s, a), nb = ring_n(s, b);
+    for (int32_t id = 0; id < na; id++) {
+        int count = 0;
+        for (int32_t idx1 = 0; idx1 < nb; idx1++) {
+            int32_t idx2 = (idx1 == nb - 1) ? 0 : idx1 + 1;
+            if (point_line_intersect(pa[2 * id], pa[2 * id + 1], pb + 2 * idx1, pb + 2 * idx2)) count += 1;
+        }
+        if (count % 2 != 0) push_invasion(s, a, b, id);
+    }
+}
+
+static void find_invasions(OracleSys* s, int64_t r1, int64_t r2) {
+    /* both lists are formed before either is pushed; pushing does not change them */
+    push_inside(s, r1, r2);
+    push_inside(s, r2, r1);
+}
+
+/* check_invasions! (:472-509). With ring chunks: update_chunks!(r_chunks)
+ * (src/rings/integration.jl:18-23 with update_particle_chunk!,
+ * src/chunks.jl:120-147, on RingsInfo.cms), then every ring against the later
+ * rings of its chunk and all rings of the neighbour chunks; the list is
+ * emptied first. Without: ring ids 1:length(get_rings_ids), list kept. */
+static int32_t check_invasions(OracleSys* s) {
+    if (s->rcols == 0) {
+        int64_t L = rings_count(s);
+        for (int64_t r1 = 0; r1 < L; r1++)
+            for (int64_t r2 = r1 + 1; r2 < L; r2++) find_invasions(s, r1, r2);
+        return MAVI_OK;
+    }
+    s->inv_n = 0;
+    int64_t R = s->rrows, C = s->rcols, nch = R * C;
+    memset(s->rcount, 0, sizeof(int32_t) * nch);
+    int64_t L = rings_count(s);
+    int32_t* cell = (int32_t*)malloc(sizeof(int32_t) * (L ? L : 1));
+    for (int64_t k = 0; k < L; k++) {
+        int64_t ring = ring_at(s, k);
+        double x = s->cms[2 * ring], y = s->cms[2 * ring + 1];
+        double qr = oracle_julia_div(-y + s->r_bly + s->r_h, s->r_ch);
+        double qc = oracle_julia_div(x - s->r_blx, s->r_cl);
+        if (!isfinite(qr) || !isfinite(qc) || fabs(qr) >= 4e18 || fabs(qc) >= 4e18) {
+            free(cell);
+            return MAVI_ERR_NONFINITE;
+        }
+        int64_t row = (int64_t)qr + 1, col = (int64_t)qc + 1;
+        row -= (row == R + 1) ? 1 : 0;
+        col -= (col == C + 1) ? 1 : 0;
+        if (row < 1 || row > R || col < 1 || col > C) { free(cell); return MAVI_ERR_OUT_OF_GRID; }
+        cell[k] = (int32_t)((col - 1) * R + (row - 1));
+        s->rcount[cell[k]] += 1;
+    }
+    int32_t acc = 0;
+    for (int64_t c = 0; c < nch; c++) { s->rstart[c] = acc; acc += s->rcount[c]; s->rcount[c] = 0; }
+    for (int64_t k = 0; k < L; k++) {
+        int32_t c = cell[k];
+        s->rlist[s->rstart[c] + s->rcount[c]++] = (int32_t)ring_at(s, k);
+    }
+    free(cell);
+    for (int64_t col = 0; col < C; col++)
+        for (int64_t row = 0; row < R; row++) {
+            int64_t c = col * R + row;
+            int32_t np = s->rcount[c];
+            const int32_t* chunk = s->rlist + s->rstart[c];
+            for (int32_t i = 0; i < np; i++) {
+                int64_t r1 = chunk[i];
+                for (int32_t j = i + 1; j < np; j++) find_invasions(s, r1, chunk[j]);
+                for (int32_t q = 0; q < s->rnbr_cnt[c]; q++) {
+                    int32_t nb = s->rnbr[4 * c + q];
+                    for (int32_t j = 0; j < s->rcount[nb]; j++) find_invasions(s, r1, s->rlist[s->rstart[nb] + j]);
+                }
+            }
+        }
+    return MAVI_OK;
+}
+
+/* update_invasions! (:511-520) */
+static int32_t update_invasions(OracleSys* s) {
+    if (!s->inv_on) return MAVI_OK;
+    if (s->num_steps - s->inv_last < s->inv_steps) return MAVI_OK;
+    s->inv_last = s->num_steps;
+    return check_invasions(s);
+}
+
+int32_t oracle_rings_invasions_config(OracleSys* s, int32_t enable, int64_t steps_to_update, int32_t num_cols,
+                                      int32_t num_rows) {
+    if (s->p.state_kind != MAVI_STATE_RINGS) return MAVI_ERR_UNSUPPORTED;
+    if (num_cols < 0 || num_rows < 0 || ((num_cols == 0) != (num_rows == 0))) return MAVI_ERR_INVALID_ARG;
+    free(s->rnbr); free(s->rnbr_cnt); free(s->rcount); free(s->rstart); free(s->rlist);
+    s->rnbr = s->rnbr_cnt = s->rcount = s->rstart = s->rlist = NULL;
+    s->inv_on = enable != 0;
+    s->inv_steps = steps_to_update;
+    s->inv_n = 0;
+    s->rcols = enable ? num_cols : 0;
+    s->rrows = enable ? num_rows : 0;
+    if (s->rcols > 0) {
+        int64_t nch = (int64_t)s->rrows * s->rcols;
+        s->rnbr = (int32_t*)calloc(4 * nch, sizeof(int32_t));
+        s->rnbr_cnt = (int32_t*)calloc(nch, sizeof(int32_t));
+        s->rcount = (int32_t*)calloc(nch, sizeof(int32_t));
+        s->rstart = (int32_t*)calloc(nch, sizeof(int32_t));
+        s->rlist = (int32_t*)calloc(s->num_rings ? s->num_rings : 1, sizeof(int32_t));
+        int32_t st = neighbor_table(s->rrows, s->rcols, s->p.spaces[0].wall == MAVI_WALL_PERIODIC, s->rnbr,
+                                    s->rnbr_cnt);
+        if (st) return st;
+        bbox_of(&s->p, &s->r_len, &s->r_h, &s->r_blx, &s->r_bly);
+        s->r_cl = s->r_len / s->rcols;
+        s->r_ch = s->r_h / s->rrows;
+    }
+    if (!s->cms) s->cms = (double*)calloc(2 * s->num_rings, sizeof(double));
+    /* RingsSystem() (src/rings/rings.jl:276-284): last_check = num_steps,
+     * update_continuos_pos!, update_cms!, then update_invasions! */
+    s->inv_last = s->num_steps;
+    update_continuos_pos(s);
+    update_cms(s);
+    return update_invasions(s);
+}
+
+int32_t oracle_rings_invasions(OracleSys* s, MaviInvasion* out, int64_t capacity, int64_t* count,
+                               int64_t* last_check) {
+    int64_t n = s->inv_n < capacity ? s->inv_n : capacity;
+    if (n > 0) memcpy(out, s->inv, sizeof(MaviInvasion) * n);
+    if (count) *count = s->inv_n;
+    if (last_check) *last_check = s->inv_last;
+    return MAVI_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* integrators (src/integration.jl:415-498)                                  */
 /* ------------------------------------------------------------------------ */
 
@@ -1004,13 +1197,14 @@ static int32_t step_once(OracleSys* s, int32_t fm, const double* noise) {
         update_time(s);
         return MAVI_OK;
     case MAVI_STEP_RINGS:                           /* src/rings/integration.jl:522-543 */
+        if (s->var_ids || s->inv_on) update_cms(s);
         if (s->var_ids) {
-            update_cms(s);
             process_sources(s, noise ? noise + s->num_rings : NULL);
             update_ids(s);
         }
         if ((st = oracle_update_chunks(s))) return st;
         update_continuos_pos(s);
+        if ((st = update_invasions(s))) return st;
         clean_forces(s);
         calc_forces(s, fm);
         rings_bonded_forces(s);
@@ -1275,6 +1469,7 @@ void oracle_destroy(OracleSys* s) {
     free(s->pos); free(s->vel); free(s->pol); free(s->types); free(s->forces); free(s->slices);
     free(s->pids); free(s->chunk_particles); free(s->num_in_chunk); free(s->nbr); free(s->nbr_cnt);
     free(s->cont_pos); free(s->areas);
+    free(s->rnbr); free(s->rnbr_cnt); free(s->rcount); free(s->rstart); free(s->rlist); free(s->inv);
     free(s->mask); free(s->uids); free(s->ids); free(s->cms);
     free(s->src); free(s->boxes); free(s->spawn); free(s->chunk_rc); free(s->box_chunk0);
     free(s);
@@ -1346,5 +1541,6 @@ int32_t oracle_struct_sizes(int64_t* out) {
     out[6] = (int64_t)sizeof(MaviProfile);
     out[7] = (int64_t)sizeof(MaviSourceEntry);
     out[8] = (int64_t)sizeof(MaviSpawnBox);
-    return 9;
+    out[9] = (int64_t)sizeof(MaviInvasion);
+    return 10;
 }

@@ -59,6 +59,11 @@ int32_t oracle_rings_sources(OracleSys* s, const int32_t* active_mask, int32_t n
                              const MaviSourceEntry* entries, const MaviSpawnBox* boxes, const double* spawn_xy,
                              const int32_t* chunk_rc);
 int32_t oracle_rings_active(OracleSys* s, int32_t* active_mask, int32_t* uids, int32_t* num_active);
+/* Invasion detection, as mavi_rings_invasions_config / mavi_rings_invasions. */
+int32_t oracle_rings_invasions_config(OracleSys* s, int32_t enable, int64_t steps_to_update, int32_t num_cols,
+                                      int32_t num_rows);
+int32_t oracle_rings_invasions(OracleSys* s, MaviInvasion* out, int64_t capacity, int64_t* count,
+                               int64_t* last_check);
 /* Julia float `div` as used by update_particle_chunk! (src/chunks.jl:129-130). */
 double  oracle_julia_div(double x, double y);
 /* update_particle_chunk! row/col (1-based, before bounds checks) for a point. */

@@ -59,6 +59,8 @@ def _load_lib():
         "oracle_rings_sources": (C.c_int32, [vp, ip, C.c_int32, C.POINTER(abi.MaviSourceEntry),
                                              C.POINTER(abi.MaviSpawnBox), dp, ip]),
         "oracle_rings_active": (C.c_int32, [vp, ip, ip, ip]),
+        "oracle_rings_invasions_config": (C.c_int32, [vp, C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+        "oracle_rings_invasions": (C.c_int32, [vp, C.POINTER(abi.MaviInvasion), C.c_int64, lp, lp]),
         "oracle_julia_div": (C.c_double, [C.c_double, C.c_double]),
         "oracle_chunk_of": (C.c_int32, [vp, C.c_double, C.c_double, lp, lp]),
         "oracle_struct_sizes": (C.c_int32, [lp]),
@@ -225,6 +227,20 @@ class OracleSystem:
                  "rings_active")
         return m.astype(bool), u, int(na.value)
 
+    def rings_invasions_config(self, enable, steps_to_update, num_cols=0, num_rows=0):
+        """InvasionsCfg and ring chunks, as mavi_rings_invasions_config."""
+        self._ck(self.lib.oracle_rings_invasions_config(self.h, 1 if enable else 0, int(steps_to_update),
+                                                        int(num_cols), int(num_rows)), "rings_invasions_config")
+
+    def rings_invasions(self):
+        """(list of (invasor, invaded, p_id), last_check)."""
+        from mavi_gb300 import abi
+        n, last = C.c_int64(), C.c_int64()
+        self._ck(self.lib.oracle_rings_invasions(self.h, None, 0, C.byref(n), C.byref(last)), "rings_invasions")
+        out = (abi.MaviInvasion * max(n.value, 1))()
+        self._ck(self.lib.oracle_rings_invasions(self.h, out, n.value, C.byref(n), C.byref(last)), "rings_invasions")
+        return [(out[k].invasor, out[k].invaded, out[k].p_id) for k in range(n.value)], int(last.value)
+
     def chunk_of(self, x, y):
         r, c = C.c_int64(), C.c_int64()
         st = self.lib.oracle_chunk_of(self.h, float(x), float(y), C.byref(r), C.byref(c))
@@ -239,7 +255,7 @@ def struct_sizes():
     out = (C.c_int64 * 16)()
     n = _load_lib().oracle_struct_sizes(out)
     names = ["MaviSpace", "MaviRingsCfg", "MaviDynamicCfg", "MaviReplicaParams", "MaviOptions", "MaviStats",
-             "MaviProfile", "MaviSourceEntry", "MaviSpawnBox"]
+             "MaviProfile", "MaviSourceEntry", "MaviSpawnBox", "MaviInvasion"]
     return {names[k]: out[k] for k in range(n)}
 
 
@@ -264,4 +280,7 @@ def from_system(system, nthreads: int = 1, step_kind=None) -> OracleSystem:
     src = system.sources_abi() if hasattr(system, "sources_abi") else None
     if src is not None:
         o.rings_sources(*src)
+    inv = system.invasions_abi() if hasattr(system, "invasions_abi") else None
+    if inv is not None:
+        o.rings_invasions_config(*inv)
     return o
