@@ -1,7 +1,8 @@
 """In-tree build of libmavi_cuda.so for sm_103a (GB300).
 
-Three translation units (host runtime + C ABI, FP64 passes, mixed passes)
-compile in parallel, then link into ``lib/libmavi_cuda.so``. No cmake.
+The translation units (host runtime + C ABI, FP64 passes, mixed passes, the
+FMA peak probe, the allocation-free chunk lists, invasion detection) compile
+in parallel, then link into ``lib/libmavi_cuda.so``. No cmake.
 """
 from __future__ import annotations
 

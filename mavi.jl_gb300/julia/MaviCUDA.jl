@@ -95,6 +95,10 @@ struct CSpawnBox
     num_chunks::Int32; _pad0::Int32
 end
 
+struct CInvasion
+    invasor::Int32; invaded::Int32; p_id::Int32; _pad0::Int32
+end
+
 struct COptions
     precision::Int32; noise_mode::Int32; seed::UInt64
     device::Int32; use_graph::Int32; block_size::Int32; gather_mode::Int32
@@ -271,7 +275,30 @@ function handle!(system)
     finalizer(x -> ccall((:mavi_destroy, libmavi), Cint, (Ptr{Cvoid},), x.ptr), h)
     HANDLES[system] = h
     st isa Rings.RingsState && configure_sources!(system, h.ptr)
+    st isa Rings.RingsState && configure_invasions!(system, h.ptr)
     return h.ptr
+end
+
+"The system's InvasionsCfg and ring chunks (RingsIntCfg extra, src/rings/configs.jl:334-350), or nothing."
+function _invasions_cfg(system)
+    extra = hasproperty(system.int_cfg, :extra) ? system.int_cfg.extra : nothing
+    (isnothing(extra) || !hasproperty(extra, :invasions_cfg)) && return nothing
+    return extra.invasions_cfg, extra.r_chunks_cfg
+end
+
+"""
+Invasion detection (update_invasions!, src/rings/integration.jl:511-520)
+passed to `mavi_rings_invasions_config`: steps_to_update and the ring-chunk
+grid; the handle's creation stands for the system's construction
+(`last_check = num_steps`, src/rings/rings.jl:276-284).
+"""
+function configure_invasions!(system, h)
+    cfg = _invasions_cfg(system)
+    (isnothing(cfg) || isnothing(cfg[1])) && return
+    inv, rc = cfg
+    cols, rows = isnothing(rc) ? (0, 0) : (rc.num_cols, rc.num_rows)
+    check(ccall((:mavi_rings_invasions_config, libmavi), Cint, (Ptr{Cvoid}, Int32, Int32, Int64, Int32, Int32),
+                h, 0, 1, inv.steps_to_update, cols, rows), "mavi_rings_invasions_config", h)
 end
 
 """
@@ -348,6 +375,24 @@ function sync!(system)
         ids.mask .= mask .!= 0
         ids.uids .= uids
         Mavi.States.update_ids!(st)          # ids, p_ids, counts (calc_active_ids!)
+    end
+    cfg = st isa Rings.RingsState ? _invasions_cfg(system) : nothing
+    if !isnothing(cfg) && !isnothing(cfg[1])
+        # RingsInfo.invasions: the list in the reference's push order, last_check
+        cnt, last = Ref{Int64}(0), Ref{Int64}(0)
+        check(ccall((:mavi_rings_invasions, libmavi), Cint,
+                    (Ptr{Cvoid}, Int32, Ptr{CInvasion}, Int64, Ref{Int64}, Ref{Int64}),
+                    h, 0, C_NULL, 0, cnt, last), "mavi_rings_invasions", h)
+        buf = Vector{CInvasion}(undef, cnt[])
+        check(ccall((:mavi_rings_invasions, libmavi), Cint,
+                    (Ptr{Cvoid}, Int32, Ptr{CInvasion}, Int64, Ref{Int64}, Ref{Int64}),
+                    h, 0, buf, cnt[], cnt, last), "mavi_rings_invasions", h)
+        info = system.info.invasions
+        empty!(info.list)
+        for v in buf
+            push!(info.list, Rings.Invasion(invasor=Int(v.invasor), invaded=Int(v.invaded), p_id=Int(v.p_id)))
+        end
+        info.last_check = last[]
     end
     n, t = Ref{Int64}(0), Ref{Float64}(0)
     check(ccall((:mavi_get_time, libmavi), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Float64}), h, n, t),

@@ -21,6 +21,7 @@ PAIRS = {
     "COptions": ("MaviOptions", None),
     "CSourceEntry": ("MaviSourceEntry", None),
     "CSpawnBox": ("MaviSpawnBox", None),
+    "CInvasion": ("MaviInvasion", None),
 }
 
 
