@@ -10,10 +10,10 @@
 //    chunk centre in int32 fixed point (int2, 2^-28 chunk units);
 //  * chunks in CSR form: count[c], start[c] over all replicas' chunks.
 // A step reads the state in "previous order" (*_out arrays, written by the
-// last step together with each particle's new chunk, its rank of arrival in
-// it and, in the mixed form, its new offset), rebuilds the chunk lists
-// (scan -> scatter -> deterministic per-chunk order + permutation into *_cur)
-// and runs the fused force/update passes.
+// last step together with each particle's new chunk and, in the mixed form,
+// its new offset; the chunk counts were added up by the same pass), rebuilds
+// the chunk lists (scan -> scatter claims places -> deterministic per-chunk
+// order + permutation into *_cur) and runs the fused force/update passes.
 //
 // GB300 executes FP64 at ~1/70 of the FP32 rate, so the per-particle FP64
 // work outside the pair loop is kept to a few tens of operations: the
@@ -198,8 +198,7 @@ __device__ __forceinline__ bool edge_chunk(const DevRep& R, int64_t row, int64_t
 }
 
 // Warp-aggregated histogram update: lanes with the same chunk share one
-// atomic; each lane gets its rank of arrival inside the chunk. Must be called
-// by all 32 lanes of the warp.
+// atomic. Must be called by all 32 lanes of the warp.
 __device__ __forceinline__ void count_into_chunk(const Ctx& C, bool valid, int64_t s, int64_t cell,
                                                  int32_t cap) {
     // a fire-and-forget add (no rank returned: nothing waits on the atomic);
