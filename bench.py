@@ -534,6 +534,8 @@ def main():
     cpu = None
     if rank == 0 and orc is not None:
         cpu = cpu_baseline(mg, orc, runners["fp64"], args.cpu_seconds, os.cpu_count() or 1)
+        one = cpu_baseline(mg, orc, runners["fp64"], max(args.cpu_seconds / 2, 1.0), 1)
+        cpu["one_core"] = {"value": one["value"], "sample": one["sample"]}
     if rank == 0:
         mx = line_forms["mixed"]
         first = runners["mixed"].first

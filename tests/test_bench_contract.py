@@ -20,3 +20,25 @@ def test_reference_arm_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"]["workload"] == "lj_1024"
+
+
+def test_cpu_baseline_at_one_core_and_all_cores(mg, orc):
+    """The CPU baseline leg times whole replicas of the workload through the
+    oracle, sequential at one thread and column-split threaded above."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    from helpers import lj_grid
+
+    class FakeRunner:           # the attributes cpu_baseline reads, no device handle
+        def __init__(self, systems):
+            self.systems = systems
+            self.kind = mg.abi.MAVI_STEP_NEWTON
+            self.num_slots = sum(s.num_slots for s in systems)
+
+    r = FakeRunner([lj_grid(mg, 16, 16, chunks=(6, 6))])
+    for nthreads in (1, 2):
+        out = bench.cpu_baseline(mg, orc, r, 0.2, nthreads)
+        assert out["value"] > 0 and out["cores"] == nthreads and out["kind"] == "port"
+        assert ("Threaded" in out["sample"]) == (nthreads > 1)
