@@ -334,6 +334,15 @@ static void sort_records(std::vector<InvRecord>& r) {
 
 int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sources) {
     if (due.empty()) return MAVI_OK;
+    constexpr size_t kMaxGridY = 65535;   // the replicas of one check ride on gridDim.y
+    if (due.size() > kMaxGridY) {
+        for (size_t a = 0; a < due.size(); a += kMaxGridY) {
+            std::vector<int32_t> part(due.begin() + a, due.begin() + std::min(due.size(), a + kMaxGridY));
+            int rc = run_invasions(s, part, from_sources);
+            if (rc) return rc;
+        }
+        return MAVI_OK;
+    }
     MaviSystem::InvBuffers& b = s->invb;
     std::vector<InvRepD> reps(due.size());
     int32_t max_rings = 0;
