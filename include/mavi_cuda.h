@@ -306,8 +306,14 @@ int mavi_set_seed(MaviSystem* sys, uint64_t seed);
  * pe_mode: MAVI_PE_STENCIL or MAVI_PE_ALL_PAIRS. Outputs num_replicas doubles. */
 int mavi_energies(MaviSystem* sys, int32_t pe_mode, double* ke, double* pe);
 
-/* time_info (src/systems.jl:30-33, src/integration.jl:500-503). */
+/* time_info (src/systems.jl:30-33, src/integration.jl:500-503) of replica 0. */
 int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
+/* Start one replica's clock at a system's time_info (a System constructed
+ * with `time_info`, src/systems.jl:84-87, e.g. a loaded one); a handle
+ * starts at TimeInfo(0, 0.0). Call before mavi_rings_invasions_config, whose
+ * last_check is the step count at that call. Device noise does not depend on
+ * it. */
+int mavi_set_time(MaviSystem* sys, int32_t replica, int64_t num_steps, double time);
 
 /* Particle neighbour lists of the rings model (NeighborsCfg / ParticleNeighbors,
  * src/rings/neighbors.jl:8-136, src/rings/rings.jl:143-158): with enable != 0,

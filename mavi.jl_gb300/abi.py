@@ -209,6 +209,7 @@ SIGNATURES = {
     "mavi_set_seed": (C.c_int, [_vp, C.c_uint64]),
     "mavi_energies": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
     "mavi_get_time": (C.c_int, [_vp, C.POINTER(C.c_int64), _dp]),
+    "mavi_set_time": (C.c_int, [_vp, C.c_int32, C.c_int64, C.c_double]),
     "mavi_get_stats": (C.c_int, [_vp, C.POINTER(MaviStats)]),
     "mavi_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "mavi_profile_read": (C.c_int, [_vp, C.POINTER(MaviProfile)]),

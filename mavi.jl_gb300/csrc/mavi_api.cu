@@ -1086,6 +1086,13 @@ int mavi_get_time(MaviSystem* s, int64_t* num_steps, double* time) {
     return MAVI_OK;
 }
 
+int mavi_set_time(MaviSystem* s, int32_t replica, int64_t num_steps, double time) {
+    if (!s || replica < 0 || replica >= s->R || num_steps < 0) return MAVI_ERR_INVALID_ARG;
+    s->num_steps[replica] = num_steps;
+    s->time[replica] = time;
+    return MAVI_OK;
+}
+
 int mavi_rings_neighbors_config(MaviSystem* s, int32_t enable, int32_t only_count, int32_t type_all, double tol) {
     if (!s) return MAVI_ERR_INVALID_ARG;
     if (!s->is_rings) return fail(s, MAVI_ERR_UNSUPPORTED, "particle neighbour lists belong to the rings model");

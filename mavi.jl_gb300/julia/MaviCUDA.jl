@@ -274,6 +274,9 @@ function handle!(system)
     h = Handle(out[])
     finalizer(x -> ccall((:mavi_destroy, libmavi), Cint, (Ptr{Cvoid},), x.ptr), h)
     HANDLES[system] = h
+    # the handle's clock starts at the system's time_info (a loaded system keeps its count)
+    check(ccall((:mavi_set_time, libmavi), Cint, (Ptr{Cvoid}, Int32, Int64, Float64),
+                h.ptr, 0, system.time_info.num_steps, system.time_info.time), "mavi_set_time", h.ptr)
     st isa Rings.RingsState && configure_sources!(system, h.ptr)
     st isa Rings.RingsState && configure_invasions!(system, h.ptr)
     return h.ptr

@@ -135,7 +135,10 @@ class _Handle:
         _check(self.lib, None, st, "mavi_create")
         self.slot_offsets = np.cumsum([0] + [s.num_slots for s in self.systems])
         self.pol_offsets = np.cumsum([0] + [s.num_pol for s in self.systems])
-        for k, s in enumerate(self.systems):   # per-replica configuration (rings sources and sinks)
+        for k, s in enumerate(self.systems):   # per-replica clocks, then configuration (rings)
+            ti = s.time_info
+            if ti.num_steps or ti.time:
+                self.check(self.lib.mavi_set_time(self.handle, k, int(ti.num_steps), float(ti.time)), "mavi_set_time")
             hook = getattr(s, "_configure_replica", None)
             if hook is not None:
                 hook(self, k)

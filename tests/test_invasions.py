@@ -361,3 +361,25 @@ def test_invasions_config_errors(mg):
     h.check(h.lib.mavi_rings_invasions(h.handle, 0, None, 0, C.byref(n), C.byref(last)), "read")
     assert n.value == 0
     s.close()
+
+
+@pytest.mark.gpu
+def test_invasions_start_from_time_info(mg):
+    """A system constructed with a time_info (e.g. a loaded one) keeps its step
+    count on the device: last_check starts there and the schedule follows it."""
+    s = _with_invasions(mg, _overlapped(mg), 3, mg.ChunksCfg(3, 3))
+    s.time_info = mg.system.TimeInfo(num_steps=100, time=1.0)
+    assert _gpu_list(s) == ([], 100)
+    h = s._ensure()
+    nc = h.noise_count()
+    rng = np.random.default_rng(4)
+    s.run(3, noise=rng.standard_normal(3 * nc))
+    assert _gpu_list(s)[1] == 100                         # steps at num_steps 100..102 do not check
+    s.run(1, noise=rng.standard_normal(nc))
+    lst, last = _gpu_list(s)
+    assert last == 103 and len(lst) > 0
+    n, t = C.c_int64(), C.c_double()
+    h.check(h.lib.mavi_get_time(h.handle, C.byref(n), C.byref(t)), "time")
+    assert n.value == 104 == s.time_info.num_steps
+    assert t.value == s.time_info.time
+    s.close()
