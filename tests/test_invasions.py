@@ -33,28 +33,29 @@ def _winding_inside(p, poly):
     return w != 0
 
 
-def _find(rp, r1, r2, nmax, out):
+def _find(rp, r1, r2, nmax, out, ns):
     for a, b in ((r1, r2), (r2, r1)):
-        for i, p in enumerate(rp[a]):
-            if _winding_inside(p, rp[b]):
+        for i, p in enumerate(rp[a][:ns[a]]):
+            if _winding_inside(p, rp[b][:ns[b]]):
                 out.append((a + 1, b + 1, a * nmax + i + 1))
 
 
-def _expected(rp, grid=None, bbox=None):
+def _expected(rp, grid=None, bbox=None, ns=None):
     """check_invasions! with the winding-number membership: all pairs of ring
     ids, or the ring-chunk traversal (columns outer, rows inner, later rings
     of the chunk, then the neighbour chunks of an open grid)."""
     nr, nmax = rp.shape[0], rp.shape[1]
+    ns = [nmax] * nr if ns is None else list(ns)
     out = []
     if grid is None:
         for r1 in range(nr):
             for r2 in range(r1 + 1, nr):
-                _find(rp, r1, r2, nmax, out)
+                _find(rp, r1, r2, nmax, out, ns)
         return out
     cols, rows = grid
     blx, bly, L, H = bbox
     cl, ch = L / cols, H / rows
-    cms = rp.mean(axis=1)
+    cms = np.stack([rp[r][:ns[r]].mean(axis=0) for r in range(nr)])
     lists = {}
     for r in range(nr):
         row = int((-cms[r, 1] + bly + H) // ch) + 1
@@ -75,10 +76,10 @@ def _expected(rp, grid=None, bbox=None):
             chunk = lists.get((row, col), [])
             for i, r1 in enumerate(chunk):
                 for r2 in chunk[i + 1:]:
-                    _find(rp, r1, r2, nmax, out)
+                    _find(rp, r1, r2, nmax, out, ns)
                 for nb in nbrs(row, col):
                     for r2 in lists.get(nb, []):
-                        _find(rp, r1, r2, nmax, out)
+                        _find(rp, r1, r2, nmax, out, ns)
     return out
 
 
@@ -157,6 +158,40 @@ def test_random_rings_chunk_traversal(mg, orc, seed):
     s2 = _system(mg, rp, invasions=mg.rings.InvasionsCfg(0))
     full, _ = orc.from_system(s2).rings_invasions()
     assert sorted(lst) == sorted(full)
+
+
+def _typed(mg, seed, nr=30, ns=(12, 7), box=20.0):
+    """Two ring types of different sizes (rows past a ring's size are padding)."""
+    R = mg.rings
+    rng = np.random.default_rng(seed)
+    types = rng.integers(1, 3, nr)
+    c = rng.uniform(2.0 - box / 2, box / 2 - 2.0, size=(nr, 2))
+    rp = np.zeros((nr, max(ns), 2))
+    for k in range(nr):
+        n = ns[types[k] - 1]
+        rp[k, :n] = _ring(c[k], 1.2 * rng.uniform(0.8, 1.2), n, rng.uniform(0, 2 * np.pi))
+        rp[k, n:] = rp[k, 0]
+    inter = mg.HarmTruncCfg(k_rep=13.0, k_atr=0.1, dist_eq=1.0, dist_max=1.1)
+    cfg = R.RingsCfg(p0=3.5, relax_time=1.0, vo=1.0, mobility=1.0, rot_diff=0.5, k_area=1.0, k_spring=20.0,
+                     l_spring=[0.8, 0.8], num_particles=list(ns),
+                     interaction_finder=R.InteractionMatrix([[inter, inter], [inter, inter]]))
+    st = R.RingsState(rp, np.zeros(nr), num_particles=list(ns), types=list(types))
+    space = mg.SpaceCfg(_container(mg), mg.CircleCfg(0.71 * box, (0.0, 0.0)))
+    return rp, [ns[q - 1] for q in types], space, cfg, st
+
+
+@pytest.mark.parametrize("chunks", [None, (4, 3)])
+def test_two_ring_types(mg, orc, chunks):
+    """Rings of two sizes: each polygon is its own type's points only, and
+    p_id counts rows of nmax."""
+    R = mg.rings
+    rp, ns, space, cfg, st = _typed(mg, 11)
+    rc = mg.ChunksCfg(*chunks) if chunks else None
+    s = R.RingsSystem(st, space, cfg, R.RingsIntCfg(dt=0.001, r_chunks_cfg=rc, invasions_cfg=R.InvasionsCfg(0),
+                                                    device=mg.CUDADevice(noise="injected")))
+    lst, _ = orc.from_system(s).rings_invasions()
+    exp = _expected(rp, grid=chunks, bbox=_CIRCLE_BBOX if chunks else None, ns=ns)
+    assert lst == exp and len(exp) > 5
 
 
 def test_check_schedule_and_last_check(mg, orc):
@@ -382,4 +417,23 @@ def test_invasions_start_from_time_info(mg):
     h.check(h.lib.mavi_get_time(h.handle, C.byref(n), C.byref(t)), "time")
     assert n.value == 104 == s.time_info.num_steps
     assert t.value == s.time_info.time
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("chunks", [None, (4, 3)])
+def test_two_ring_types_gpu(mg, orc, chunks):
+    R = mg.rings
+    rp, ns, space, cfg, st = _typed(mg, 11)
+    rc = mg.ChunksCfg(*chunks) if chunks else None
+    s = R.RingsSystem(st, space, cfg, R.RingsIntCfg(dt=0.001, r_chunks_cfg=rc, invasions_cfg=R.InvasionsCfg(0),
+                                                    device=mg.CUDADevice(noise="injected")))
+    o = orc.from_system(s)
+    assert _gpu_list(s) == o.rings_invasions()
+    rng = np.random.default_rng(6)
+    for _ in range(3):
+        z = rng.standard_normal(o.noise_count())
+        s.run(1, noise=z)
+        o.step(1, orc.SEQUENTIAL, z)
+        assert _gpu_list(s) == o.rings_invasions()
     s.close()
