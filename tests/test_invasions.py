@@ -437,3 +437,27 @@ def test_two_ring_types_gpu(mg, orc, chunks):
         o.step(1, orc.SEQUENTIAL, z)
         assert _gpu_list(s) == o.rings_invasions()
     s.close()
+
+
+def _wrap(rp, box):
+    return (rp + box / 2) % box - box / 2
+
+
+def test_periodic_polygons_are_unwrapped_per_ring(mg, orc):
+    """With periodic walls each ring's polygon is its continuous positions,
+    unwrapped from its own first particle (update_continuos_pos!,
+    src/rings/integration.jl:118-138), and no image of the other ring is
+    taken: two rings that overlap across the boundary are in different frames
+    and report nothing, while the same pair away from the boundary does."""
+    n, box = 10, 20.0
+    a = _ring((9.3, 0.05), 1.0, n, np.pi / 2)       # first particle at (9.3, 1.05): inside the box
+    b = _ring((10.9, -0.02), 1.0, n, np.pi / 2 + 0.1)
+    across = _wrap(np.stack([a, b]), box)           # b sits at the left edge, a straddles the right one
+    inside = np.stack([a, b]) - np.array([5.0, 0.0])
+    for rp, expect_none in ((across, True), (inside, False)):
+        s = _system(mg, rp, box=box, wall="periodic", invasions=mg.rings.InvasionsCfg(0))
+        lst, _ = orc.from_system(s).rings_invasions()
+        if expect_none:
+            assert lst == []
+        else:
+            assert lst == _expected(rp) and len(lst) > 0
