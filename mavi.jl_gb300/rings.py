@@ -432,8 +432,7 @@ class RingsSystem(System):
     def invasions(self) -> InvasionsInfo:
         """RingsInfo.invasions: the list of the last check (every check's,
         appended, without ring chunks) and last_check."""
-        h = self._batch.handle if getattr(self, "_batch", None) is not None else self._ensure()
-        k = h.systems.index(self)
+        h, k = self._replica()
         n, last = C.c_int64(), C.c_int64()
         h.check(h.lib.mavi_rings_invasions(h.handle, k, None, 0, C.byref(n), C.byref(last)), "mavi_rings_invasions")
         out = (abi.MaviInvasion * max(n.value, 1))()
@@ -442,23 +441,31 @@ class RingsSystem(System):
         return InvasionsInfo([Invasion(out[q].invasor, out[q].invaded, out[q].p_id) for q in range(n.value)],
                              int(last.value))
 
+    def _replica(self):
+        """(handle, replica index) of this system: its own handle, or the
+        SystemBatch's that drives it."""
+        b = getattr(self, "_batch", None)
+        if b is not None:
+            return b.handle, b.handle.systems.index(self)
+        return self._ensure(), 0
+
     def areas(self) -> np.ndarray:
         """RingsInfo.areas (src/rings/integration.jl:140-160): ring areas at
         the last force evaluation."""
-        h = self._ensure()
+        h, k = self._replica()
         out = np.zeros(self.state.num_rings)
-        h.check(h.lib.mavi_rings_areas(h.handle, 0, abi.as_dptr(out)), "mavi_rings_areas")
+        h.check(h.lib.mavi_rings_areas(h.handle, k, abi.as_dptr(out)), "mavi_rings_areas")
         return out
 
     def rings_ids(self):
         """(active_mask[num_rings] bool, uids[num_rings], num_active) on the
         device (VarRingsIds: mask, uids, num_active)."""
-        h = self._ensure()
+        h, k = self._replica()
         nr = self.state.num_rings
         mask = np.zeros(nr, dtype=np.int32)
         uids = np.zeros(nr, dtype=np.int32)
         na = C.c_int32()
-        h.check(h.lib.mavi_rings_active(h.handle, 0, abi.as_iptr(mask), abi.as_iptr(uids), C.byref(na)),
+        h.check(h.lib.mavi_rings_active(h.handle, k, abi.as_iptr(mask), abi.as_iptr(uids), C.byref(na)),
                 "mavi_rings_active")
         return mask.astype(bool), uids, int(na.value)
 

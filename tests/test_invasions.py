@@ -383,6 +383,12 @@ def test_invasions_in_a_batch_of_replicas(mg, orc):
         ob.step(1, orc.SEQUENTIAL, zb)
         assert _gpu_list(a) == oa.rings_invasions()
         assert _gpu_list(b) == ob.rings_invasions()
+    # the other rings accessors read a batched system's own replica too
+    for s_, o in ((a, oa), (b, ob)):
+        ar, ra = s_.areas(), o.areas(nr)
+        assert np.max(np.abs(ar - ra) / np.abs(ra)) < 1e-10
+        mask, uids, na = s_.rings_ids()
+        assert mask.all() and na == nr and np.array_equal(uids, np.arange(1, nr + 1))
     batch.close()
 
 
