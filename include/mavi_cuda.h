@@ -311,8 +311,10 @@ int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);
 /* Start one replica's clock at a system's time_info (a System constructed
  * with `time_info`, src/systems.jl:84-87, e.g. a loaded one); a handle
  * starts at TimeInfo(0, 0.0). Call before mavi_rings_invasions_config, whose
- * last_check is the step count at that call. Device noise does not depend on
- * it. */
+ * last_check is the step count at that call. The device noise counter
+ * (Philox key = seed, counter = step) follows replica 0's count, so a run
+ * resumed from a checkpoint with its seed continues the noise stream where it
+ * stopped (as the reference's serialized RNG does) instead of replaying it. */
 int mavi_set_time(MaviSystem* sys, int32_t replica, int64_t num_steps, double time);
 
 /* Particle neighbour lists of the rings model (NeighborsCfg / ParticleNeighbors,

@@ -1090,6 +1090,12 @@ int mavi_set_time(MaviSystem* s, int32_t replica, int64_t num_steps, double time
     if (!s || replica < 0 || replica >= s->R || num_steps < 0) return MAVI_ERR_INVALID_ARG;
     s->num_steps[replica] = num_steps;
     s->time[replica] = time;
+    if (replica == 0) {
+        // the noise counter: steps completed, as every step's chunk update advances it
+        const int64_t v = num_steps;
+        CUDA_TRY(s, cudaMemcpyAsync(s->C.d_step, &v, sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+    }
     return MAVI_OK;
 }
 

@@ -182,6 +182,9 @@ class _Handle:
             pol = np.ascontiguousarray(np.concatenate([s.state.pol_array() for s in self.systems]))
         self.check(self.lib.mavi_upload_state(self.handle, abi.as_dptr(pos), abi.as_dptr(vel), abi.as_dptr(pol)),
                    "mavi_upload_state")
+        for k, s in enumerate(self.systems):   # and the clocks (a restored checkpoint's time_info)
+            ti = s.time_info
+            self.check(self.lib.mavi_set_time(self.handle, k, int(ti.num_steps), float(ti.time)), "mavi_set_time")
 
     def noise_count(self) -> int:
         return int(self.lib.mavi_noise_count(self.handle))

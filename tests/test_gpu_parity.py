@@ -440,3 +440,23 @@ def test_line_walls(mg, orc, kind, potential, precision):
     assert np.max(np.abs(s.state.pos - p)) < tol
     assert np.max(np.abs(s.state.vel - v)) < tol * 10
     s.close()
+
+
+def test_resume_continues_the_device_noise(mg):
+    """A system rebuilt from a snapshot (state + time_info) continues the
+    device noise where the first run was (Philox counter = steps done), so the
+    resumed trajectory equals the uninterrupted one bit for bit."""
+    a = self_propelled(mg, "szabo", noise="device")
+    a.run(20)
+    pos, pol = a.state.pos.copy(), a.state.pol.copy()
+    ti = mg.system.TimeInfo(num_steps=a.time_info.num_steps, time=a.time_info.time)
+    a.run(20)
+    c = self_propelled(mg, "szabo", noise="device")
+    c.state.pos[...] = pos
+    c.state.pol[...] = pol
+    c.time_info = ti
+    c.run(20)
+    assert c.time_info.num_steps == a.time_info.num_steps == 40
+    assert np.array_equal(c.state.pos, a.state.pos) and np.array_equal(c.state.pol, a.state.pol)
+    a.close()
+    c.close()
