@@ -26,6 +26,25 @@ def test_ctypes_signatures_cover_header(mg):
     assert set(header_functions()) == set(abi.SIGNATURES)
 
 
+def header_arity():
+    """{entry point: number of parameters} from the prototypes of the header."""
+    text = (ROOT / "include" / "mavi_cuda.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(mavi_[a-z_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_ctypes_signatures_have_the_prototypes_arity(mg):
+    from mavi_gb300 import abi
+    arity = header_arity()
+    assert set(arity) == set(abi.SIGNATURES)
+    for name, (_, args) in abi.SIGNATURES.items():
+        assert len(args) == arity[name], (name, len(args), arity[name])
+
+
 def test_struct_layout_matches_c(mg, orc):
     from mavi_gb300 import abi
     sizes = orc.struct_sizes()

@@ -95,3 +95,16 @@ def test_julia_shim_binds_declared_entry_points():
     header = (ROOT / "include" / "mavi_cuda.h").read_text()
     for name in set(re.findall(r"ccall\(\(:(\w+), libmavi\)", text)):
         assert re.search(rf"\b{name}\s*\(", header), f"{name} is not declared in include/mavi_cuda.h"
+
+
+def test_julia_ccalls_have_the_prototypes_arity():
+    """Every ccall's argument-type tuple has as many entries as the C
+    prototype has parameters (the shim is not executed here)."""
+    from test_abi import header_arity
+    arity = header_arity()
+    text = SHIM.read_text()
+    calls = re.findall(r"ccall\(\(:(\w+), libmavi\),\s*\w+,\s*\(([^()]*)\)", text)
+    assert len(calls) >= 10
+    for name, types in calls:
+        n = len([x for x in types.split(",") if x.strip()])
+        assert n == arity[name], (name, n, arity[name])
