@@ -77,3 +77,9 @@ def test_product_never_imports_the_oracle():
     pkg = ROOT / "mavi.jl_gb300"
     for p in list(pkg.rglob("*.py")) + list(pkg.rglob("*.cu")) + list(pkg.rglob("*.cuh")):
         assert "oracle" not in p.read_text().lower().replace("oracle/", ""), p
+
+
+def test_integration_guide_names_every_entry_point():
+    text = (ROOT / "INTEGRATION.md").read_text()
+    missing = [n for n in header_functions() if f"`{n}`" not in text]
+    assert not missing, missing
