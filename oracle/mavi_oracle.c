@@ -1523,6 +1523,12 @@ int32_t oracle_get_time(OracleSys* s, int64_t* num_steps, double* time) {
     return MAVI_OK;
 }
 
+/* A System constructed with a time_info (src/systems.jl:84-87). */
+int32_t oracle_set_time(OracleSys* s, int64_t num_steps, double time) {
+    s->num_steps = num_steps; s->time = time;
+    return MAVI_OK;
+}
+
 int32_t oracle_get_areas(OracleSys* s, double* areas) {
     if (!s->areas) return MAVI_ERR_INVALID_ARG;
     memcpy(areas, s->areas, sizeof(double) * s->num_rings);

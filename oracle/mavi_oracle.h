@@ -49,6 +49,7 @@ int32_t oracle_get_state(OracleSys* s, double* pos, double* vel, double* pol);
 int32_t oracle_set_state(OracleSys* s, const double* pos, const double* vel, const double* pol);
 int32_t oracle_energies(OracleSys* s, int32_t pe_mode, double* ke, double* pe);
 int32_t oracle_get_time(OracleSys* s, int64_t* num_steps, double* time);
+int32_t oracle_set_time(OracleSys* s, int64_t num_steps, double time);
 int32_t oracle_get_areas(OracleSys* s, double* areas);
 int64_t oracle_count_pairs(OracleSys* s);
 int32_t oracle_rings_neighbors(OracleSys* s, double tol, int32_t type_all, int32_t max_list, int32_t* counts,

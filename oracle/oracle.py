@@ -52,6 +52,7 @@ def _load_lib():
         "oracle_set_state": (C.c_int32, [vp, dp, dp, dp]),
         "oracle_energies": (C.c_int32, [vp, C.c_int32, dp, dp]),
         "oracle_get_time": (C.c_int32, [vp, lp, dp]),
+        "oracle_set_time": (C.c_int32, [vp, C.c_int64, C.c_double]),
         "oracle_get_areas": (C.c_int32, [vp, dp]),
         "oracle_count_pairs": (C.c_int64, [vp]),
         "oracle_rings_neighbors": (C.c_int32, [vp, C.c_double, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
@@ -277,6 +278,9 @@ def from_system(system, nthreads: int = 1, step_kind=None) -> OracleSystem:
     pol = st.pol_array()
     types = st.types_array() if getattr(system, "is_rings", False) else None
     o = OracleSystem(p, st.pos, vel, pol, types, nthreads=nthreads)
+    ti = getattr(system, "time_info", None)
+    if ti is not None and (ti.num_steps or ti.time):
+        o.lib.oracle_set_time(o.h, int(ti.num_steps), float(ti.time))
     src = system.sources_abi() if hasattr(system, "sources_abi") else None
     if src is not None:
         o.rings_sources(*src)

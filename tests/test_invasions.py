@@ -208,6 +208,23 @@ def test_check_schedule_and_last_check(mg, orc):
     assert seen == [0, 0, 0, 3, 3, 3, 6, 6]
 
 
+def test_check_schedule_from_a_time_info(mg, orc):
+    """A system constructed with a time_info: last_check starts at its
+    num_steps (src/rings/rings.jl:276-278) and the checks follow from there."""
+    rp = _random_rings(6)
+    s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(3), r_chunks=mg.ChunksCfg(4, 4))
+    s.time_info = mg.system.TimeInfo(num_steps=100, time=1.0)
+    o = orc.from_system(s)
+    assert o.rings_invasions() == ([], 100)
+    rng = np.random.default_rng(0)
+    seen = []
+    for _ in range(8):
+        o.step(1, orc.SEQUENTIAL, rng.standard_normal(o.noise_count()))
+        seen.append(o.rings_invasions()[1])
+    assert seen == [100, 100, 100, 103, 103, 103, 106, 106]
+    assert o.time()[0] == 108
+
+
 def test_all_pairs_list_is_never_emptied(mg, orc):
     rp = _random_rings(7)
     s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(1))
