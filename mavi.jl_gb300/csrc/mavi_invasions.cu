@@ -389,6 +389,8 @@ int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sour
         D.rec = static_cast<InvRecord*>(b.rec);
         D.cap = b.rec_cap;
     }
+    if (nrec > b.rec_cap)   // the second pass finds what the first did; never copy past the buffer
+        return fail(s, MAVI_ERR_CUDA, "invasion records: %d found, room for %lld", nrec, (long long)b.rec_cap);
     std::vector<InvRecord> rec((size_t)nrec);
     if (nrec > 0)
         CUDA_TRY(s, cudaMemcpyAsync(rec.data(), b.rec, sizeof(InvRecord) * nrec, cudaMemcpyDeviceToHost, s->stream));
