@@ -484,3 +484,18 @@ def test_periodic_polygons_are_unwrapped_per_ring(mg, orc):
             assert lst == []
         else:
             assert lst == _expected(rp) and len(lst) > 0
+
+
+@pytest.mark.gpu
+def test_more_invasions_than_the_record_buffer(mg, orc):
+    """36 rings stacked on one another: ~5,000 invasions in one check, more
+    than the first record buffer holds; the buffer grows and the pairs are
+    visited again, with the same list as the oracle's."""
+    rng = np.random.default_rng(12)
+    rp = np.stack([_ring(rng.uniform(-0.3, 0.3, 2), 1.0 + 0.1 * rng.random(), 10, rng.uniform(0, 2 * np.pi))
+                   for _ in range(36)])
+    s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(0))
+    lst, last = orc.from_system(s).rings_invasions()
+    assert len(lst) > 1024
+    assert _gpu_list(s) == (lst, last)
+    s.close()
