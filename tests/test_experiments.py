@@ -106,3 +106,75 @@ def test_experiment_on_gpu_and_resume_from_checkpoint(mg, tmp_path):
     assert s2.time_info.num_steps == n_full
     assert np.array_equal(s2.state.pos, full)
     s2.close()
+
+
+def _fake_experiment(ex, root, dt=0.01, tf=1.0, delta=0.2):
+    s = FakeSystem(dt)
+    e = ex.Experiment(ex.ExperimentCfg(tf=tf, root=str(root), checkpoint_cfg=ex.CheckpointCfg(delta)),
+                      ex.DelayedCfg(0.05), s, custom_step=types.SimpleNamespace(kind=0))
+    return s, e
+
+
+def test_crash_while_writing_a_checkpoint_resumes_from_the_last_complete_one(mg, tmp_path):
+    """Host-side fault injection (as test/tests_experiments.jl:60-65 does with
+    an `error`): the third checkpoint write fails half-way; the info file still
+    names the last complete checkpoint, and a resumed run ends where an
+    uninterrupted one does."""
+    ex = mg.experiments
+    orig = ex._save_snapshot
+    calls = {"n": 0}
+
+    def failing(snap, path):
+        if "checkpoint" in str(path):
+            calls["n"] += 1
+            if calls["n"] == 3:
+                raise RuntimeError("injected failure while writing a checkpoint")
+        return orig(snap, path)
+    ex._save_snapshot = failing
+    try:
+        s, e = _fake_experiment(ex, tmp_path / "a")
+        with pytest.raises(RuntimeError, match="injected"):
+            ex.run_experiment(e)
+    finally:
+        ex._save_snapshot = orig
+    info = json.loads((tmp_path / "a" / "checkpoint" / "checkpoint_info.json").read_text())
+    assert info["is_valid"] == {"1": True, "2": True}
+    s2 = FakeSystem(0.01)
+    e2 = ex.load_experiment(tmp_path / "a", s2, ex.DelayedCfg(0.05), custom_step=types.SimpleNamespace(kind=0))
+    assert s2.time_info.time == info["last_time"]
+    assert np.all(s2.state.pos == s2.time_info.num_steps)          # the state of that checkpoint
+    e2.cfg = ex.ExperimentCfg(tf=1.0, root=str(tmp_path / "b"), checkpoint_cfg=ex.CheckpointCfg(0.2))
+    ex.run_experiment(e2)
+    ref, ref_e = _fake_experiment(ex, tmp_path / "c")
+    ex.run_experiment(ref_e)
+    assert s2.time_info.num_steps == ref.time_info.num_steps
+    assert np.array_equal(s2.state.pos, ref.state.pos)
+
+
+def test_invalid_checkpoints_are_skipped_or_refused(mg, tmp_path):
+    """load_experiment (src/experiments.jl:490-520): the last used checkpoint
+    if valid, else the other one; neither valid is an error."""
+    ex = mg.experiments
+    s, e = _fake_experiment(ex, tmp_path)
+    ex.run_experiment(e)
+    path = tmp_path / "checkpoint" / "checkpoint_info.json"
+    info = json.loads(path.read_text())
+    last, other = info["last_used"], ("2" if info["last_used"] == "1" else "1")
+    times = {}
+    for name in ("1", "2"):
+        info2 = dict(info, last_used=name, is_valid={"1": True, "2": True})
+        path.write_text(json.dumps(info2))
+        s2 = FakeSystem(0.01)
+        ex.load_experiment(tmp_path, s2, ex.DelayedCfg(0.05), custom_step=types.SimpleNamespace(kind=0))
+        times[name] = s2.time_info.time
+    assert times[last] > times[other]
+    path.write_text(json.dumps(dict(info, is_valid={last: False, other: True})))
+    s3 = FakeSystem(0.01)
+    ex.load_experiment(tmp_path, s3, ex.DelayedCfg(0.05), custom_step=types.SimpleNamespace(kind=0))
+    assert s3.time_info.time == times[other]
+    path.write_text(json.dumps(dict(info, is_valid={"1": False, "2": False})))
+    with pytest.raises(RuntimeError, match="corrupted"):
+        ex.load_experiment(tmp_path, FakeSystem(0.01), ex.DelayedCfg(0.05))
+    path.unlink()
+    with pytest.raises(FileNotFoundError):
+        ex.load_experiment(tmp_path, FakeSystem(0.01), ex.DelayedCfg(0.05))
