@@ -218,6 +218,34 @@ def test_outside_space_rejected_at_creation(mg):
     assert e.value.status == mg.abi.MAVI_ERR_OUTSIDE_SPACE
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_non_finite_position_reports_error(mg, precision):
+    """A NaN position is turned into MAVI_ERR_NONFINITE by the binning's own
+    check (the chunk index is clamped, no access leaves the arrays); the
+    handle stays usable once the state is repaired."""
+    s = lj_grid(mg, 8, 8, wall="periodic", chunks=(4, 4), precision=precision)
+    s.calc_forces()
+    good = s.state.pos[5].copy()
+    s.state.pos[5] = (np.nan, 1.0)
+    s.upload()
+    with pytest.raises(mg.MaviError) as e:
+        s.calc_forces()
+    assert e.value.status == mg.abi.MAVI_ERR_NONFINITE
+    s.state.pos[5] = good
+    s.upload()
+    s.calc_forces()
+    s.close()
+
+
+def test_injected_noise_missing_is_refused_before_any_launch(mg):
+    s = self_propelled(mg, "szabo", noise="injected")
+    h = s._ensure()
+    assert h.lib.mavi_step(h.handle, 3) == mg.abi.MAVI_ERR_NOISE_MISSING
+    s.run(1, noise=np.zeros(h.noise_count()))           # one step of noise: one step runs
+    assert s.time_info.num_steps == 1
+    s.close()
+
+
 def test_chunk_overflow_reports_error(mg):
     s = soft_disks(mg, 256, phi=0.3)
     s.state.pos[:60] = s.state.pos[0]
