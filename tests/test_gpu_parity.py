@@ -476,15 +476,15 @@ def test_resume_continues_the_device_noise(mg):
     resumed trajectory equals the uninterrupted one bit for bit."""
     a = self_propelled(mg, "szabo", noise="device")
     a.run(20)
-    pos, pol = a.state.pos.copy(), a.state.pol.copy()
+    pos, pol = a.state.pos.copy(), a.state.pol_angle.copy()
     ti = mg.system.TimeInfo(num_steps=a.time_info.num_steps, time=a.time_info.time)
     a.run(20)
     c = self_propelled(mg, "szabo", noise="device")
     c.state.pos[...] = pos
-    c.state.pol[...] = pol
+    c.state.pol_angle[...] = pol
     c.time_info = ti
     c.run(20)
     assert c.time_info.num_steps == a.time_info.num_steps == 40
-    assert np.array_equal(c.state.pos, a.state.pos) and np.array_equal(c.state.pol, a.state.pol)
+    assert np.array_equal(c.state.pos, a.state.pos) and np.array_equal(c.state.pol_angle, a.state.pol_angle)
     a.close()
     c.close()
