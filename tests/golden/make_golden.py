@@ -12,6 +12,11 @@ Contents:
   * lj_pair / harm_pair: two-particle forces from the closed forms
     (src/configs.jl:354-368, 389-397).
   * grid: rectangular_grid corner positions and box (src/init_states.jl:34-57).
+  * invasions: rings with dyadic vertex coordinates (multiples of 1/64, so
+    every binary64 operation of point_line_intersect lands on the exact
+    comparison outcome) and the invasion list check_invasions!(system,
+    ::Nothing) pushes (src/rings/integration.jl:378-470, 497-507), with the
+    ray crossings decided in exact rational arithmetic.
 
 Run: python tests/golden/make_golden.py
 """
@@ -88,8 +93,51 @@ def main():
     ans["grid"] = {"nx": 32, "ny": 32, "offset": 0.4, "radius": r,
                    "first": [-r + r * (2 + 0.4), r * (0.4 + 1)],
                    "length": 32 * 2 * r + r * 0.4 * 33}
+    ans["invasions"] = invasion_cases()
     OUT.write_text(json.dumps(ans, indent=1))
     print(f"wrote {OUT}")
+
+
+def crosses(p, a, b):
+    """point_line_intersect with exact rationals: the ray from p towards +x
+    crosses edge a-b strictly inside both ranges."""
+    dx, dy = b[0] - a[0], b[1] - a[1]
+    ylo, yhi = (b[1], a[1]) if dy < 0 else (a[1], b[1])
+    if dx == 0:
+        return a[0] > p[0] and ylo < p[1] < yhi
+    if dy == 0:
+        return False
+    x_inter = (dy * a[0] - dx * a[1] + dx * p[1]) / dy
+    xlo, xhi = (b[0], a[0]) if dx < 0 else (a[0], b[0])
+    return x_inter > p[0] and xlo < x_inter < xhi and ylo < p[1] < yhi
+
+
+def invasion_cases():
+    import random
+    rnd = random.Random(2024)
+    cases = []
+    for _ in range(3):
+        nr, n = 6, 7
+        rings = []
+        for _ in range(nr):
+            cx, cy = Fraction(rnd.randint(-192, 192), 64), Fraction(rnd.randint(-192, 192), 64)
+            pts = []
+            for k in range(n):
+                ang = 2 * math.pi * k / n + rnd.random() * 0.3
+                rad = 1.0 + rnd.random() * 0.5
+                pts.append((cx + Fraction(round(rad * math.cos(ang) * 64), 64),
+                            cy + Fraction(round(rad * math.sin(ang) * 64), 64)))
+            rings.append(pts)
+        out = []
+        for r1 in range(nr):
+            for r2 in range(r1 + 1, nr):
+                for a, b in ((r1, r2), (r2, r1)):
+                    for i, p in enumerate(rings[a]):
+                        c = sum(crosses(p, rings[b][e], rings[b][(e + 1) % n]) for e in range(n))
+                        if c % 2:
+                            out.append([a + 1, b + 1, a * n + i + 1])
+        cases.append({"rings_pos": [[[float(x), float(y)] for x, y in r] for r in rings], "invasions": out})
+    return cases
 
 
 if __name__ == "__main__":

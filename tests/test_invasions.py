@@ -138,6 +138,20 @@ def test_known_answer_two_rings(mg, orc):
     assert last == 0
 
 
+def test_golden_invasions_exact(mg, orc):
+    """Known answers decided in exact rational arithmetic on dyadic vertices
+    (tests/golden/make_golden.py): the oracle's FP64 list equals them."""
+    import json
+    from conftest import ROOT
+    gold = json.loads((ROOT / "tests" / "golden" / "known_answers.json").read_text())["invasions"]
+    assert len(gold) == 3
+    for case in gold:
+        rp = np.asarray(case["rings_pos"], dtype=np.float64)
+        s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(0))
+        lst, _ = orc.from_system(s).rings_invasions()
+        assert lst == [tuple(v) for v in case["invasions"]] and len(lst) > 0
+
+
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_random_rings_all_pairs(mg, orc, seed):
     rp = _random_rings(seed)
@@ -499,3 +513,21 @@ def test_more_invasions_than_the_record_buffer(mg, orc):
     assert len(lst) > 1024
     assert _gpu_list(s) == (lst, last)
     s.close()
+
+
+@pytest.mark.gpu
+def test_golden_invasions_exact_gpu(mg):
+    """The CUDA check against the exact known answers, with and without ring
+    chunks (one 4 x 4 grid holds every pair as neighbours here)."""
+    import json
+    from conftest import ROOT
+    gold = json.loads((ROOT / "tests" / "golden" / "known_answers.json").read_text())["invasions"]
+    for case in gold:
+        rp = np.asarray(case["rings_pos"], dtype=np.float64)
+        want = [tuple(v) for v in case["invasions"]]
+        s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(0))
+        assert _gpu_list(s) == (want, 0)
+        s.close()
+        s = _system(mg, rp, invasions=mg.rings.InvasionsCfg(0), r_chunks=mg.ChunksCfg(4, 4))
+        assert sorted(_gpu_list(s)[0]) == sorted(want)
+        s.close()
