@@ -1,11 +1,16 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 step loop: particle-steps/s of the mixed-precision
-form and of the plain FP64 drop-in on one workload, through libmavi_cuda.so.
+batched form and of the plain FP64 drop-in on one workload, through
+libmavi_cuda.so.
 
-Default workload (one GPU): 262,144 harmonic-truncated soft disks, periodic
-box at area fraction 0.70, relaxed by 200 overdamped steps, overdamped
-dt = 1e-2 (see mavi.jl_gb300/workloads.py). A "step" is one whole step of the
-step loop (chunk rebuild -> pair forces -> integration -> walls).
+Default workload (one GPU): 512 independent 2D Lennard-Jones replicas of
+uneven N (log-uniform in [1000, 65536], 7,871,648 particles in total),
+density 0.6, rigid/periodic walls x rectangular/circular geometry, Maxwell
+velocities at T in [0.3, 1.0], velocity Verlet dt = 1e-3, all replicas behind
+one handle (see mavi.jl_gb300/workloads.py). `--workload harm_262144` (one
+large soft-disk system), `lj_4194304` and `rings_64` are the other shapes. A
+"step" is one whole step of the step loop (chunk rebuild -> pair forces ->
+integration -> walls) of every replica.
 
 Timing: W untimed warm-up steps, then K steps; before every timed step a
 256 MiB buffer is written (L2 flush), then one step runs as a CUDA graph whose
@@ -18,8 +23,11 @@ upload state -> one step -> download state, host-timed.
 restatement in oracle/, OpenMP over chunk columns like the reference's
 Threaded mode), on the same workload, a bounded number of steps.
 
-Multi-GPU (torchrun): replicas only — every rank advances its own copy of the
-workload; value = all ranks' particle-steps / max-over-ranks time.
+Multi-GPU (torchrun): replicas only. A batched workload of R replicas per GPU
+becomes R x world replicas (the same seeded generator, continued), split
+between the ranks by particle count (replicas.shard_replicas; weak scaling, no
+data-path collective); a single-system workload runs one copy per rank.
+value = all ranks' particle-steps / max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -51,7 +59,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="harm_262144")
+    ap.add_argument("--workload", default="lj_batch_512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     return ap.parse_args()
@@ -112,10 +120,12 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def launches_per_step(step_kind, abi):
+def launches_per_step(step_kind, abi, precision):
     rebin = 3   # scan, scatter, deterministic per-chunk order + permutation
     body = {abi.MAVI_STEP_NEWTON: 2, abi.MAVI_STEP_OVERDAMPED: 1, abi.MAVI_STEP_SZABO: 1, abi.MAVI_STEP_RTP: 1,
             abi.MAVI_STEP_RINGS: 3}[step_kind]   # rings: pair pass, ring terms + update + histogram, polarisation
+    if step_kind == abi.MAVI_STEP_RINGS and precision == "fp64":
+        body += 1                                # ring areas in the reference's operation order
     return rebin + body
 
 
@@ -130,9 +140,10 @@ class Runner:
     """One workload behind one handle: a single System, or a list of systems
     advanced together as a SystemBatch (replicas in the same launches)."""
 
-    def __init__(self, mg, obj, step):
+    def __init__(self, mg, obj, step, precision):
         self.mg = mg
         self.step = step
+        self.precision = precision
         if isinstance(obj, (list, tuple)):
             self.systems = list(obj)
             self.batch = mg.SystemBatch(self.systems, step)
@@ -215,7 +226,7 @@ def time_form(mg, runner, K, W, flush, torch):
     kinds = {abi.MAVI_KERNEL_NAMES[k]: {"ms": p.ms[k] * K / kb, "launches": int(p.launches[k]) * K // kb}
              for k in range(abi.MAVI_NUM_KERNEL_KINDS) if p.launches[k]}
     return {"total_ms": float(sum(step_ms)), "step_ms": step_ms, "kinds": kinds,
-            "launches_per_step": launches_per_step(h.step_kind, abi),
+            "launches_per_step": launches_per_step(h.step_kind, abi, runner.precision),
             "kernel_breakdown_steps": kb}
 
 
@@ -368,10 +379,20 @@ def cpu_baseline(mg, orc, runner, seconds, nthreads):
                       f"{'Threaded column split' if nthreads > 1 else 'Sequencial'}"}
 
 
-def build_workload(mg, name, precision):
-    W = __import__("mavi_gb300.workloads", fromlist=["WORKLOADS"]).WORKLOADS
+BATCHED = {"lj_batch_512": 512, "rings_64": 64}
+
+
+def build_workload(mg, name, precision, rank=0, world=1):
+    """The workload's handle. Batched workloads under torchrun: R x world
+    replicas, this rank's share by particle count (no exchange between ranks)."""
+    from mavi_gb300 import replicas, workloads
+    W = workloads.WORKLOADS
+    if name in BATCHED and world > 1:
+        obj, step = W[name](precision=precision, num_replicas=BATCHED[name] * world)
+        mine = replicas.my_replicas([s.num_slots for s in obj], rank, world)
+        return Runner(mg, [obj[i] for i in mine], step, precision)
     obj, step = W[name](precision=precision)
-    return Runner(mg, obj, step)
+    return Runner(mg, obj, step, precision)
 
 
 def run_reference_generic(args, mg, orc, workloads, nthreads):
@@ -476,7 +497,8 @@ def main():
     def flush():
         flush_buf.fill_(1.0)
 
-    runners = {precision: build_workload(mg, args.workload, precision) for precision in ("fp64", "mixed")}
+    runners = {precision: build_workload(mg, args.workload, precision, rank, world)
+               for precision in ("fp64", "mixed")}
 
     # force accuracy at the starting state (both forms and the oracle)
     f64 = runners["fp64"].forces()
@@ -495,18 +517,17 @@ def main():
         v = C.c_double()
         fma[prec] = v.value if lib.mavi_fma_peak(code, local_dev, C.byref(v)) == 0 else None
 
-    clocks = Clocks(local)
     meas = {}
+    clk_form = {}
     for precision in ("fp64", "mixed"):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        if precision == "mixed":
-            clocks.start()
+        clocks = Clocks(local)      # sampled around each form's timed region
+        clocks.start()
         m = time_form(mg, runners[precision], args.steps, max(args.warmup, 3), flush, torch)
-        if precision == "mixed":
-            clk = clocks.stop()
         torch.cuda.synchronize()
+        clk_form[precision] = clocks.stop()
         if world > 1:
             t = torch.tensor([m["total_ms"]], device="cuda", dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -550,7 +571,8 @@ def main():
                        "form": "mixed", "chunks": grid, "total_chunks": stats.total_chunks,
                        "candidate_pairs": stats.candidate_pairs,
                        "gather": {0: "staged", 1: "global", 2: "columns"}.get(runners["mixed"].stats().gather_mode),
-                       "parallelism": "replicas" if world > 1 else "single",
+                       "parallelism": (f"replicas split over {world} GPUs" if world > 1 else
+                                       ("replicas" if len(runners["mixed"].systems) > 1 else "single")),
                        "l2": "flushed (256 MiB write) before every timed step"},
             "roofline": mx["roofline"],
             "cpu_baseline": cpu,
@@ -558,8 +580,9 @@ def main():
                     "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
                     "path": "mavi_upload_state -> mavi_step(1) -> mavi_download_state, pinned host buffers"},
             "gpu_launches": mx["gpu_launches"],
-            "clocks": clk,
+            "clocks": clk_form["mixed"],
             "plain_fp64": {"value": line_forms["fp64"]["value"], "ms_per_step": line_forms["fp64"]["ms_per_step"],
+                           "clocks": clk_form["fp64"],
                            "roofline": line_forms["fp64"]["roofline"],
                            "kernels_ms_per_step": line_forms["fp64"]["kernels_ms_per_step"],
                            "gpu_launches": line_forms["fp64"]["gpu_launches"]},

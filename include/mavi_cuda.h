@@ -463,9 +463,14 @@ int mavi_fma_peak(int32_t precision, int32_t device, double* flops_per_s);
  * Scratch is one fixed device array inside the library: at most 1,048,576
  * chunks and a chunk capacity of at most 1024; larger requests return
  * MAVI_ERR_INVALID_ARG with the limit in msg. The first call on a device
- * locates that array (set-up): make it before any stream capture. Every call
- * clears the scratch it uses. Calls on one device share the scratch, so calls
- * that overlap in time race: serialise them per device. */
+ * loads this part of the library on that device (CUDA's lazy module loading),
+ * which reserves the 4 MiB array there, and locates the array (set-up): make
+ * that first call before any stream capture. Later calls allocate nothing.
+ * Every call waits for `stream` before it returns (it reads the status back).
+ * A CUDA error already pending in the calling thread is returned as
+ * MAVI_ERR_CUDA, named as not this call's, before anything is launched.
+ * Every call clears the scratch it uses. Calls on one device share the
+ * scratch, so calls that overlap in time race: serialise them per device. */
 int mavi_chunk_lists_noalloc(const MaviReplicaParams* params, const double* pos_dev, int64_t n,
                              int32_t* start_dev, int32_t* ids_dev, void* stream,
                              char* msg, int32_t msg_len);

@@ -656,6 +656,12 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
                 R.ring_karea_f[t] = (float)(p.rings.k_area[t] * R.u2_d * 0.5);
                 R.ring_ks_f[t] = (float)p.rings.k_spring[t];
                 R.ring_ls_f[t] = (float)p.rings.l_spring[t];
+                const long double ls2 = (long double)p.rings.l_spring[t] * p.rings.l_spring[t] / uu;
+                R.ring_ls2_u[t] = ls2 < 9.0e18L ? (long long)(ls2 + 0.5L) : -1;
+                R.ring_ls2_d[t] = p.rings.l_spring[t] * p.rings.l_spring[t];
+                const double ku = p.rings.k_spring[t] * std::sqrt(R.u2_d), lu = p.rings.l_spring[t] / std::sqrt(R.u2_d);
+                R.ring_ku_h[t] = (float)ku; R.ring_ku_l[t] = (float)(ku - (double)R.ring_ku_h[t]);
+                R.ring_lu_h[t] = (float)lu; R.ring_lu_l[t] = (float)(lu - (double)R.ring_lu_h[t]);
                 R.ring_kb_f[t] = (float)p.rings.k_bend[t];
                 R.ring_vo_f[t] = (float)p.rings.vo[t];
                 R.ring_mu_f[t] = (float)p.rings.mobility[t];

@@ -121,6 +121,13 @@ struct DevRep {
     long long ring_a0x2_hi[MAVI_MAX_TYPES];
     unsigned long long ring_a0x2_lo[MAVI_MAX_TYPES];
     float ring_karea_f[MAVI_MAX_TYPES];
+    // springs without cancellation: l^2 / u^2 rounded to an integer (-1 when it
+    // does not fit int64; the spring then falls back to FP32 L - l) and l^2
+    long long ring_ls2_u[MAVI_MAX_TYPES];
+    double ring_ls2_d[MAVI_MAX_TYPES];
+    // mixed-form springs in float-float: k_spring * u and l / u as (high, low) pairs
+    float ring_ku_h[MAVI_MAX_TYPES], ring_ku_l[MAVI_MAX_TYPES];
+    float ring_lu_h[MAVI_MAX_TYPES], ring_lu_l[MAVI_MAX_TYPES];
     int32_t wall_precheck;          // 0 none, 1 inside mode, 2 repulsion
     long long wall_cx_u, wall_cy_u;
     float wall_lo2_u, wall_hi2_u;
@@ -313,5 +320,56 @@ __device__ __forceinline__ double f32_to_f64_bits(float f) {
     return __hiloint2double((int)hi, (int)(b << 29));
 }
 
+
+// ---------------------------------------------------------------------------
+// Float-float ("double-word") arithmetic on the FP32 pipe: a value is h + l
+// with |l| <= ulp(h) / 2, about 44 bits of precision. The error-free
+// transformations are Knuth's TwoSum, Dekker's FastTwoSum and the FMA-based
+// TwoProd; add, multiply, divide and square root follow the classical
+// double-word algorithms (Dekker 1971; Joldes, Muller, Popescu 2017). The _rn
+// intrinsics keep the compiler from fusing or reordering the operations whose
+// rounding errors are captured.
+// ---------------------------------------------------------------------------
+struct FF { float h, l; };
+
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = ff_two_sum(a.h, b.h);
+    return ff_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q = __fdiv_rn(a.h, b.h);
+    const float ph = __fmul_rn(q, b.h), pl = fmaf(q, b.h, -ph);    // q * b.h exactly
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.h, ph), pl), fmaf(-q, b.l, a.l));
+    return ff_fast_two_sum(q, __fdiv_rn(r, b.h));
+}
+__device__ __forceinline__ FF ff_sqrt(FF a) {
+    const float s = __fsqrt_rn(a.h);
+    const float ph = __fmul_rn(s, s), pl = fmaf(s, s, -ph);        // s^2 exactly
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.h, ph), pl), a.l);
+    return ff_fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
+}
+// An int64 as float-float: three 24-bit limbs, each exact in FP32.
+__device__ __forceinline__ FF ff_from_i64(long long v) {
+    const float c0 = (float)(int32_t)(v & 0xffffff);
+    const float c1 = (float)(int32_t)((v >> 24) & 0xffffff) * 16777216.0f;     // 2^24
+    const float c2 = (float)(int32_t)(v >> 48) * 281474976710656.0f;          // 2^48
+    const FF t = ff_fast_two_sum(c2, c1);
+    const FF u = ff_two_sum(t.h, c0);
+    return ff_fast_two_sum(u.h, __fadd_rn(u.l, t.l));
+}
 
 }  // namespace mavi

@@ -1806,20 +1806,54 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             const float bxf = i64_to_f32(bx) * uf, byf = i64_to_f32(by) * uf;
             const float L = sqrtf(bxf * bxf + byf * byf);
             const float inv = 1.0f / L;
-            const float bmx = __shfl_sync(full, bxf, pm), bmy = __shfl_sync(full, byf, pm);   // bond p-1
-            const float Lm = __shfl_sync(full, L, pm), invm = __shfl_sync(full, inv, pm);
+            const long long bmxi = __shfl_sync(full, bx, pm), bmyi = __shfl_sync(full, by, pm);   // bond p-1
+            const float bmx = __shfl_sync(full, bxf, pm), bmy = __shfl_sync(full, byf, pm);
+            const float invm = __shfl_sync(full, inv, pm);
             const float ks = R.ring_ks_f[t], ls = R.ring_ls_f[t], kbt = R.ring_kb_f[t];
-            const float spf = ks * (L - ls) * inv, smf = ks * (Lm - ls) * invm;
-            float fx = spf * bxf - smf * bmx;
-            float fy = spf * byf - smf * bmy;
+            // Bond components below 2^31 units keep the squares and the cross
+            // products of the exact integer bonds inside int64, so the two
+            // quantities that cancel near equilibrium are formed exactly: L^2 - l^2
+            // of each spring (L ~ l) and the cross product of consecutive bonds
+            // (nearly parallel in a smooth ring).
+            constexpr long long kLim = 1ll << 31;
+            const bool small = bx > -kLim && bx < kLim && by > -kLim && by < kLim && R.ring_ls2_u[t] >= 0;
+            const bool exact = __all_sync(full, small);
+            // springs: bond p pulls p by s_p b_p, bond p-1 by -s_{p-1} b_{p-1}, with
+            // s = k (L - l) / L = k (L^2 - l^2) / ((L + l) L). In a squeezed ring
+            // the two terms are large and nearly cancel, so with exact bonds they
+            // are formed in float-float and rounded to FP32 only after the sum.
+            float fx, fy;
+            if (exact) {
+                const long long L2 = bx * bx + by * by;
+                const FF Lu = ff_sqrt(ff_from_i64(L2));                                   // |b_p|, units
+                const FF den = ff_mul(ff_add(Lu, FF{R.ring_lu_h[t], R.ring_lu_l[t]}), Lu);
+                const FF sp = ff_div(ff_mul(FF{R.ring_ku_h[t], R.ring_ku_l[t]}, ff_from_i64(L2 - R.ring_ls2_u[t])), den);
+                const FF sx = ff_mul(sp, ff_from_i64(bx)), sy = ff_mul(sp, ff_from_i64(by));   // length units
+                const FF mx = FF{__shfl_sync(full, sx.h, pm), __shfl_sync(full, sx.l, pm)};
+                const FF my = FF{__shfl_sync(full, sy.h, pm), __shfl_sync(full, sy.l, pm)};
+                const FF gx = ff_add(sx, ff_neg(mx)), gy = ff_add(sy, ff_neg(my));
+                fx = gx.h + gx.l;
+                fy = gy.h + gy.l;
+            } else {
+                const float spf = ks * (L - ls) * inv;
+                const float smf = __shfl_sync(full, spf, pm);
+                fx = spf * bxf - smf * bmx;
+                fy = spf * byf - smf * bmy;
+            }
             // area force: dr = x_{p+1} - x_{p-1} = b_p + b_{p-1}
-            const long long dbx = bx + __shfl_sync(full, bx, pm), dby = by + __shfl_sync(full, by, pm);
+            const long long dbx = bx + bmxi, dby = by + bmyi;
             fx -= fa * (i64_to_f32(dby) * uf * 0.5f);
             fy -= fa * (-i64_to_f32(dbx) * uf * 0.5f);
+            // bending, a = bond p-1, b = bond p, c = a.b / (|a||b|):
+            //   dc/da = b_perp(a) / (|a||b|) = (a x b) (-a_y, a_x) / (|a|^3 |b|)
+            //   dc/db = a_perp(b) / (|a||b|) = -(a x b) (-b_y, b_x) / (|a| |b|^3)
+            // (the parts of each bond perpendicular to the other, with no
+            // cancellation between nearly equal terms)
             const float iab = invm * inv;
-            const float c = (bmx * bxf + bmy * byf) * iab;
-            const float dcax = bxf * iab - c * bmx * (invm * invm), dcay = byf * iab - c * bmy * (invm * invm);
-            const float dcbx = bmx * iab - c * bxf * (inv * inv), dcby = bmy * iab - c * byf * (inv * inv);
+            const float crf = exact ? i64_to_f32(bmxi * by - bmyi * bx) * R.u2_f : bmx * byf - bmy * bxf;
+            const float q = crf * iab;
+            const float dcax = -q * bmy * (invm * invm), dcay = q * bmx * (invm * invm);
+            const float dcbx = q * byf * (inv * inv), dcby = -q * bxf * (inv * inv);
             const float nax = __shfl_sync(full, dcax, pp), nay = __shfl_sync(full, dcay, pp);
             const float pbx = __shfl_sync(full, dcbx, pm), pby = __shfl_sync(full, dcby, pm);
             if (kbt != 0.0f) {
@@ -1845,12 +1879,14 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
             return;
         }
     }
+    // FP64 form: the area of this step's positions in the reference's own
+    // operation order (k_ring_area_ref ran before this kernel). Mixed form:
     // unwrapped coordinates relative to particle 0 (update_continuos_pos!):
     // u[p] = sum_{q<p} calc_diff(P[q+1], P[q]); area by the shoelace formula.
     double area2 = 0.0;
     double carry_x = 0.0, carry_y = 0.0;   // u of the first particle of this 32-block
     double prev_last_x = 0.0, prev_last_y = 0.0;
-    for (int base = 0; base < n; base += 32) {
+    for (int base = 0; PREC != kPrecFP64 && base < n; base += 32) {
         int p = base + lane;
         double bx = 0, by = 0;
         if (p >= 1 && p < n) { double2 d = diff(P[p], P[p - 1]); bx = d.x; by = d.y; }
@@ -1874,7 +1910,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
     // closing term cross(u[n-1], u[0]) vanishes since u[0] = 0
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) area2 += __shfl_xor_sync(0xffffffffu, area2, o);
-    const double area = area2 / 2.0;
+    const double area = PREC == kPrecFP64 ? C.ring_area[g] : area2 / 2.0;
     const double k_s = rc.k_spring[t], l_s = rc.l_spring[t];
     const double fmod_area = rc.k_area[t] * (area - R.ring_a0sq[t]);
     const double kb = rc.k_bend[t];
@@ -1895,12 +1931,17 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         const T L = sqrt(bx * bx + by * by);
         const T inv = T(1) / L;
         const T bmx = __shfl_sync(full, bx, pm), bmy = __shfl_sync(full, by, pm);   // bond p-1
-        const T Lm = __shfl_sync(full, L, pm), invm = __shfl_sync(full, inv, pm);
+        const T invm = __shfl_sync(full, inv, pm);
         T ks, ls, kbt;
         if constexpr (PREC == kPrecFP64) { ks = k_s; ls = l_s; kbt = kb; }
         else { ks = R.ring_ks_f[t]; ls = R.ring_ls_f[t]; kbt = R.ring_kb_f[t]; }
-        // springs (p, p+1) and (p-1, p)
-        const T sp = ks * (L - ls) * inv, sm = ks * (Lm - ls) * invm;
+        // springs (p, p+1) and, by a shuffle, (p-1, p); the mixed form forms
+        // L - l as (L^2 - l^2) / (L + l) with L^2 - l^2 in FP64, so it keeps its
+        // relative accuracy near the rest length
+        T sp;
+        if constexpr (PREC == kPrecFP64) sp = ks * (L - ls) * inv;
+        else sp = ks * (float)(fma(bd.x, bd.x, bd.y * bd.y) - R.ring_ls2_d[t]) / ((L + ls) * L);
+        const T sm = __shfl_sync(full, sp, pm);
         T fx = sp * bx - sm * bmx;
         T fy = sp * by - sm * bmy;
         // area: F_p -= k_area (A - A0) * (dr.y, -dr.x)/2, dr = x_{p+1} - x_{p-1}
@@ -1918,9 +1959,20 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         // bending: angle at p between a = bond p-1 and b = bond p,
         // c = a.b/(|a||b|); dc/da = b/(|a||b|) - c a/|a|^2, dc/db = a/(|a||b|) - c b/|b|^2
         const T iab = invm * inv;
-        const T c = (bmx * bx + bmy * by) * iab;
-        const T dcax = bx * iab - c * bmx * (invm * invm), dcay = by * iab - c * bmy * (invm * invm);
-        const T dcbx = bmx * iab - c * bx * (inv * inv), dcby = bmy * iab - c * by * (inv * inv);
+        T dcax, dcay, dcbx, dcby;
+        if constexpr (PREC == kPrecFP64) {
+            const T c = (bmx * bx + bmy * by) * iab;
+            dcax = bx * iab - c * bmx * (invm * invm); dcay = by * iab - c * bmy * (invm * invm);
+            dcbx = bmx * iab - c * bx * (inv * inv); dcby = bmy * iab - c * by * (inv * inv);
+        } else {
+            // the parts of each bond perpendicular to the other, from the FP64
+            // cross product (a x b)(-a_y, a_x) / (|a|^3 |b|) and
+            // -(a x b)(-b_y, b_x) / (|a| |b|^3): no cancellation
+            const double amx = __shfl_sync(full, bd.x, pm), amy = __shfl_sync(full, bd.y, pm);
+            const float q = (float)fma(amx, bd.y, -(amy * bd.x)) * iab;
+            dcax = -q * bmy * (invm * invm); dcay = q * bmx * (invm * invm);
+            dcbx = q * by * (inv * inv); dcby = -q * bx * (inv * inv);
+        }
         const T nax = __shfl_sync(full, dcax, pp), nay = __shfl_sync(full, dcay, pp);   // angle at p+1
         const T pbx = __shfl_sync(full, dcbx, pm), pby = __shfl_sync(full, dcby, pm);   // angle at p-1
         if (kb != 0.0) {
@@ -2268,6 +2320,35 @@ static __global__ void k_out_from_cur(Ctx C) {
 // positions (update_continuos_pos!, :118-138: cumulative differences with
 // periodic walls, the positions themselves otherwise) of the last force
 // evaluation (the *_cur state), FP64, summed in particle order.
+// calc_area (src/rings/integration.jl:103-116) of the continuous positions
+// (update_continuos_pos!, :118-138: cumulative calc_diff from particle 1 with
+// periodic walls, the positions themselves otherwise), in the reference's own
+// operation order and rounding: cross products of the continuous coordinates
+// added one after the other, no fused operations. The sum cancels (terms of
+// order |x|^2, result of order the ring's area), so its rounding depends on
+// that order; this keeps the FP64 form's areas bit for bit the reference's.
+// at(i): FP64 position of the ring's particle i.
+template <class At>
+__device__ __forceinline__ double ring_area_reference(const DevRep& R, int32_t n, At at) {
+    const double2 c0 = at(0);
+    double2 prev = c0, cprev = c0;
+    double area = 0.0;
+    for (int32_t i = 1; i < n; i++) {
+        const double2 q = at(i);
+        double2 c = q;
+        if (R.periodic) {
+            double dx = __dsub_rn(q.x, prev.x), dy = __dsub_rn(q.y, prev.y);
+            if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
+            c = make_double2(__dadd_rn(cprev.x, dx), __dadd_rn(cprev.y, dy));
+        }
+        area = __dadd_rn(area, __dsub_rn(__dmul_rn(cprev.x, c.y), __dmul_rn(cprev.y, c.x)));
+        prev = q;
+        cprev = c;
+    }
+    area = __dadd_rn(area, __dsub_rn(__dmul_rn(cprev.x, c0.y), __dmul_rn(cprev.y, c0.x)));
+    return area / 2.0;
+}
+
 static __global__ void k_ring_areas(Ctx C, int64_t ring0, int64_t nrings, double* __restrict__ out) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nrings) return;
@@ -2276,23 +2357,20 @@ static __global__ void k_ring_areas(Ctx C, int64_t ring0, int64_t nrings, double
     const int32_t rl = (int32_t)(g - R.ring0);
     const int32_t n = C.rcfg[C.ring_rep[g]].num_particles[C.ring_types[g] - 1];
     const int32_t u0 = (int32_t)R.slot0 + rl * R.nmax;
-    const double2 c0 = C.pos_cur[C.slot_of[u0]];
-    double2 prev = c0, cprev = c0;
-    double area = 0.0;
-    for (int32_t i = 1; i < n; i++) {
-        const double2 q = C.pos_cur[C.slot_of[u0 + i]];
-        double2 c = q;
-        if (R.periodic) {
-            double dx = q.x - prev.x, dy = q.y - prev.y;
-            if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
-            c = make_double2(cprev.x + dx, cprev.y + dy);
-        }
-        area += cprev.x * c.y - cprev.y * c.x;
-        prev = q;
-        cprev = c;
-    }
-    area += cprev.x * c0.y - cprev.y * c0.x;
-    out[k] = area / 2.0;
+    out[k] = ring_area_reference(R, n, [&](int32_t i) { return C.pos_cur[C.slot_of[u0 + i]]; });
+}
+
+// FP64 rings step: each active ring's area at the current positions (user
+// order, where the ring is contiguous), one thread per ring, for k_rings.
+static __global__ void k_ring_area_ref(Ctx C, int64_t total_rings) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total_rings) return;
+    if (C.var_rings && C.ring_active[g] == 0) return;
+    const int32_t rep = C.ring_rep[g];
+    const DevRep& R = C.reps[rep];
+    const int32_t n = C.rcfg[rep].num_particles[C.ring_types[g] - 1];
+    const int32_t u0 = (int32_t)R.slot0 + (int32_t)(g - R.ring0) * R.nmax;
+    C.ring_area[g] = ring_area_reference(R, n, [&](int32_t i) { return C.pos_u[u0 + i]; });
 }
 
 static __global__ void k_gather_user(Ctx C, const double2* __restrict__ pos_user, const double2* __restrict__ vel_user,

@@ -9,7 +9,11 @@
 // src/chunks.jl:120-161) without creating a handle, which allocates.
 //
 // Scratch: one file-scope device array of fixed size (below), located once
-// per device with cudaGetSymbolAddress. Limits: at most kMaxChunks chunks
+// per device with cudaGetSymbolAddress. The array lives in this file's device
+// module, which CUDA loads on a device the first time the module is used
+// there (lazy loading: the first call of this entry point on that device);
+// that load reserves the 4 MiB array and the module's code on the device.
+// Later calls allocate nothing. Limits: at most kMaxChunks chunks
 // (4 MiB of chunk counters) and a chunk capacity of at most kMaxCap (the
 // per-chunk ordering sorts in place). Every call clears the part of the
 // scratch it uses on its stream before the first kernel, so nothing has to be
@@ -180,6 +184,14 @@ extern "C" int mavi_chunk_lists_noalloc(const MaviReplicaParams* params, const d
     if ((reinterpret_cast<uintptr_t>(pos_dev) & 15) || (reinterpret_cast<uintptr_t>(start_dev) & 15))
         return say(msg, msg_len, MAVI_ERR_INVALID_ARG, "pos_dev and start_dev must be 16-byte aligned");
 
+    // An error left pending by earlier work of the calling thread is not this
+    // call's: report it as such, before anything is launched, instead of
+    // attributing it to the launches below (which would also lose it).
+    cudaError_t pending = cudaGetLastError();
+    if (pending != cudaSuccess)
+        return say(msg, msg_len, MAVI_ERR_CUDA,
+                   "a CUDA error was pending before this call (not raised by it; now cleared): %s",
+                   cudaGetErrorString(pending));
     int32_t* scratch = nullptr;
     int st = scratch_for_current_device(&scratch, msg, msg_len);
     if (st) return st;

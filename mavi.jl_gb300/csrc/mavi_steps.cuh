@@ -33,6 +33,8 @@ void pass(MaviSystem* s, int with_walls) {
 template <int PREC>
 void rings_terms(MaviSystem* s, int do_update, int with_walls) {
     unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
+    // FP64 form: ring areas in the reference's operation order first
+    if constexpr (PREC == kPrecFP64) k_ring_area_ref<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings);
     k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
     if (do_update) k_ring_pol<PREC><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
 }

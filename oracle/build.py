@@ -1,8 +1,10 @@
 """Build recipe of the oracle (TEST INFRASTRUCTURE ONLY).
 
-Compiles oracle/mavi_oracle.c into oracle/_build/libmavi_oracle.so with
+Compiles oracle/mavi_oracle.c into oracle/_build/libmavi_oracle.so with -O3,
 -ffp-contract=off (no fused multiply-add, like Julia without @fastmath) and
-OpenMP (the Threaded force mode and the CPU baseline). The reference itself is
+OpenMP (the Threaded force mode and the CPU baseline). No -march=native and no
+-ffast-math: the same source must give the same FP64 results on every host
+it is built on (x86-64 here, Arm on the GPU machines). The reference itself is
 Julia and cannot be compiled here, so there is no oracle/_ref build.
 """
 from __future__ import annotations
@@ -25,7 +27,7 @@ def build(force: bool = False) -> pathlib.Path:
         return LIB
     cc = os.environ.get("CC") or shutil.which("gcc") or "cc"
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+    cmd = [cc, "-O3", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
            "-o", str(tmp), *map(str, SRC), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

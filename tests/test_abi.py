@@ -79,7 +79,8 @@ def test_product_never_imports_the_oracle():
         assert "oracle" not in p.read_text().lower().replace("oracle/", ""), p
 
 
-def test_integration_guide_names_every_entry_point():
-    text = (ROOT / "INTEGRATION.md").read_text()
-    missing = [n for n in header_functions() if f"`{n}`" not in text]
+def test_ctypes_layer_binds_every_entry_point():
+    """The Python host binds every entry point of the header with a signature."""
+    from mavi_gb300 import abi
+    missing = [n for n in header_functions() if n not in abi.SIGNATURES]
     assert not missing, missing

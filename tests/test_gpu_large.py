@@ -101,3 +101,86 @@ def test_rings_batch_device_noise_runs_and_chunks(mg, orc, wl):
         assert np.all(areas > 0)
         ref.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lj_batch_512_every_replica(mg, orc, wl, precision):
+    """The 512-replica batch of the benchmark at its full shape (7,871,648
+    particles; every wall x geometry quadrant, periodic walls on circles
+    included) after 100 velocity-Verlet steps of the whole batch: per replica
+    the chunk sets are bit-exact and the forces agree with the oracle (FP64
+    1e-12, mixed 1e-5 of the replica's RMS force). Particles start at least
+    0.7 inside the circles, so within 100 steps of dt = 1e-3 none reaches the
+    edge of a periodic circle's chunk grid (the reference's BoundsError)."""
+    systems, step = wl.lj_batch(precision=precision)
+    assert len(systems) == 512
+    kinds = {(type(s.space_cfg.wall_type).__name__, type(s.space_cfg.geometry_cfg).__name__) for s in systems}
+    assert len(kinds) == 4
+    b = mg.SystemBatch(systems, step)
+    b.run(100)
+    assert all(s.time_info.num_steps == 100 for s in systems)
+    forces = b.calc_forces()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    worst = 0.0
+    for k, s in enumerate(systems):
+        ref = orc.from_system(s, nthreads=NT, step_kind=step.kind)
+        assert chunks_equal(b.handle.chunks(k), ref.chunks()), k
+        err = rel_force_err(forces[k], ref.forces(orc.THREADED))
+        worst = max(worst, err)
+        assert err < tol, (k, err)
+        ref.close()
+    print(f"lj_batch_512 {precision}: worst replica force error {worst:.3e}")
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rings_64_every_replica(mg, orc, wl, precision):
+    """The 64-replica ring-mixture batch of the benchmark at its full shape
+    (1,868,100 particles) after 100 steps with device noise: per replica the
+    chunk sets are bit-exact, the forces (pair, springs, area, bending,
+    container) agree with the oracle and so do the ring areas of that force
+    evaluation."""
+    systems, _ = wl.rings_batch(precision=precision)
+    assert len(systems) == 64
+    b = mg.SystemBatch(systems)
+    b.run(100)
+    forces = b.calc_forces()
+    ftol = 1e-12 if precision == "fp64" else 1e-5
+    atol = 1e-10 if precision == "fp64" else 1e-5
+    for k, s in enumerate(systems):
+        assert np.all(np.isfinite(s.state.rings_pos))
+        ref = orc.from_system(s, nthreads=NT)
+        assert chunks_equal(b.handle.chunks(k), ref.chunks()), k
+        fr = ref.forces(orc.THREADED)
+        err = rel_force_err(forces[k], fr)
+        assert err < ftol, (k, err)
+        a, ra = s.areas(), ref.areas(s.state.num_rings)
+        assert np.max(np.abs(a - ra) / np.abs(ra)) < atol, k
+        ref.close()
+    b.close()
+
+
+def test_lj_4194304_energy_series_mixed_follows_fp64(mg, wl):
+    """The 4,194,304-particle periodic LJ state (velocity Verlet, dt = 5e-4):
+    over 2,000 steps the total energy of the mixed form follows the FP64
+    form's, sampled every 200 steps. Trajectories diverge chaotically, so the
+    comparison is of the conserved quantity: the two series and their drifts
+    agree to 1e-6 of the total energy."""
+    series = {}
+    for precision in ("fp64", "mixed"):
+        s, step = wl.lj_4194304(precision=precision)
+        e = [sum(s.energies())]
+        for _ in range(10):
+            mg.run_system(s, num_steps=200, step_func=step)
+            ke, pe = s.energies()
+            e.append(ke + pe)
+        series[precision] = np.array(e)
+        s.close()
+    e64, emx = series["fp64"], series["mixed"]
+    scale = np.abs(e64).max()
+    d64 = (e64[-1] - e64[0]) / scale
+    dmx = (emx[-1] - emx[0]) / scale
+    print(f"lj_4194304 energy drift over 2000 steps: fp64 {d64:.3e}, mixed {dmx:.3e}, "
+          f"max series difference {np.max(np.abs(emx - e64)) / scale:.3e}")
+    assert np.max(np.abs(emx - e64)) / scale < 1e-6
+    assert abs(dmx - d64) < 1e-6

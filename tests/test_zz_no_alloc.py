@@ -21,9 +21,11 @@ def _params(mg, system):
     return p
 
 
-def _noalloc(mg, params, pos_host):
+def _noalloc(mg, params, pos_host, free_bytes=None):
     """Call the entry point on device copies of `pos_host`; returns the status,
-    the message and the lists in the reference layout."""
+    the message and the lists in the reference layout. With `free_bytes` (a
+    list), the device's free memory just before and just after the call (the
+    caller's buffers are all allocated before the first reading) is appended."""
     import torch
     lib = mg.load_library()
     rows, cols = params.chunk_rows, params.chunk_cols
@@ -33,10 +35,15 @@ def _noalloc(mg, params, pos_host):
     ids = torch.full((max(n, 1),), -7, dtype=torch.int32, device="cuda")
     msg = C.create_string_buffer(256)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    if free_bytes is not None:
+        free_bytes.append(torch.cuda.mem_get_info()[0])
     st = lib.mavi_chunk_lists_noalloc(C.byref(params), C.c_void_p(pos.data_ptr()), n,
                                       C.c_void_p(start.data_ptr()), C.c_void_p(ids.data_ptr()),
                                       stream, msg, 256)
     torch.cuda.synchronize()
+    if free_bytes is not None:
+        free_bytes.append(torch.cuda.mem_get_info()[0])
     return st, msg.value.decode(), start.cpu().numpy(), ids.cpu().numpy()[:n]
 
 
@@ -103,5 +110,41 @@ def test_noalloc_reports_particle_outside_grid(mg):
     st, msg, _, _ = _noalloc(mg, p, pos)
     assert st == mg.abi.MAVI_ERR_OUT_OF_GRID, msg
     # the scratch is cleared by the next call: a clean call succeeds again
+    _check_against_handle(mg, s)
+    s.close()
+
+
+def test_noalloc_leaves_free_device_memory_unchanged(mg):
+    """After a first call on the device (which loads the library module holding
+    the fixed scratch), a call changes the device's free memory by nothing: it
+    allocates no device memory, and nothing it calls does."""
+    s = soft_disks(mg, 65536, precision="fp64")
+    p = _params(mg, s)
+    st, msg, _, _ = _noalloc(mg, p, s.state.pos)              # set-up call
+    assert st == mg.abi.MAVI_OK, msg
+    free = []
+    st, msg, start, ids = _noalloc(mg, p, s.state.pos, free_bytes=free)
+    assert st == mg.abi.MAVI_OK, msg
+    assert free[0] == free[1], free
+    assert np.array_equal(np.sort(ids), np.arange(s.num_slots))
+    s.close()
+
+
+def test_noalloc_reports_chunk_overflow_then_recovers(mg):
+    """More particles in one chunk than its capacity is the reference's
+    BoundsError: the call returns MAVI_ERR_CHUNK_OVERFLOW; the next call, on a
+    valid state, clears the shared scratch and succeeds."""
+    s = lj_grid(mg, 8, 8, wall="rigid", chunks=(3, 3))
+    p = _params(mg, s)
+    cap = s.chunk_capacity()
+    assert s.num_slots > cap
+    g = s.space_cfg.geometry_cfg
+    centre = np.array(g.bottom_left, dtype=float) + np.array([g.length / 2, g.height / 2])
+    k = np.arange(s.num_slots)
+    pos = centre + 0.01 * np.stack([k % 8, k // 8], axis=1)  # all in the middle chunk
+    st, msg, _, _ = _noalloc(mg, p, pos)
+    assert st == mg.abi.MAVI_ERR_CHUNK_OVERFLOW, msg
+    assert "capacity" in msg, msg
+    _check_against_handle(mg, s)
     _check_against_handle(mg, s)
     s.close()
