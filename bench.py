@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--workload", default="lj_batch_512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--accuracy-steps", type=int, default=500,
+                    help="steps of the energy-drift / g(r) comparison of the two forms (0: skip)")
     return ap.parse_args()
 
 
@@ -259,6 +261,73 @@ def e2e_form(mg, runner, K, torch):
     return {"seconds": dt, "h2d": bi, "d2h": bo}
 
 
+def accuracy_form(mg, runner, steps, samples, r_max, nbins):
+    """From the workload's starting state (uploaded again): the total energy
+    after every steps/samples steps, recorded on the device, and the
+    pair-distance histogram of all replicas at the end."""
+    abi = mg.abi
+    h = runner.handle
+    pos, vel, pol = runner.host_state()
+    dp = C.POINTER(C.c_double)
+    h.check(h.lib.mavi_upload_state(h.handle, pos.ctypes.data_as(dp),
+                                    None if vel is None else vel.ctypes.data_as(dp),
+                                    None if pol is None else pol.ctypes.data_as(dp)), "upload")
+    out = {}
+    if runner.kind == abi.MAVI_STEP_NEWTON:
+        ke0, pe0 = h.energies(abi.MAVI_PE_STENCIL)
+        ke, pe = h.energy_series(samples, steps // samples, abi.MAVI_PE_STENCIL)
+        out["energy"] = np.vstack([ke0 + pe0, ke + pe])            # (samples + 1, replicas)
+    else:
+        h.step(steps)
+    out["hist"] = h.pair_distribution(-1, r_max, nbins).astype(np.float64)
+    return out
+
+
+def ideal_pairs(runner, r_max, nbins):
+    """Pairs an ideal gas at each replica's density puts in each annulus, summed."""
+    edges = np.linspace(0.0, r_max, nbins + 1)
+    shell = np.pi * (edges[1:] ** 2 - edges[:-1] ** 2)
+    w = 0.0
+    for sy in runner.systems:
+        g = sy.space_cfg.geometry_cfg
+        area = g.length * g.height if hasattr(g, "height") else math.pi * g.radius ** 2
+        w += 0.5 * sy.num_slots ** 2 / area
+    return shell * w
+
+
+def accuracy(mg, runners, steps, samples):
+    """Energy drift of both forms (velocity Verlet only: overdamped steps
+    conserve nothing) and the L-inf difference of their g(r), from the same
+    start; trajectories diverge chaotically, so the forms are compared on
+    statistics. The g(r) bound is five standard deviations of the counting
+    noise of two independent samples."""
+    def chunk_side(sy):
+        bb = sy.space_cfg.bounding_box()
+        cc = getattr(sy.int_cfg, "chunks_cfg", None) or getattr(sy.int_cfg, "p_chunks_cfg")
+        return min(bb.length / cc.num_cols, bb.height / cc.num_rows)
+
+    r_max = math.floor(min(chunk_side(sy) for sy in runners["mixed"].systems) * 50) / 50
+    nbins = max(1, int(round(r_max / 0.02)))
+    res = {p: accuracy_form(mg, runners[p], steps, samples, r_max, nbins) for p in ("fp64", "mixed")}
+    ideal = ideal_pairs(runners["mixed"], r_max, nbins)
+    g = {p: res[p]["hist"] / ideal for p in res}
+    noise = np.sqrt(res["fp64"]["hist"] + res["mixed"]["hist"]) / ideal
+    out = {"steps": steps, "gr_linf": float(np.max(np.abs(g["mixed"] - g["fp64"]))),
+           "gr_5sigma_bound": float(np.max(5 * noise)),
+           "gr_within_bound": bool(np.all(np.abs(g["mixed"] - g["fp64"]) <= 5 * noise + 1e-12)),
+           "gr_bins": {"r_max": r_max, "num_bins": nbins}}
+    if "energy" in res["fp64"]:
+        drift = {}
+        for p in res:
+            e = res[p]["energy"]
+            drift[p] = (e[-1] - e[0]) / np.max(np.abs(e), axis=0)      # per replica
+        out["energy_drift"] = {"fp64_max_abs": float(np.max(np.abs(drift["fp64"]))),
+                               "mixed_max_abs": float(np.max(np.abs(drift["mixed"]))),
+                               "max_abs_difference": float(np.max(np.abs(drift["mixed"] - drift["fp64"]))),
+                               "samples": samples, "per": "replica, relative to its largest |E| in the series"}
+    return out
+
+
 def algorithmic_bytes(kind, precision, step_kind, abi, has_vel):
     """Algorithmic HBM bytes per particle of one launch of each kernel kind:
     the unique data the launch must read and write once (neighbour reads hit
@@ -382,16 +451,22 @@ def cpu_baseline(mg, orc, runner, seconds, nthreads):
 BATCHED = {"lj_batch_512": 512, "rings_64": 64}
 
 
-def build_workload(mg, name, precision, rank=0, world=1):
-    """The workload's handle. Batched workloads under torchrun: R x world
-    replicas, this rank's share by particle count (no exchange between ranks)."""
+def workload_share(name, precision, rank=0, world=1):
+    """The systems this rank advances (host side, no device handle yet).
+    Batched workloads under torchrun: R x world replicas from the same seeded
+    generator, this rank's share by particle count (replicas.shard_replicas:
+    every rank derives the same partition alone; no exchange between ranks)."""
     from mavi_gb300 import replicas, workloads
     W = workloads.WORKLOADS
     if name in BATCHED and world > 1:
         obj, step = W[name](precision=precision, num_replicas=BATCHED[name] * world)
         mine = replicas.my_replicas([s.num_slots for s in obj], rank, world)
-        return Runner(mg, [obj[i] for i in mine], step, precision)
-    obj, step = W[name](precision=precision)
+        return [obj[i] for i in mine], step
+    return W[name](precision=precision)
+
+
+def build_workload(mg, name, precision, rank=0, world=1):
+    obj, step = workload_share(name, precision, rank, world)
     return Runner(mg, obj, step, precision)
 
 
@@ -529,13 +604,13 @@ def main():
         torch.cuda.synchronize()
         clk_form[precision] = clocks.stop()
         if world > 1:
-            t = torch.tensor([m["total_ms"]], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            m["total_ms"] = float(t.item())
+            from mavi_gb300 import replicas
+            m["total_ms"] = replicas.max_over_ranks(m["total_ms"], dist)   # the slowest rank sets the job time
             dist.barrier()
         meas[precision] = m
 
     e2e = e2e_form(mg, runners["mixed"], min(args.steps, 300), torch)
+    acc = accuracy(mg, runners, args.accuracy_steps, 5) if args.accuracy_steps >= 5 else None
 
     n = runners["mixed"].num_slots
     K = args.steps
@@ -589,6 +664,9 @@ def main():
             "kernels_ms_per_step": mx["kernels_ms_per_step"],
             "speedup_mixed_vs_fp64": mx["value"] / line_forms["fp64"]["value"],
             "force_error": err,
+            "energy_drift": acc.get("energy_drift") if acc else None,
+            "gr_linf": acc["gr_linf"] if acc else None,
+            "accuracy": acc,
             "fma_peak_tflops": {k: (v / 1e12 if v else None) for k, v in fma.items()},
         }
         print(json.dumps(out))

@@ -46,6 +46,11 @@ extern "C" {
 #define MAVI_ERR_NOISE_MISSING  9  /* injected-noise mode but no noise supplied for a step  */
 #define MAVI_ERR_NEIGHBOR_OVERFLOW 10 /* more rings particle neighbours than MAVI_MAX_NEIGHBORS
                                       (reference: BoundsError, src/rings/neighbors.jl:107-113) */
+#define MAVI_ERR_OFFSET_RANGE   11 /* mixed form only: a particle more than 1.5 chunks from the
+                                      centre of the chunk it is binned against (it moved more
+                                      than a chunk within one step); its fixed-point offset
+                                      would leave the exact integer range. No reference
+                                      counterpart: the FP64 form has no such limit */
 
 /* ---- enums -------------------------------------------------------------- */
 /* State kinds: src/states.jl:75 (SecondLawState), :104 (SelfPropelledState),
@@ -305,6 +310,30 @@ int mavi_set_seed(MaviSystem* sys, uint64_t seed);
 /* Kinetic energy (src/quantities.jl:12-18) and potential energy per replica.
  * pe_mode: MAVI_PE_STENCIL or MAVI_PE_ALL_PAIRS. Outputs num_replicas doubles. */
 int mavi_energies(MaviSystem* sys, int32_t pe_mode, double* ke, double* pe);
+
+/* Energy time series on the device: num_samples times, advance every replica
+ * steps_between steps (as mavi_step) and record its kinetic and potential
+ * energy (as mavi_energies); everything is enqueued on the handle's stream
+ * and the series is copied back once at the end. ke and pe receive
+ * num_samples * num_replicas doubles, sample-major. Replaces the reference's
+ * pattern of calling kinetic_energy / potential_energy (src/quantities.jl:12-66)
+ * between run_system calls, without a host round trip per sample. The
+ * series buffer on the device grows (one allocation) when a call needs more
+ * samples than any call before it. */
+int mavi_energy_series(MaviSystem* sys, int64_t num_samples, int64_t steps_between, int32_t pe_mode,
+                       double* ke, double* pe);
+
+/* Pair-distance histogram of the current state, the counts behind the pair
+ * distribution g(r): counts[k] = number of unordered particle pairs of
+ * `replica` (-1: all replicas summed) at distance d with floor(d / dr) == k,
+ * d < r_max, dr = r_max / num_bins; d is the length of calc_diff (minimum
+ * image where the reference applies it, src/integration.jl:38-52) computed
+ * in FP64 without fused operations, so the counts are exact. The reference
+ * has no g(r) routine; this is the statistic its long runs are judged by.
+ * r_max must not exceed any selected replica's chunk sides (replicas without
+ * chunks: any r_max); 1 <= num_bins <= 4096. counts: num_bins uint64. */
+int mavi_pair_distribution(MaviSystem* sys, int32_t replica, double r_max, int32_t num_bins,
+                           uint64_t* counts);
 
 /* time_info (src/systems.jl:30-33, src/integration.jl:500-503) of replica 0. */
 int mavi_get_time(MaviSystem* sys, int64_t* num_steps, double* time);

@@ -15,7 +15,7 @@ from .configs import (
 from .states import SecondLawState, SelfPropelledState, get_num_total_particles
 from .system import (
     OverdampedStep, System, SystemBatch, TimeInfo, get_step_function, kinetic_energy, newton_step,
-    overdamped_step, potential_energy, rings_step, rtp_step, run_system, szabo_step,
+    overdamped_step, pair_correlation, potential_energy, rings_step, rtp_step, run_system, szabo_step,
 )
 from .init_states import fixed_speed_vel, maxwell_vel, random_vel, rectangular_grid
 from . import rings

@@ -23,6 +23,7 @@ MAVI_ERR_UNSUPPORTED = 7
 MAVI_ERR_NO_DEVICE = 8
 MAVI_ERR_NOISE_MISSING = 9
 MAVI_ERR_NEIGHBOR_OVERFLOW = 10
+MAVI_ERR_OFFSET_RANGE = 11
 MAVI_MAX_NEIGHBORS = 15
 
 MAVI_STATE_SECOND_LAW = 0
@@ -208,6 +209,8 @@ SIGNATURES = {
     "mavi_set_noise": (C.c_int, [_vp, _dp, C.c_int64]),
     "mavi_set_seed": (C.c_int, [_vp, C.c_uint64]),
     "mavi_energies": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
+    "mavi_energy_series": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int32, _dp, _dp]),
+    "mavi_pair_distribution": (C.c_int, [_vp, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_uint64)]),
     "mavi_get_time": (C.c_int, [_vp, C.POINTER(C.c_int64), _dp]),
     "mavi_set_time": (C.c_int, [_vp, C.c_int32, C.c_int64, C.c_double]),
     "mavi_get_stats": (C.c_int, [_vp, C.POINTER(MaviStats)]),

@@ -430,6 +430,10 @@ static int check_device_error(MaviSystem* s) {
         return fail(s, e.code, "chunk %lld holds more particles than its capacity (particle %d)", (long long)e.aux, uid);
     case MAVI_ERR_NONFINITE:
         return fail(s, e.code, "particle %d has a non-finite position", uid);
+    case MAVI_ERR_OFFSET_RANGE:
+        return fail(s, e.code,
+                    "particle %d is more than 1.5 chunks from the centre of its chunk (it moved more than a chunk "
+                    "in one step); the mixed form's fixed-point offsets cannot represent it", uid);
     }
     return fail(s, e.code, "device error %d", e.code);
 }
@@ -519,6 +523,7 @@ const char* mavi_status_string(int st) {
     case MAVI_ERR_NO_DEVICE: return "no CUDA device";
     case MAVI_ERR_NOISE_MISSING: return "noise not supplied";
     case MAVI_ERR_NEIGHBOR_OVERFLOW: return "neighbour list overflow";
+    case MAVI_ERR_OFFSET_RANGE: return "particle beyond the mixed form's fixed-point offset range";
     }
     return "unknown status";
 }
@@ -535,6 +540,8 @@ int mavi_destroy(MaviSystem* s) {
     if (s->ev.step_b) cudaEventDestroy(s->ev.step_b);
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (void* p : s->allocs) cudaFree(p);
+    if (s->series) cudaFree(s->series);
+    if (s->hist) cudaFree(s->hist);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return MAVI_OK;
@@ -1067,14 +1074,20 @@ int mavi_calc_forces(MaviSystem* s, int32_t include_walls, double* forces_out) {
     return check_device_error(s);
 }
 
-int mavi_energies(MaviSystem* s, int32_t pe_mode, double* ke, double* pe) {
-    if (!s) return MAVI_ERR_INVALID_ARG;
+// Per-replica kinetic and potential energies of the current state into the
+// device arrays ke_out / pe_out (num_replicas doubles each), enqueued.
+static void enqueue_energies(MaviSystem* s, int32_t pe_mode, double* ke_out, double* pe_out) {
     s->counts_valid = false;
     launch_rebin(s, false);
     k_energy_terms<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->dyn, pe_mode == MAVI_PE_ALL_PAIRS, s->ke_t, s->pe_t,
                                                             s->has_vel ? 1 : 0);
-    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->ke_t, s->ke_r, 0.5);
-    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->pe_t, s->pe_r, 1.0);
+    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->ke_t, ke_out, 0.5);
+    k_reduce_per_replica<<<s->R, 256, 0, s->stream>>>(s->C, s->pe_t, pe_out, 1.0);
+}
+
+int mavi_energies(MaviSystem* s, int32_t pe_mode, double* ke, double* pe) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    enqueue_energies(s, pe_mode, s->ke_r, s->pe_r);
     CUDA_TRY(s, cudaGetLastError());
     if (ke) CUDA_TRY(s, cudaMemcpyAsync(ke, s->ke_r, sizeof(double) * s->R, cudaMemcpyDeviceToHost, s->stream));
     if (pe) CUDA_TRY(s, cudaMemcpyAsync(pe, s->pe_r, sizeof(double) * s->R, cudaMemcpyDeviceToHost, s->stream));
@@ -1082,6 +1095,63 @@ int mavi_energies(MaviSystem* s, int32_t pe_mode, double* ke, double* pe) {
     bool pe_defined = s->dyn == MAVI_DYN_LEN_JONES || s->dyn == MAVI_DYN_HARM_TRUNC || s->dyn == MAVI_DYN_RUN_TUMBLE;
     if (pe && !pe_defined)
         for (int r = 0; r < s->R; r++) pe[r] = NAN;
+    return check_device_error(s);
+}
+
+int mavi_energy_series(MaviSystem* s, int64_t num_samples, int64_t steps_between, int32_t pe_mode, double* ke,
+                       double* pe) {
+    if (!s || num_samples < 1 || steps_between < 0 || !ke || !pe) return MAVI_ERR_INVALID_ARG;
+    const int64_t need = 2 * num_samples * (int64_t)s->R;
+    if (need > s->series_cap) {
+        if (s->series) {
+            CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+            cudaFree(s->series);
+            s->series = nullptr;
+            s->series_cap = 0;
+        }
+        CUDA_TRY(s, cudaMalloc((void**)&s->series, sizeof(double) * need));
+        s->series_cap = need;
+    }
+    for (int64_t k = 0; k < num_samples; k++) {
+        int rc = mavi_step(s, steps_between);
+        if (rc) return rc;
+        double* row = s->series + 2 * k * s->R;
+        enqueue_energies(s, pe_mode, row, row + s->R);
+    }
+    CUDA_TRY(s, cudaGetLastError());
+    std::vector<double> h(need);
+    CUDA_TRY(s, cudaMemcpyAsync(h.data(), s->series, sizeof(double) * need, cudaMemcpyDeviceToHost, s->stream));
+    int rc = check_device_error(s);   // waits for the stream
+    if (rc) return rc;
+    const bool pe_defined = s->dyn == MAVI_DYN_LEN_JONES || s->dyn == MAVI_DYN_HARM_TRUNC || s->dyn == MAVI_DYN_RUN_TUMBLE;
+    for (int64_t k = 0; k < num_samples; k++)
+        for (int r = 0; r < s->R; r++) {
+            ke[k * s->R + r] = h[2 * k * s->R + r];
+            pe[k * s->R + r] = pe_defined ? h[2 * k * s->R + s->R + r] : NAN;
+        }
+    return MAVI_OK;
+}
+
+int mavi_pair_distribution(MaviSystem* s, int32_t replica, double r_max, int32_t num_bins, uint64_t* counts) {
+    if (!s || !counts || replica < -1 || replica >= s->R) return MAVI_ERR_INVALID_ARG;
+    if (num_bins < 1 || num_bins > kHistMaxBins)
+        return fail(s, MAVI_ERR_INVALID_ARG, "num_bins must be in 1..%d", kHistMaxBins);
+    if (!(r_max > 0) || !std::isfinite(r_max)) return fail(s, MAVI_ERR_INVALID_ARG, "r_max must be positive");
+    for (int r = 0; r < s->R; r++) {
+        if (replica >= 0 && r != replica) continue;
+        const DevRep& R = s->reps_h[r];
+        if (R.has_chunks && r_max > std::min(R.chunk_l, R.chunk_h))
+            return fail(s, MAVI_ERR_INVALID_ARG, "r_max %g exceeds the chunk sides of replica %d (%g x %g)", r_max, r,
+                        R.chunk_l, R.chunk_h);
+    }
+    if (!s->hist) CUDA_TRY(s, cudaMalloc((void**)&s->hist, sizeof(unsigned long long) * kHistMaxBins));
+    s->counts_valid = false;
+    launch_rebin(s, false);
+    CUDA_TRY(s, cudaMemsetAsync(s->hist, 0, sizeof(unsigned long long) * num_bins, s->stream));
+    k_pair_hist<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, replica, r_max, r_max / num_bins, num_bins, s->hist);
+    CUDA_TRY(s, cudaGetLastError());
+    CUDA_TRY(s, cudaMemcpyAsync(counts, s->hist, sizeof(unsigned long long) * num_bins, cudaMemcpyDeviceToHost,
+                                s->stream));
     return check_device_error(s);
 }
 

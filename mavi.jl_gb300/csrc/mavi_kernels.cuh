@@ -35,6 +35,9 @@ constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
 constexpr int64_t kScanDirectTiles = 512;  // above this, tile offsets come from k_tile_offsets
 constexpr int kTileScanThreads = 1024;     // tiles per group of k_tile_offsets
 constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
+// |offset| allowed in a pair term: two offsets of at most 1.5 chunks and the
+// one-chunk stencil shift keep every difference within 4 chunks < 2^31 units
+constexpr int32_t kFixRange = 3 << (kFixBits - 1);
 
 // Fixed-point parameters of the pair laws of one (type, type) pair, in units
 // u = max(chunk_l, chunk_h) / 2^28 of the replica.
@@ -171,12 +174,16 @@ __device__ __forceinline__ void bin_position(const DevRep& R, double x, double y
 // Fixed-point offset of a position from the centre of chunk (row, col),
 // computed from the binning numerators (x - cx = tx - (col + 1/2) l,
 // y - cy = (row + 1/2) h - ty).
-__device__ __forceinline__ int2 fixed_offset(const DevRep& R, int64_t row, int64_t col, double tx, double ty) {
+// An offset beyond 1.5 chunks (a particle that moved more than a chunk in
+// one step) is reported (MAVI_ERR_OFFSET_RANGE) instead of giving wrong pair
+// terms; the conversion saturates and the clamp keeps the value finite.
+__device__ __forceinline__ int2 fixed_offset(const DevRep& R, int64_t row, int64_t col, double tx, double ty,
+                                             DevError* err, int64_t s) {
     double ox = fma(-((double)col + 0.5), R.chunk_l, tx) * R.inv_u;
     double oy = fma((double)row + 0.5, R.chunk_h, -ty) * R.inv_u;
-    // the conversion saturates; the clamp keeps differences inside int32
     int32_t ix = min(max(__double2int_rn(ox), -kFixClamp), kFixClamp);
     int32_t iy = min(max(__double2int_rn(oy), -kFixClamp), kFixClamp);
+    if (R.has_chunks && (abs(ix) > kFixRange || abs(iy) > kFixRange)) raise_error(err, MAVI_ERR_OFFSET_RANGE, s, 0);
     return make_int2(ix, iy);
 }
 
@@ -226,7 +233,7 @@ __device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int6
     if (!R.has_chunks) {
         if constexpr (PREC == kPrecMixed) {
             double tx = __dsub_rn(x, R.bb_blx), ty = __dadd_rn(__dadd_rn(-y, R.bb_bly), R.bb_h);
-            const int2 o = fixed_offset(R, 0, 0, tx, ty);
+            const int2 o = fixed_offset(R, 0, 0, tx, ty, C.err, s);
             C.off_out[s] = o;
             if (uw >= 0) C.off_u[uw] = o;
         }
@@ -245,7 +252,7 @@ __device__ __forceinline__ int64_t bin_final(const Ctx& C, const DevRep& R, int6
     bin_position(R, x, y, grow, gcol, has_guess, row, col, tx, ty, finite);
     int64_t cell = checked_cell(R, row, col, finite, C.err, s);
     if constexpr (PREC == kPrecMixed) {
-        const int2 o = fixed_offset(R, row, col, tx, ty);
+        const int2 o = fixed_offset(R, row, col, tx, ty, C.err, s);
         C.off_out[s] = o;
         if (uw >= 0) C.off_u[uw] = o;
     }
@@ -1550,7 +1557,7 @@ k_pass(Ctx C, int32_t with_wall_forces) {
                 int32_t lc = (int32_t)(cell - R.c0);
                 int64_t col = lc / R.rows, row = lc - col * R.rows;
                 double tx = __dsub_rn(nx, R.bb_blx), ty = __dadd_rn(__dadd_rn(-ny, R.bb_bly), R.bb_h);
-                C.off_mid[s] = fixed_offset(R, row, col, tx, ty);
+                C.off_mid[s] = fixed_offset(R, row, col, tx, ty, C.err, s);
             }
         } else {
             double x = p.x, y = p.y, vx = 0, vy = 0;
@@ -2476,6 +2483,64 @@ static __global__ void k_reduce_per_replica(Ctx C, const double* __restrict__ t,
         __syncthreads();
     }
     if (threadIdx.x == 0) out[blockIdx.x] = sh[0] * scale;
+}
+
+// Pair-distance histogram of the current state (the counts behind the pair
+// distribution g(r)): counts[k] += the unordered pairs (i, j) of a replica
+// (rep_sel; -1: every replica) with floor(d / dr) == k and d < r_max, where d
+// is the length of calc_diff(x_i, x_j) (src/integration.jl:38-52) from the
+// FP64 positions, formed with IEEE operations in a fixed order (no fused
+// multiply-add) and binned by a correctly rounded division: the counts are
+// exact integers, equal to the CPU restatement's. r_max must not exceed the
+// chunk sides, so every pair closer than r_max lies in the 3x3 chunk
+// neighbourhood; a pair is counted from its lower sorted slot. Bins live in
+// shared memory per block (nbins <= kHistMaxBins) and are added to the global
+// counts once per block.
+constexpr int kHistMaxBins = 4096;
+static __global__ void k_pair_hist(Ctx C, int32_t rep_sel, double r_max, double dr, int32_t nbins,
+                                   unsigned long long* __restrict__ counts) {
+    __shared__ uint32_t bins[kHistMaxBins];
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x) bins[k] = 0;
+    __syncthreads();
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t rep = (s < C.M && C.num_reps > 1) ? C.rep_cur[s] : 0;
+    if (s < C.M && (rep_sel < 0 || rep == rep_sel) && !(C.var_rings && C.cell_cur[s] == C.park)) {
+        const DevRep& R = C.reps[rep];
+        const double2 pi = C.pos_cur[s];
+        auto visit = [&](int32_t b, int32_t e) {
+            for (int32_t j = max(b, (int32_t)s + 1); j < e; j++) {
+                const double2 q = C.pos_cur[j];
+                double dx = __dsub_rn(pi.x, q.x), dy = __dsub_rn(pi.y, q.y);
+                if (R.min_image) { dx = min_image1(dx, R.box_x, R.half_box_x); dy = min_image1(dy, R.box_y, R.half_box_y); }
+                const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                if (d < r_max) {
+                    const int32_t k = min((int32_t)__ddiv_rn(d, dr), nbins - 1);
+                    atomicAdd(&bins[k], 1u);
+                }
+            }
+        };
+        if (!R.has_chunks) {
+            visit(C.start[R.c0], C.start[R.c0 + 1]);
+        } else {
+            const int64_t lc = C.cell_cur[s] - R.c0;
+            const int32_t row = (int32_t)(lc % R.rows), col = (int32_t)(lc / R.rows);
+            for (int dc = -1; dc <= 1; dc++) {
+                int ncol = col + dc;
+                if (R.periodic) ncol = ncol < 0 ? ncol + R.cols : (ncol >= R.cols ? ncol - R.cols : ncol);
+                else if (ncol < 0 || ncol >= R.cols) continue;
+                for (int drow = -1; drow <= 1; drow++) {
+                    int nrow = row + drow;
+                    if (R.periodic) nrow = nrow < 0 ? nrow + R.rows : (nrow >= R.rows ? nrow - R.rows : nrow);
+                    else if (nrow < 0 || nrow >= R.rows) continue;
+                    const int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
+                    visit(C.start[nc], C.start[nc + 1]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x)
+        if (bins[k]) atomicAdd(&counts[k], (unsigned long long)bins[k]);
 }
 
 // candidate-pair count per particle (roofline accounting)

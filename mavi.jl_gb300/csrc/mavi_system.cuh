@@ -45,6 +45,9 @@ struct MaviSystem {
     double* pol_user = nullptr;
     double *ke_t = nullptr, *pe_t = nullptr, *ke_r = nullptr, *pe_r = nullptr;
     unsigned long long* d_pairs = nullptr;
+    double* series = nullptr;          // energy series (mavi_energy_series), grown on demand
+    int64_t series_cap = 0;            // doubles
+    unsigned long long* hist = nullptr;    // pair-distance histogram bins (mavi_pair_distribution)
     double* noise_cur = nullptr;
     double* noise_queue = nullptr;
     int64_t noise_queue_cap = 0, noise_queue_len = 0, noise_queue_pos = 0;

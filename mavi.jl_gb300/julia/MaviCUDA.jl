@@ -14,6 +14,12 @@ library by pointer: `Vector{SVector{2,Float64}}` is the interleaved
 The GPU copy of the state is authoritative while stepping; `sync!(system)`
 copies it back into `system.state` (done automatically by `run_system` here and
 by `gpu_run!`). Indices crossing the ABI are 0-based.
+
+Bulk drivers: for a CUDA system, `run_system` runs all its steps in one
+`mavi_step` call and `run_experiment` one call per event (collector save,
+checkpoint, final time), copying the state back once per call instead of once
+per step; the single-step `gpu_step!` keeps exact per-step semantics for code
+that calls the step function itself.
 """
 module MaviCUDA
 
@@ -436,6 +442,155 @@ function calc_forces(system; include_walls=false)
     check(ccall((:mavi_calc_forces, libmavi), Cint, (Ptr{Cvoid}, Int32, Ptr{Cvoid}),
                 h, include_walls ? 1 : 0, f), "mavi_calc_forces", h)
     return f
+end
+
+"Energy series on the device (`mavi_energy_series`): per sample, advance `steps_between` steps and record the
+kinetic and potential energy; one copy back at the end, then `sync!`. Returns (ke, pe) vectors."
+function energy_series(system, num_samples::Integer, steps_between::Integer; all_pairs=false)
+    h = handle!(system)
+    ke, pe = zeros(Float64, num_samples), zeros(Float64, num_samples)
+    check(ccall((:mavi_energy_series, libmavi), Cint, (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Float64}, Ptr{Float64}),
+                h, num_samples, steps_between, all_pairs ? 1 : 0, ke, pe), "mavi_energy_series", h)
+    sync!(system)
+    return ke, pe
+end
+
+"Pair-distance histogram (`mavi_pair_distribution`) of the current state: `num_bins` counts of
+unordered pairs with floor(d / dr) == k, d < r_max, dr = r_max / num_bins."
+function pair_distribution(system, r_max::Real, num_bins::Integer)
+    h = handle!(system)
+    counts = zeros(UInt64, num_bins)
+    check(ccall((:mavi_pair_distribution, libmavi), Cint, (Ptr{Cvoid}, Int32, Float64, Int32, Ptr{UInt64}),
+                h, 0, r_max, num_bins, counts), "mavi_pair_distribution", h)
+    return counts
+end
+
+# ---- bulk drivers ------------------------------------------------------------------
+# The reference's drivers call the step function once per step (src/run_system.jl:7-23,
+# src/experiments.jl:94-144). For a CUDA system the steps between two host-side events
+# run in one mavi_step call and the state is copied back once per event, not per step.
+
+const CUDASystem = Mavi.Systems.System{T, ND, NT, S, W, G, D,
+                                       <:Mavi.Configs.IntCfg{<:Number, <:Any, CUDADevice}} where {T, ND, NT, S, W, G, D}
+
+"Steps the reference's `while cond(time)` loop takes from `t0` (replays `time += dt`, update_time!,
+src/integration.jl:500-503); returns (steps, final time)."
+function steps_while(cond, t0::Float64, dt::Float64)
+    t, n = t0, 0
+    while cond(t)
+        t += dt
+        n += 1
+    end
+    return n, t
+end
+
+"""
+    run_system(system::CUDASystem; tf, num_steps, step_func)
+
+`run_system` (src/run_system.jl:7-23) for a system on the GPU: the number of steps
+(`num_steps`, or the steps the reference's `while time < tf` loop takes) runs in one
+`mavi_step` call and the state is copied back once. A caller-supplied `step_func`
+other than the GPU step runs the reference's loop unchanged.
+"""
+function Mavi.RunSystem.run_system(system::CUDASystem; tf=nothing, num_steps=nothing, step_func=nothing)
+    if !isnothing(step_func) && step_func !== gpu_step!
+        if !isnothing(tf)
+            while system.time_info.time < tf
+                step_func(system)
+            end
+        else
+            for _ in 1:num_steps
+                step_func(system)
+            end
+        end
+        return
+    end
+    n = isnothing(tf) ? num_steps : steps_while(t -> t < tf, system.time_info.time, system.int_cfg.dt)[1]
+    n > 0 && gpu_run!(system, n)
+    return
+end
+
+const EXP = Mavi.Experiments
+
+# Steps until a collector acts, for the collectors whose rule is known; `nothing` for
+# any other collector (the experiment then runs one step per call, as the reference).
+_steps_to_collect(::EXP.Collector, t0, dt, limit) = nothing
+function _steps_to_collect(col::EXP.DelayedCol, t0, dt, limit)
+    # collect (src/experiments.jl:435-445): saves when time - last_save_time > delay_time
+    last, delay = col.state.last_save_time, col.cfg.delay_time
+    n = steps_while(t -> !(t - last > delay), t0, dt)[1]
+    return n == 0 ? 1 : min(n, limit)      # already due: the collect after the next step saves
+end
+function _steps_to_collect(col::EXP.ManyCols, t0, dt, limit)
+    n = limit
+    for c in values(col.cols)
+        k = _steps_to_collect(c, t0, dt, limit)
+        isnothing(k) && return nothing
+        n = min(n, k)
+    end
+    return n
+end
+
+# check_checkpoint (src/experiments.jl:461-467): acts when time - last_time >= delta_time
+_steps_to_checkpoint(::Nothing, ::Nothing, t0, dt, limit) = limit
+function _steps_to_checkpoint(cfg::EXP.CheckpointCfg, cp, t0, dt, limit)
+    n = steps_while(t -> t - cp.last_time < cfg.delta_time, t0, dt)[1]
+    return n == 0 ? 1 : min(n, limit)
+end
+
+"""
+    run_experiment(experiment::Experiment{<:CUDASystem}, stop_func=nothing; prog_kwargs, check_every=1)
+
+`run_experiment` (src/experiments.jl:94-144) for a system on the GPU. Between two
+events (a collector saving, a checkpoint, the final time) the steps run in one
+`mavi_step` call; `collect`, `check_checkpoint` and the progress display then run
+exactly as in the reference's loop, on the state copied back at that step, and
+they see the same times (the host replays `time += dt`). `stop_func` is evaluated
+every `check_every` steps (1: every step, the reference's behaviour). A custom
+step function other than the GPU step, or a collector whose saving rule is not
+known here, runs the reference's loop unchanged.
+"""
+function EXP.run_experiment(experiment::EXP.Experiment{<:CUDASystem}, stop_func=nothing;
+                            prog_kwargs=nothing, check_every::Integer=1)
+    system, col, cfg = experiment.system, experiment.col, experiment.cfg
+    dt = system.int_cfg.dt
+    if experiment.custom_step !== gpu_step! || isnothing(_steps_to_collect(col, system.time_info.time, dt, 1))
+        return invoke(EXP.run_experiment, Tuple{EXP.Experiment, Any}, experiment, stop_func;
+                      prog_kwargs=prog_kwargs)
+    end
+    prog_kwargs = isnothing(prog_kwargs) ? () : prog_kwargs
+    stop = isnothing(stop_func) ? nothing : stop_func
+    EXP.save_system_configs(system, cfg.root)
+    EXP.save_experiment_configs(experiment)
+    col_path = mkpath(joinpath(cfg.root, EXP.COL_DIRNAME))
+    if !isnothing(experiment.checkpoint)
+        mkpath(joinpath(cfg.root, EXP.CHECKPOINT_DIRNAME, "1"))
+        mkpath(joinpath(cfg.root, EXP.CHECKPOINT_DIRNAME, "2"))
+    end
+    prog = EXP.ProgContinuos(init=system.time_info.time, final=cfg.tf; prog_kwargs...)
+    while system.time_info.time < cfg.tf
+        t = system.time_info.time
+        limit = steps_while(x -> x < cfg.tf, t, dt)[1]
+        isnothing(stop) || (limit = min(limit, check_every))
+        n = min(_steps_to_collect(col, t, dt, limit),
+                _steps_to_checkpoint(cfg.checkpoint_cfg, experiment.checkpoint, t, dt, limit))
+        gpu_run!(system, max(n, 1))
+        EXP.collect(col, system)
+        EXP.check_checkpoint(cfg.checkpoint_cfg, experiment)
+        EXP.show_progress(prog, system.time_info.time)
+        if !isnothing(stop) && stop(system)
+            break
+        end
+    end
+    EXP.save_data(col, col_path)
+    if cfg.save_final_state
+        EXP.save_system(system, joinpath(cfg.root, EXP.FINAL_STATE_NAME))
+    end
+    EXP.show_finish(prog)
+    open(joinpath(cfg.root, ".done"), "w") do f
+        write(f, "Experiment concluded on $(EXP.Dates.now())\n")
+    end
+    return
 end
 
 # ---- the hook into Mavi.jl -------------------------------------------------------

@@ -226,6 +226,21 @@ class _Handle:
         self.check(self.lib.mavi_get_stats(self.handle, C.byref(st)), "mavi_get_stats")
         return st
 
+    def energy_series(self, num_samples: int, steps_between: int, pe_mode: int):
+        n = len(self.systems)
+        ke = np.zeros((int(num_samples), n))
+        pe = np.zeros((int(num_samples), n))
+        self.check(self.lib.mavi_energy_series(self.handle, int(num_samples), int(steps_between), pe_mode,
+                                               abi.as_dptr(ke), abi.as_dptr(pe)), "mavi_energy_series")
+        return ke, pe
+
+    def pair_distribution(self, replica: int, r_max: float, num_bins: int) -> np.ndarray:
+        out = np.zeros(int(num_bins), dtype=np.uint64)
+        self.check(self.lib.mavi_pair_distribution(self.handle, int(replica), float(r_max), int(num_bins),
+                                                   out.ctypes.data_as(C.POINTER(C.c_uint64))),
+                   "mavi_pair_distribution")
+        return out
+
 
 class System:
     """A particle system (src/systems.jl:45-114) whose step loop runs on the GPU."""
@@ -320,6 +335,26 @@ class System:
     def stats(self) -> abi.MaviStats:
         return self._ensure().stats()
 
+    def energy_series(self, num_samples: int, steps_between: int, step_func: StepFunction | None = None,
+                      pe_mode=abi.MAVI_PE_STENCIL):
+        """Advance num_samples * steps_between steps and return the kinetic and
+        potential energy after every steps_between steps (arrays of
+        num_samples), recorded on the device without a host round trip per
+        sample (mavi_energy_series); the state is downloaded once at the end."""
+        h = self._ensure(step_func.kind if step_func is not None else None)
+        ke, pe = h.energy_series(num_samples, steps_between, pe_mode)
+        h.download()
+        for _ in range(int(num_samples) * int(steps_between)):
+            self.time_info.time += self.int_cfg.dt
+            self.time_info.num_steps += 1
+        return ke[:, 0], pe[:, 0]
+
+    def pair_distribution(self, r_max: float, num_bins: int) -> np.ndarray:
+        """Pair-distance histogram (num_bins uint64 counts of unordered pairs per
+        bin of width r_max / num_bins) of the current state; pair_correlation()
+        turns it into g(r)."""
+        return self._ensure().pair_distribution(0, r_max, num_bins)
+
     @property
     def handle(self) -> _Handle:
         return self._ensure()
@@ -361,6 +396,22 @@ class SystemBatch:
     def energies(self, pe_mode=abi.MAVI_PE_STENCIL):
         return self._handle.energies(pe_mode)
 
+    def energy_series(self, num_samples: int, steps_between: int, pe_mode=abi.MAVI_PE_STENCIL, download=True):
+        """Per-replica (num_samples, num_replicas) kinetic and potential energy
+        after every steps_between steps (mavi_energy_series)."""
+        ke, pe = self._handle.energy_series(num_samples, steps_between, pe_mode)
+        if download:
+            self._handle.download()
+        for s in self.systems:
+            for _ in range(int(num_samples) * int(steps_between)):
+                s.time_info.time += s.int_cfg.dt
+                s.time_info.num_steps += 1
+        return ke, pe
+
+    def pair_distribution(self, r_max: float, num_bins: int, replica: int = -1) -> np.ndarray:
+        """Pair-distance histogram of one replica, or of all replicas summed (-1)."""
+        return self._handle.pair_distribution(replica, r_max, num_bins)
+
     def close(self):
         self._handle.close()
         for s in self.systems:
@@ -395,3 +446,15 @@ def potential_energy(system: System, pe_mode=abi.MAVI_PE_ALL_PAIRS) -> float:
     (pe_mode=MAVI_PE_ALL_PAIRS); MAVI_PE_STENCIL sums the chunk-stencil pairs
     the forces use."""
     return system.energies(pe_mode)[1]
+
+
+def pair_correlation(counts, r_max: float, num_particles: int, area: float):
+    """g(r) from pair-distance counts: the counts of each bin over the number
+    of pairs an ideal gas at the same density would place in that annulus,
+    (N / 2) (N / area) pi (r_hi^2 - r_lo^2). Returns (bin centres, g)."""
+    counts = np.asarray(counts, dtype=np.float64)
+    edges = np.linspace(0.0, float(r_max), counts.size + 1)
+    shell = np.pi * (edges[1:] ** 2 - edges[:-1] ** 2)
+    ideal = 0.5 * num_particles * (num_particles / float(area)) * shell
+    return 0.5 * (edges[1:] + edges[:-1]), counts / ideal
+

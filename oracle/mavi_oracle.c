@@ -1319,6 +1319,51 @@ int64_t oracle_count_pairs(OracleSys* s) {
     return pairs;
 }
 
+/* Pair-distance histogram (the counts behind the pair distribution g(r)),
+ * the definition mavi_pair_distribution implements: every unordered pair of
+ * the chunk loop of calc_forces! (src/integration.jl:112-157; all active
+ * pairs without chunks, :197-224) whose calc_diff length d is below r_max
+ * adds one to bin floor(d / dr), dr = r_max / nbins (the last bin also takes
+ * a division that rounds up to nbins). r_max must not exceed the chunk
+ * sides, so the chunk loop holds every such pair. */
+int32_t oracle_pair_distribution(OracleSys* s, double r_max, int32_t nbins, uint64_t* counts) {
+    if (nbins < 1 || !(r_max > 0)) return MAVI_ERR_INVALID_ARG;
+    memset(counts, 0, sizeof(uint64_t) * (size_t)nbins);
+    const double dr = r_max / nbins;
+    #define HIST_PAIR(I, J) do {                                                             \
+        V2 d_ = calc_diff(s, P(s, (I)), P(s, (J)));                                          \
+        double dd_ = sqrt(sum_sq(d_));                                                       \
+        if (dd_ < r_max) {                                                                   \
+            int32_t k_ = (int32_t)(dd_ / dr);                                                \
+            counts[k_ > nbins - 1 ? nbins - 1 : k_]++;                                       \
+        }                                                                                    \
+    } while (0)
+    if (!s->has_chunks) {
+        for (int64_t a = 0; a < s->npids; a++)
+            for (int64_t b = a + 1; b < s->npids; b++) HIST_PAIR(s->pids[a], s->pids[b]);
+        return MAVI_OK;
+    }
+    if (oracle_update_chunks(s)) return s->err;
+    for (int64_t col = 0; col < s->cols; col++) {
+        for (int64_t row = 0; row < s->rows; row++) {
+            int64_t ch = col * s->rows + row;
+            int32_t np = s->num_in_chunk[ch];
+            const int32_t* chunk = s->chunk_particles + ch * s->cap;
+            for (int32_t i = 0; i < np; i++) {
+                int64_t p1 = chunk[i];
+                for (int32_t j = i + 1; j < np; j++) HIST_PAIR(p1, (int64_t)chunk[j]);
+                for (int32_t k = 0; k < s->nbr_cnt[ch]; k++) {
+                    int64_t nb = s->nbr[ch * 4 + k];
+                    const int32_t* nchunk = s->chunk_particles + nb * s->cap;
+                    for (int32_t j = 0; j < s->num_in_chunk[nb]; j++) HIST_PAIR(p1, (int64_t)nchunk[j]);
+                }
+            }
+        }
+    }
+    #undef HIST_PAIR
+    return MAVI_OK;
+}
+
 /* Particle neighbour lists of the rings model (src/rings/neighbors.jl:116-136,
  * called from calc_interaction, src/rings/integration.jl:32-44): every
  * candidate pair (i, j) of the chunk loop with dist < max_dist * tol, where

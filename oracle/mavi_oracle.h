@@ -52,6 +52,7 @@ int32_t oracle_get_time(OracleSys* s, int64_t* num_steps, double* time);
 int32_t oracle_set_time(OracleSys* s, int64_t num_steps, double time);
 int32_t oracle_get_areas(OracleSys* s, double* areas);
 int64_t oracle_count_pairs(OracleSys* s);
+int32_t oracle_pair_distribution(OracleSys* s, double r_max, int32_t nbins, uint64_t* counts);
 int32_t oracle_rings_neighbors(OracleSys* s, double tol, int32_t type_all, int32_t max_list, int32_t* counts,
                                int32_t* lists);
 /* Variable rings ids with sources and sinks, as mavi_rings_sources; the step's

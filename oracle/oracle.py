@@ -55,6 +55,7 @@ def _load_lib():
         "oracle_set_time": (C.c_int32, [vp, C.c_int64, C.c_double]),
         "oracle_get_areas": (C.c_int32, [vp, dp]),
         "oracle_count_pairs": (C.c_int64, [vp]),
+        "oracle_pair_distribution": (C.c_int32, [vp, C.c_double, C.c_int32, C.POINTER(C.c_uint64)]),
         "oracle_rings_neighbors": (C.c_int32, [vp, C.c_double, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                                C.POINTER(C.c_int32)]),
         "oracle_rings_sources": (C.c_int32, [vp, ip, C.c_int32, C.POINTER(abi.MaviSourceEntry),
@@ -206,6 +207,13 @@ class OracleSystem:
 
     def count_pairs(self) -> int:
         return int(self.lib.oracle_count_pairs(self.h))
+
+    def pair_distribution(self, r_max: float, nbins: int) -> np.ndarray:
+        """Pair-distance histogram counts (num_bins uint64) of the current state."""
+        out = np.zeros(int(nbins), dtype=np.uint64)
+        self._ck(self.lib.oracle_pair_distribution(self.h, float(r_max), int(nbins),
+                                                   out.ctypes.data_as(C.POINTER(C.c_uint64))), "pair_distribution")
+        return out
 
     def rings_sources(self, mask, num_entries, entries, boxes, spawn_xy, chunk_rc):
         """Variable rings ids with sources and sinks (the arguments of

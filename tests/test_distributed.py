@@ -23,6 +23,12 @@ def _free_port():
         return s.getsockname()[1]
 
 
+def id_of(system):
+    """A replica's identity: its size and first position (the generator draws
+    every replica's size and positions from one seeded stream)."""
+    return (int(system.num_slots), float(system.state.pos[0, 0]), float(system.state.pos[0, 1]))
+
+
 def _worker(rank, world, port, result_dir):
     sys.path.insert(0, str(ROOT))
     import torch.distributed as dist
@@ -46,8 +52,19 @@ def _worker(rank, world, port, result_dir):
                                           "load": int(sum(sizes[i] for i in mine)),
                                           "partition": replicas.shard_replicas(sizes, world)})
         t = replicas.max_over_ranks(1.5 + rank, dist)
+        # the benchmark's own sharding path: lj_batch_512 at two ranks is 1,024
+        # replicas, each rank building only its share
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("bench_mod", ROOT / "bench.py")
+        bench = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(bench)
+        share, _ = bench.workload_share("lj_batch_512", "mixed", rank, world)
+        bench_ids = [id_of(s) for s in share]
+        bench_gathered = [None] * world
+        dist.all_gather_object(bench_gathered, {"ids": bench_ids, "n": int(sum(s.num_slots for s in share))})
         np.save(os.path.join(result_dir, f"r{rank}.npy"),
-                np.array([{"gathered": gathered, "sizes": sizes, "tmax": t}], dtype=object))
+                np.array([{"gathered": gathered, "sizes": sizes, "tmax": t, "bench": bench_gathered}],
+                         dtype=object))
     finally:
         dist.destroy_process_group()
 
@@ -86,3 +103,12 @@ def test_two_rank_gloo_replica_sharding(tmp_path, mg):
     assert abs(g0[0]["load"] - g0[1]["load"]) <= max(out[0]["sizes"])
     # job time = the slowest rank
     assert out[0]["tmax"] == out[1]["tmax"] == 2.5
+    # the benchmark's split of the 1,024-replica batch: disjoint shares that
+    # together are exactly the replicas the generator makes, balanced by particles
+    b = out[0]["bench"]
+    from mavi_gb300 import workloads
+    every, _ = workloads.lj_batch(num_replicas=1024, precision="mixed")
+    assert sorted(b[0]["ids"] + b[1]["ids"]) == sorted(id_of(s) for s in every)
+    assert not set(b[0]["ids"]) & set(b[1]["ids"])
+    assert b[0]["n"] + b[1]["n"] == sum(s.num_slots for s in every)
+    assert abs(b[0]["n"] - b[1]["n"]) <= max(s.num_slots for s in every)

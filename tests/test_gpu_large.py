@@ -160,27 +160,36 @@ def test_rings_64_every_replica(mg, orc, wl, precision):
     b.close()
 
 
-def test_lj_4194304_energy_series_mixed_follows_fp64(mg, wl):
-    """The 4,194,304-particle periodic LJ state (velocity Verlet, dt = 5e-4):
-    over 2,000 steps the total energy of the mixed form follows the FP64
-    form's, sampled every 200 steps. Trajectories diverge chaotically, so the
-    comparison is of the conserved quantity: the two series and their drifts
-    agree to 1e-6 of the total energy."""
-    series = {}
+def test_lj_4194304_energy_and_pair_distribution_mixed_follow_fp64(mg, wl):
+    """The 4,194,304-particle periodic LJ state (velocity Verlet, dt = 5e-4)
+    over 2,000 steps from the same start in both forms. Trajectories diverge
+    chaotically, so the forms are compared on the conserved quantity and on
+    the structure: the total-energy series (device-side, every 200 steps) and
+    its drift agree to 1e-6 of the total energy, and the final g(r) (bins of
+    0.02 up to 2.5) agree within five standard deviations of the counting
+    noise of two independent samples, sqrt(n_fp64 + n_mixed) per bin."""
+    from mavi_gb300 import workloads
+    series, hist = {}, {}
+    r_max, nb = 2.5, 125
     for precision in ("fp64", "mixed"):
         s, step = wl.lj_4194304(precision=precision)
-        e = [sum(s.energies())]
-        for _ in range(10):
-            mg.run_system(s, num_steps=200, step_func=step)
-            ke, pe = s.energies()
-            e.append(ke + pe)
-        series[precision] = np.array(e)
+        e0 = sum(s.energies())
+        ke, pe = s.energy_series(10, 200, step)
+        series[precision] = np.concatenate([[e0], ke + pe])
+        hist[precision] = s.pair_distribution(r_max, nb).astype(np.float64)
+        n, area = s.num_slots, s.space_cfg.geometry_cfg.length ** 2
         s.close()
     e64, emx = series["fp64"], series["mixed"]
     scale = np.abs(e64).max()
     d64 = (e64[-1] - e64[0]) / scale
     dmx = (emx[-1] - emx[0]) / scale
-    print(f"lj_4194304 energy drift over 2000 steps: fp64 {d64:.3e}, mixed {dmx:.3e}, "
-          f"max series difference {np.max(np.abs(emx - e64)) / scale:.3e}")
+    _, g64 = mg.pair_correlation(hist["fp64"], r_max, n, area)
+    _, gmx = mg.pair_correlation(hist["mixed"], r_max, n, area)
+    noise = np.sqrt(hist["fp64"] + hist["mixed"]) * (g64 / np.maximum(hist["fp64"], 1))
+    linf = float(np.max(np.abs(gmx - g64)))
+    print(f"lj_4194304 over 2000 steps: energy drift fp64 {d64:.3e}, mixed {dmx:.3e}, "
+          f"max series difference {np.max(np.abs(emx - e64)) / scale:.3e}; g(r) L-inf difference {linf:.3e}, "
+          f"largest 5-sigma counting bound {float(np.max(5 * noise)):.3e}")
     assert np.max(np.abs(emx - e64)) / scale < 1e-6
     assert abs(dmx - d64) < 1e-6
+    assert np.all(np.abs(gmx - g64) <= 5 * noise + 1e-12)

@@ -210,6 +210,27 @@ def test_particle_escaping_during_steps_reports_error(mg):
     s.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_jump_beyond_fixed_point_range(mg, precision):
+    """A particle that moves more than two chunks within one step (8 length
+    units against 3.05-unit chunks): the FP64 form steps on, as the reference
+    does; the mixed form, whose fixed-point offsets reach 1.5 chunks from the
+    centre of the chunk a particle is binned against, reports
+    MAVI_ERR_OFFSET_RANGE instead of forming wrong pair terms."""
+    s = lj_grid(mg, 8, 8, wall="periodic", chunks=(4, 4), precision=precision)
+    s.calc_forces()
+    s.state.vel[3] = (8000.0, 0.0)
+    s.upload()
+    if precision == "fp64":
+        mg.run_system(s, num_steps=1)
+        assert s.time_info.num_steps == 1
+    else:
+        with pytest.raises(mg.MaviError) as e:
+            mg.run_system(s, num_steps=1)
+        assert e.value.status == mg.abi.MAVI_ERR_OFFSET_RANGE
+    s.close()
+
+
 def test_outside_space_rejected_at_creation(mg):
     s = lj_grid(mg, 8, 8, wall="rigid", chunks=(4, 4))
     s.state.pos[0] = (-5.0, 1.0)

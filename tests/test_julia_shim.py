@@ -108,3 +108,13 @@ def test_julia_ccalls_have_the_prototypes_arity():
     for name, types in calls:
         n = len([x for x in types.split(",") if x.strip()])
         assert n == arity[name], (name, n, arity[name])
+
+
+def test_julia_bulk_drivers_are_defined_for_cuda_systems():
+    """run_system and run_experiment have methods for systems whose device is
+    CUDADevice (one mavi_step per event instead of one call per step); the
+    shim is not executed here, so the check is on its source."""
+    text = SHIM.read_text()
+    assert re.search(r"function Mavi\.RunSystem\.run_system\(system::CUDASystem;", text)
+    assert re.search(r"function EXP\.run_experiment\(experiment::EXP\.Experiment\{<:CUDASystem\}", text)
+    assert "gpu_run!(system, n)" in text and "gpu_run!(system, max(n, 1))" in text

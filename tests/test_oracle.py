@@ -219,3 +219,25 @@ def test_periodic_wrap(mg, orc):
     o.step(1)
     p, _, _ = o.state()
     assert p[0, 0] == pytest.approx(0.005) and p[1, 1] == pytest.approx(9.992)
+
+
+@pytest.mark.parametrize("wall", ["rigid", "periodic"])
+def test_pair_distribution_equals_brute_force(mg, orc, wall):
+    """The oracle's pair-distance histogram (chunk loop) against an independent
+    all-pairs count in numpy with the same IEEE operations: the minimum image
+    as calc_diff forms it, d = sqrt(dx*dx + dy*dy), bin floor(d / dr)."""
+    w = mg.RigidWalls() if wall == "rigid" else mg.PeriodicWalls()
+    s = _harm_system(mg, 300, w, 7)
+    L, r_max, nb = 24.0, 2.0, 40
+    o = orc.from_system(s)
+    counts = o.pair_distribution(r_max, nb)
+    p = s.state.pos
+    i, j = np.triu_indices(len(p), 1)
+    d = p[i] - p[j]
+    if wall == "periodic":
+        d = d - np.where(np.abs(d) > L / 2, np.copysign(L, d), 0.0)
+    dist = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1])
+    k = np.minimum((dist[dist < r_max] / (r_max / nb)).astype(np.int64), nb - 1)
+    expect = np.bincount(k, minlength=nb).astype(np.uint64)
+    assert counts.sum() > 0 and np.array_equal(counts, expect)
+    o.close()
