@@ -49,6 +49,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 import __graft_entry__ as graft  # noqa: E402
 
+GATHER_NAMES = {0: "staged", 1: "global", 2: "columns", 3: "tiles", 4: "tiles_queue"}
 METRIC = "particle-steps/s on 1 GB300, mixed+batched vs plain FP64, at ≤1e-5 rel force err"
 UNIT = "particle-steps/s"
 
@@ -645,7 +646,9 @@ def main():
             "config": {"workload": args.workload, "N": n, "replicas": len(runners["mixed"].systems),
                        "form": "mixed", "chunks": grid, "total_chunks": stats.total_chunks,
                        "candidate_pairs": stats.candidate_pairs,
-                       "gather": {0: "staged", 1: "global", 2: "columns"}.get(runners["mixed"].stats().gather_mode),
+                       "gather": GATHER_NAMES.get(runners["mixed"].stats().gather_mode),
+                       "autotuned_among": list(GATHER_NAMES.values()) if runners["mixed"].handle.tiles_possible
+                       else list(GATHER_NAMES.values())[:3],
                        "parallelism": (f"replicas split over {world} GPUs" if world > 1 else
                                        ("replicas" if len(runners["mixed"].systems) > 1 else "single")),
                        "l2": "flushed (256 MiB write) before every timed step"},

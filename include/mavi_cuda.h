@@ -51,6 +51,10 @@ extern "C" {
                                       than a chunk within one step); its fixed-point offset
                                       would leave the exact integer range. No reference
                                       counterpart: the FP64 form has no such limit */
+#define MAVI_ERR_FORCE_RANGE    12 /* mixed form, Lennard-Jones / WCA tiles only: a pair force
+                                      of magnitude 2^22 or more (particles closer than ~0.37
+                                      sigma), beyond the fixed-point force sums. No
+                                      reference counterpart: the FP64 form has no such limit */
 
 /* ---- enums -------------------------------------------------------------- */
 /* State kinds: src/states.jl:75 (SecondLawState), :104 (SelfPropelledState),
@@ -201,9 +205,15 @@ typedef struct MaviOptions {
     int32_t block_size;      /* threads per block for particle kernels (0 = tuned) */
     int32_t gather_mode;     /* pair gather: 0 = warp-staged shared-memory window,
                                 1 = per-thread global loads chunk by chunk,
-                                2 = per-thread contiguous row ranges per column,
-                                -1 = autotuned at creation (fastest force pass);
-                                all add the same terms in the same order        */
+                                2 = per-thread contiguous row ranges per column
+                                (0-2 add the same terms in the same order);
+                                mixed Lennard-Jones / WCA with chunks only:
+                                3 = Newton's third law inside tiles of chunks,
+                                    one CTA per tile,
+                                4 = the same tiles from a device work queue
+                                    (persistent CTAs); 3 and 4 give the same
+                                    bits (fixed-point sums);
+                                -1 = autotuned at creation (fastest force pass) */
 } MaviOptions;
 
 /* Work counters of the last force pass (for roofline accounting). */

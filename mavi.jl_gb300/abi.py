@@ -24,6 +24,7 @@ MAVI_ERR_NO_DEVICE = 8
 MAVI_ERR_NOISE_MISSING = 9
 MAVI_ERR_NEIGHBOR_OVERFLOW = 10
 MAVI_ERR_OFFSET_RANGE = 11
+MAVI_ERR_FORCE_RANGE = 12
 MAVI_MAX_NEIGHBORS = 15
 
 MAVI_STATE_SECOND_LAW = 0

@@ -277,8 +277,12 @@ class CUDADevice:
     noise: "device" (Philox on the GPU, seeded) or "injected" (the caller
     supplies each step's noise numbers).
     gather: pair gather — "staged" (warp window in shared memory), "global"
-    (chunk by chunk), "columns" (contiguous row ranges per column) or "auto"
-    (the fastest force pass at creation); all give identical results."""
+    (chunk by chunk), "columns" (contiguous row ranges per column), which give
+    identical results; for the mixed Lennard-Jones / WCA passes also "tiles"
+    (Newton's third law inside tiles of chunks, a CTA per tile) and
+    "tiles_queue" (the same tiles pulled from a device work queue by
+    persistent CTAs), identical to each other; or "auto" (the fastest force
+    pass at creation)."""
     precision: str = "fp64"
     device: int = 0
     use_graph: bool = True
@@ -293,7 +297,7 @@ class CUDADevice:
         o.seed = int(self.seed) & ((1 << 64) - 1)
         o.device = int(self.device)
         o.use_graph = 1 if self.use_graph else 0
-        o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2}[self.gather]
+        o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2, "tiles": 3, "tiles_queue": 4}[self.gather]
         return o
 
 

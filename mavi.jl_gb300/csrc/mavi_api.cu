@@ -430,6 +430,10 @@ static int check_device_error(MaviSystem* s) {
         return fail(s, e.code, "chunk %lld holds more particles than its capacity (particle %d)", (long long)e.aux, uid);
     case MAVI_ERR_NONFINITE:
         return fail(s, e.code, "particle %d has a non-finite position", uid);
+    case MAVI_ERR_FORCE_RANGE:
+        return fail(s, e.code,
+                    "a pair force on particle %d reached 2^22 (particles closer than ~0.37 sigma); the mixed form's "
+                    "fixed-point force sums cannot hold it", uid);
     case MAVI_ERR_OFFSET_RANGE:
         return fail(s, e.code,
                     "particle %d is more than 1.5 chunks from the centre of its chunk (it moved more than a chunk "
@@ -476,7 +480,8 @@ static int autotune_gather(MaviSystem* s) {
     CUDA_TRY(s, cudaEventCreate(&b));
     float best = INFINITY;
     int best_mode = 0;
-    for (int mode = 0; mode < kNumGatherModes; mode++) {
+    const int modes = s->tiles ? kNumPassModes : kNumGatherModes;   // tiles: mixed Lennard-Jones / WCA
+    for (int mode = 0; mode < modes; mode++) {
         s->C.gather_mode = mode;
         for (int w = 0; w < 2; w++) {
             if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, 0);
@@ -524,6 +529,7 @@ const char* mavi_status_string(int st) {
     case MAVI_ERR_NOISE_MISSING: return "noise not supplied";
     case MAVI_ERR_NEIGHBOR_OVERFLOW: return "neighbour list overflow";
     case MAVI_ERR_OFFSET_RANGE: return "particle beyond the mixed form's fixed-point offset range";
+    case MAVI_ERR_FORCE_RANGE: return "pair force beyond the mixed form's fixed-point force range";
     }
     return "unknown status";
 }
@@ -559,7 +565,7 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     s->params.assign(replicas, replicas + num_replicas);
     s->prec = opt->precision;
     if ((s->prec != MAVI_PREC_FP64 && s->prec != MAVI_PREC_MIXED) || opt->gather_mode < -1 ||
-        opt->gather_mode >= kNumGatherModes) {
+        opt->gather_mode >= kNumPassModes) {
         delete s;
         return MAVI_ERR_INVALID_ARG;
     }
@@ -813,6 +819,39 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     C.gather_mode = opt->gather_mode;
     C.num_reps = s->R;
     C.seed = opt->seed;
+
+    // Newton's-third-law tiles (mixed Lennard-Jones / WCA, every replica with
+    // chunks): square tiles whose window (tile plus a one-chunk halo) holds
+    // about 0.85 kTileThreads particles at the replica's mean chunk
+    // occupancy, side 2..kTileMaxDim chunks, column-major per replica
+    bool tiled = s->prec == MAVI_PREC_MIXED && (s->dyn == MAVI_DYN_LEN_JONES || s->dyn == MAVI_DYN_RUN_TUMBLE);
+    for (int r = 0; r < s->R && tiled; r++) tiled = s->reps_h[r].has_chunks != 0;
+    if (!tiled && opt->gather_mode >= kGatherTiles)
+        return bail(fail(s, MAVI_ERR_UNSUPPORTED,
+                         "gather modes 3 and 4 (tiles) serve the mixed Lennard-Jones / WCA passes with chunks"));
+    if (tiled) {
+        std::vector<TileDesc> th;
+        for (int r = 0; r < s->R; r++) {
+            const DevRep& R = s->reps_h[r];
+            const double per_chunk = std::max(1e-3, (double)R.na / ((double)R.rows * R.cols));
+            const int win = (int)std::floor(std::sqrt(0.85 * kTileThreads / per_chunk));
+            const int side = std::max(2, std::min(kTileMaxDim, win - 2));
+            const int w = std::min(side, (int)R.cols), h = std::min(side, (int)R.rows);
+            for (int c0 = 0; c0 < R.cols; c0 += w)
+                for (int r0 = 0; r0 < R.rows; r0 += h)
+                    th.push_back(TileDesc{r, c0, r0, std::min(w, R.cols - c0) | (std::min(h, R.rows - r0) << 8)});
+        }
+        s->ntiles_t = (int32_t)th.size();
+        if (dalloc(s, &s->tiles, th.size()) != cudaSuccess || dalloc(s, &s->tile_queue, 2) != cudaSuccess)
+            return bail(fail(s, MAVI_ERR_CUDA, "cudaMalloc failed for the tiles"));
+        if (cudaMemcpyAsync(s->tiles, th.data(), sizeof(TileDesc) * th.size(), cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess)
+            return bail(fail(s, MAVI_ERR_CUDA, "tile table upload failed"));
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        s->tile_grid = (unsigned)std::max(1, sms * MAVI_TILE_BLOCKS);
+    }
 
     // descriptors
     std::vector<MaviSpace> spaces_h((size_t)s->R * MAVI_MAX_SPACES);

@@ -672,8 +672,27 @@ __device__ __forceinline__ void lj_pair_df(const DevRep& R, int32_t dxi, int32_t
     fyl = fmaf(sh, yh, -fyh) + fmaf(sh, yl, sl * yh);
 }
 
-// Force accumulators. Mixed form: FP32, Kahan-compensated for Lennard-Jones
-// (no cutoff: tens of terms with cancellation), plain for the short-range laws.
+// Fixed-point force sums of the tiled (Newton's third law) Lennard-Jones /
+// WCA passes. A pair term h + l (double-float) becomes the int64
+// round(f 2^32), formed from a coarse part round(h 2^8) and the fine
+// remainder (h - coarse 2^-8 + l) 2^32, both int32 conversions. Integer sums
+// do not depend on the order of the terms, so shared-memory atomics from any
+// thread give the same bits every run; the resolution is 2^-32 per term. A
+// term of magnitude 2^22 or more (or not finite) sets `bad`
+// (MAVI_ERR_FORCE_RANGE).
+constexpr float kFixForceLimit = 1073741824.0f;   // 2^22 * 2^8: |f| < 2^22
+__device__ __forceinline__ long long fix_term(float h, float l, bool& bad) {
+    const float hs = h * 256.0f;
+    bad |= !(fabsf(hs) < kFixForceLimit);
+    const float c = rintf(fminf(fmaxf(hs, -kFixForceLimit), kFixForceLimit));
+    const float r = __fadd_rn(fmaf(-c, 0.00390625f, h), l);       // f - c 2^-8: |r| <= 2^-9
+    return ((long long)__float2int_rn(c) << 24) + (long long)__float2int_rn(r * 4294967296.0f);
+}
+__device__ __forceinline__ float fix_value(long long v) { return i64_to_f32(v) * 2.3283064365386963e-10f; }
+
+// Force accumulators of the per-particle gathers. Mixed form: FP32,
+// Kahan-compensated for Lennard-Jones (no cutoff: tens of terms with
+// cancellation), plain for the short-range laws.
 template <int PREC, int DYN> struct Acc;
 template <int DYN> struct Acc<kPrecFP64, DYN> {
     double x = 0, y = 0;
@@ -1064,6 +1083,9 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
 // in the same order, bitwise-identical sums).
 // ---------------------------------------------------------------------------
 constexpr int kNumGatherModes = 3; // staged window, per-chunk global, per-column global
+constexpr int kGatherTiles = 3;      // Lennard-Jones / WCA, mixed form: Newton's-third-law tiles, a CTA per tile
+constexpr int kGatherTilesQueue = 4; // the same tiles from a device work queue (persistent CTAs)
+constexpr int kNumPassModes = 5;
 constexpr int kStageParts = 256;   // staged particles per window
 constexpr int kPassThreads = 128;
 constexpr int kPassWarps = kPassThreads / 32;
@@ -1473,6 +1495,117 @@ __device__ __forceinline__ int64_t walls_and_bin(const Ctx& C, int32_t rep, cons
     return bin_final<PREC>(C, R, s, x, y, cell);
 }
 
+// The end of a pair pass for one particle, after its pair force is summed:
+// wall forces, then per pass the force output or the integration (Verlet
+// halves, overdamped, Szabo, RTP), walls! and the Julia-exact binning of the
+// new position. fx, fy: the pair force in FP64; gx, gy: the mixed form's FP32
+// sums (fx, fy widened); nb: rings neighbour count. Returns the new chunk (or
+// 0) and sets cap for the histogram.
+template <int PREC, int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
+__device__ __forceinline__ int64_t pass_epilogue(const Ctx& C, int64_t s, int32_t rep, const DevRep& R, int32_t cell,
+                                                 double2 p, double fx, double fy, float gx, float gy, int32_t nb,
+                                                 int32_t with_wall_forces, int32_t& cap) {
+    (void)gx; (void)gy; (void)nb;
+    int64_t new_cell = 0;
+    bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
+    if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
+    const double dt = R.dt;
+    if constexpr (PASS == kPassForce && DYN == MAVI_DYN_RINGS) {
+        // rings: the force in user order, where k_rings reads a ring's particles together
+        const int32_t u = C.uid_cur[s];
+        if constexpr (PREC == kPrecFP64) C.fd_u[u] = make_double2(fx, fy);
+        else C.ff_u[u] = make_float2(gx, gy);
+        if (C.nb_mode) C.nb_count[u] = nb;
+    } else if constexpr (PASS == kPassForce) {
+        if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
+        else if (walls_f) C.ff[s] = make_float2((float)fx, (float)fy);
+        else C.ff[s] = make_float2(gx, gy);
+    } else if constexpr (PASS == kPassVerlet1) {
+        // update_verlet! (src/integration.jl:415-431), first half
+        double2 v = C.vel_cur[s];
+        double term = dt * dt / 2;
+        double nx = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, dt), __dmul_rn(fx, term)));
+        double ny = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, dt), __dmul_rn(fy, term)));
+        C.pos_mid[s] = make_double2(nx, ny);
+        if constexpr (PREC == kPrecFP64) C.fold_d[s] = make_double2(fx, fy);
+        else {
+            C.fold_f[s] = make_float2((float)fx, (float)fy);
+            // offsets of x(t+dt) from the (stale) chunk of this step
+            int32_t lc = (int32_t)(cell - R.c0);
+            int64_t col = lc / R.rows, row = lc - col * R.rows;
+            double tx = __dsub_rn(nx, R.bb_blx), ty = __dadd_rn(__dadd_rn(-ny, R.bb_bly), R.bb_h);
+            C.off_mid[s] = fixed_offset(R, row, col, tx, ty, C.err, s);
+        }
+    } else {
+        double x = p.x, y = p.y, vx = 0, vy = 0;
+        if constexpr (HAS_VEL) { double2 v = C.vel_cur[s]; vx = v.x; vy = v.y; }
+        if constexpr (PASS == kPassVerlet2) {
+            double ox, oy;
+            if constexpr (PREC == kPrecFP64) { double2 o = C.fold_d[s]; ox = o.x; oy = o.y; }
+            else { float2 o = C.fold_f[s]; ox = o.x; oy = o.y; }
+            double h = dt / 2;
+            vx = __dadd_rn(vx, __dmul_rn(h, __dadd_rn(fx, ox)));
+            vy = __dadd_rn(vy, __dmul_rn(h, __dadd_rn(fy, oy)));
+        } else if constexpr (PASS == kPassOverdamped) {
+            if constexpr (PREC == kPrecFP64) {
+                x = __dadd_rn(x, __dmul_rn(fx, R.mdt));
+                y = __dadd_rn(y, __dmul_rn(fy, R.mdt));
+            } else {
+                // FP32 displacement (relative error 6e-8 of a step), FP64 position
+                x = __dadd_rn(x, f32_to_f64_bits(gx * R.mdt_f));
+                y = __dadd_rn(y, f32_to_f64_bits(gy * R.mdt_f));
+            }
+        } else if constexpr (PASS == kPassSzabo || PASS == kPassRTP) {
+            int32_t uid = C.uid_cur[s];
+            double theta = C.pol_cur[s];
+            double c_, s_;
+            sincos(theta, &s_, &c_);
+            int64_t step = C.d_step[0] - 1;
+            if constexpr (PASS == kPassSzabo) {
+                // update_szabo! (src/integration.jl:433-465)
+                double wx = __dadd_rn(__dmul_rn(R.vo, c_), __dmul_rn(R.mobility, fx));
+                double wy = __dadd_rn(__dmul_rn(R.vo, s_), __dmul_rn(R.mobility, fy));
+                double speed = sqrt(fabs(wx) + fabs(wy));
+                double cr = speed > 0 ? __ddiv_rn(__dsub_rn(__dmul_rn(c_, wy), __dmul_rn(s_, wx)), speed) : 0.0;
+                if (fabs(cr) > 1) cr = jsign(cr);
+                double nz;
+                if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (uid - R.slot0)];
+                else nz = philox_normal(C.seed, (uint64_t)uid, (uint64_t)step);
+                double d_theta = 1 / R.relax_time * asin(cr) * dt + sqrt(2 * R.rot_diff * dt) * nz;
+                x = __dadd_rn(x, __dmul_rn(wx, dt));
+                y = __dadd_rn(y, __dmul_rn(wy, dt));
+                theta = theta + d_theta;
+            } else {
+                // update_rtp! (src/integration.jl:467-498)
+                double wx = __dadd_rn(__dmul_rn(R.vo, c_), fx);
+                double wy = __dadd_rn(__dmul_rn(R.vo, s_), fy);
+                x = __dadd_rn(x, __dmul_rn(wx, dt));
+                y = __dadd_rn(y, __dmul_rn(wy, dt));
+                double u1, u2;
+                if (C.noise_mode == MAVI_NOISE_INJECTED) {
+                    int64_t o = R.noise0 + 2 * (int64_t)(uid - R.slot0);
+                    u1 = C.noise[o];
+                    u2 = C.noise[o + 1];
+                } else {
+                    Rand2 r2 = philox_uniform2(C.seed, (uint64_t)uid, (uint64_t)step);
+                    u1 = r2.a;
+                    u2 = r2.b;
+                }
+                if (u1 < R.tumble_rate * dt) theta = 2 * 3.141592653589793 * u2;
+            }
+            C.pol_out[s] = theta;
+        }
+        new_cell = walls_and_bin<PREC>(C, rep, R, s, cell, x, y, vx, vy, HAS_VEL);
+        C.pos_out[s] = make_double2(x, y);
+        if constexpr (HAS_VEL) C.vel_out[s] = make_double2(vx, vy);
+        if constexpr (HAS_POL && !(PASS == kPassSzabo || PASS == kPassRTP)) C.pol_out[s] = C.pol_cur[s];
+        C.uid_out[s] = C.uid_cur[s];
+        if (C.num_reps > 1) C.rep_out[s] = rep;
+        cap = R.has_chunks ? R.cap : (1 << 30);
+    }
+    return new_cell;
+}
+
 #ifndef MAVI_PASS_BLOCKS_MIXED
 #define MAVI_PASS_BLOCKS_MIXED 8   // resident pair-pass blocks per SM, mixed form (64 registers)
 #endif
@@ -1528,107 +1661,283 @@ k_pass(Ctx C, int32_t with_wall_forces) {
     if (valid) {
         // FP32 sums widen on the integer pipes (f32_to_f64_bits), not the FP64 one
         double fx, fy;
+        float gx = 0.f, gy = 0.f;
         if constexpr (PREC == kPrecFP64) { fx = acc.gx(); fy = acc.gy(); }
-        else { fx = f32_to_f64_bits(acc.gx()); fy = f32_to_f64_bits(acc.gy()); }
-        bool walls_f = (PASS != kPassVerlet2) && with_wall_forces && R.has_wall_forces;
-        if (walls_f) add_wall_forces(C, rep, R, p.x, p.y, fx, fy);
-        const double dt = R.dt;
-        if constexpr (PASS == kPassForce && DYN == MAVI_DYN_RINGS) {
-            // rings: the force in user order, where k_rings reads a ring's particles together
-            const int32_t u = C.uid_cur[s];
-            if constexpr (PREC == kPrecFP64) C.fd_u[u] = make_double2(fx, fy);
-            else C.ff_u[u] = make_float2(acc.gx(), acc.gy());
-            if (C.nb_mode) C.nb_count[u] = acc.nb;
-        } else if constexpr (PASS == kPassForce) {
-            if constexpr (PREC == kPrecFP64) C.fd[s] = make_double2(fx, fy);
-            else if (walls_f) C.ff[s] = make_float2((float)fx, (float)fy);
-            else C.ff[s] = make_float2(acc.gx(), acc.gy());
-        } else if constexpr (PASS == kPassVerlet1) {
-            // update_verlet! (src/integration.jl:415-431), first half
-            double2 v = C.vel_cur[s];
-            double term = dt * dt / 2;
-            double nx = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, dt), __dmul_rn(fx, term)));
-            double ny = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, dt), __dmul_rn(fy, term)));
-            C.pos_mid[s] = make_double2(nx, ny);
-            if constexpr (PREC == kPrecFP64) C.fold_d[s] = make_double2(fx, fy);
-            else {
-                C.fold_f[s] = make_float2((float)fx, (float)fy);
-                // offsets of x(t+dt) from the (stale) chunk of this step
-                int32_t lc = (int32_t)(cell - R.c0);
-                int64_t col = lc / R.rows, row = lc - col * R.rows;
-                double tx = __dsub_rn(nx, R.bb_blx), ty = __dadd_rn(__dadd_rn(-ny, R.bb_bly), R.bb_h);
-                C.off_mid[s] = fixed_offset(R, row, col, tx, ty, C.err, s);
-            }
-        } else {
-            double x = p.x, y = p.y, vx = 0, vy = 0;
-            if constexpr (HAS_VEL) { double2 v = C.vel_cur[s]; vx = v.x; vy = v.y; }
-            if constexpr (PASS == kPassVerlet2) {
-                double ox, oy;
-                if constexpr (PREC == kPrecFP64) { double2 o = C.fold_d[s]; ox = o.x; oy = o.y; }
-                else { float2 o = C.fold_f[s]; ox = o.x; oy = o.y; }
-                double h = dt / 2;
-                vx = __dadd_rn(vx, __dmul_rn(h, __dadd_rn(fx, ox)));
-                vy = __dadd_rn(vy, __dmul_rn(h, __dadd_rn(fy, oy)));
-            } else if constexpr (PASS == kPassOverdamped) {
-                if constexpr (PREC == kPrecFP64) {
-                    x = __dadd_rn(x, __dmul_rn(fx, R.mdt));
-                    y = __dadd_rn(y, __dmul_rn(fy, R.mdt));
-                } else {
-                    // FP32 displacement (relative error 6e-8 of a step), FP64 position
-                    x = __dadd_rn(x, f32_to_f64_bits(acc.gx() * R.mdt_f));
-                    y = __dadd_rn(y, f32_to_f64_bits(acc.gy() * R.mdt_f));
-                }
-            } else if constexpr (PASS == kPassSzabo || PASS == kPassRTP) {
-                int32_t uid = C.uid_cur[s];
-                double theta = C.pol_cur[s];
-                double c_, s_;
-                sincos(theta, &s_, &c_);
-                int64_t step = C.d_step[0] - 1;
-                if constexpr (PASS == kPassSzabo) {
-                    // update_szabo! (src/integration.jl:433-465)
-                    double wx = __dadd_rn(__dmul_rn(R.vo, c_), __dmul_rn(R.mobility, fx));
-                    double wy = __dadd_rn(__dmul_rn(R.vo, s_), __dmul_rn(R.mobility, fy));
-                    double speed = sqrt(fabs(wx) + fabs(wy));
-                    double cr = speed > 0 ? __ddiv_rn(__dsub_rn(__dmul_rn(c_, wy), __dmul_rn(s_, wx)), speed) : 0.0;
-                    if (fabs(cr) > 1) cr = jsign(cr);
-                    double nz;
-                    if (C.noise_mode == MAVI_NOISE_INJECTED) nz = C.noise[R.noise0 + (uid - R.slot0)];
-                    else nz = philox_normal(C.seed, (uint64_t)uid, (uint64_t)step);
-                    double d_theta = 1 / R.relax_time * asin(cr) * dt + sqrt(2 * R.rot_diff * dt) * nz;
-                    x = __dadd_rn(x, __dmul_rn(wx, dt));
-                    y = __dadd_rn(y, __dmul_rn(wy, dt));
-                    theta = theta + d_theta;
-                } else {
-                    // update_rtp! (src/integration.jl:467-498)
-                    double wx = __dadd_rn(__dmul_rn(R.vo, c_), fx);
-                    double wy = __dadd_rn(__dmul_rn(R.vo, s_), fy);
-                    x = __dadd_rn(x, __dmul_rn(wx, dt));
-                    y = __dadd_rn(y, __dmul_rn(wy, dt));
-                    double u1, u2;
-                    if (C.noise_mode == MAVI_NOISE_INJECTED) {
-                        int64_t o = R.noise0 + 2 * (int64_t)(uid - R.slot0);
-                        u1 = C.noise[o];
-                        u2 = C.noise[o + 1];
-                    } else {
-                        Rand2 r2 = philox_uniform2(C.seed, (uint64_t)uid, (uint64_t)step);
-                        u1 = r2.a;
-                        u2 = r2.b;
-                    }
-                    if (u1 < R.tumble_rate * dt) theta = 2 * 3.141592653589793 * u2;
-                }
-                C.pol_out[s] = theta;
-            }
-            new_cell = walls_and_bin<PREC>(C, rep, R, s, cell, x, y, vx, vy, HAS_VEL);
-            C.pos_out[s] = make_double2(x, y);
-            if constexpr (HAS_VEL) C.vel_out[s] = make_double2(vx, vy);
-            if constexpr (HAS_POL && !(PASS == kPassSzabo || PASS == kPassRTP)) C.pol_out[s] = C.pol_cur[s];
-            C.uid_out[s] = C.uid_cur[s];
-            if (C.num_reps > 1) C.rep_out[s] = rep;
-            cap = R.has_chunks ? R.cap : (1 << 30);
-        }
+        else { gx = acc.gx(); gy = acc.gy(); fx = f32_to_f64_bits(gx); fy = f32_to_f64_bits(gy); }
+        new_cell = pass_epilogue<PREC, DYN, PASS, HAS_VEL, HAS_POL>(C, s, rep, R, cell, p, fx, fy, gx, gy, acc.nb,
+                                                                  with_wall_forces, cap);
     }
     if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
         count_into_chunk(C, valid, s, new_cell, cap);
+}
+
+// ===========================================================================
+// Tiled pair pass with Newton's third law (mixed form, Lennard-Jones / WCA).
+//
+// The reference evaluates each unordered candidate pair once and adds the
+// force to both particles (F[i] += f; F[j] -= f, src/integration.jl:131-132,
+// 150-151). Here a CTA owns a tile of whole chunks (w x h chunks of one
+// replica; chunk grids are static, so tiles are fixed at creation) and stages
+// the fixed-point offsets of the tile and of a one-chunk halo ring (the
+// "window") in shared memory, one thread per window chunk. Then every window
+// particle gets a thread:
+//  * an owned particle evaluates its pairs with owned particles later in the
+//    window order (its own chunk and the neighbouring owned chunks), adds the
+//    term to its own sum and subtracts it from the partner's;
+//  * a halo particle evaluates its pairs with the owned particles next to it
+//    and adds each term to the owned partner only (the halo particle's own
+//    tile evaluates the same pair for it).
+// So every pair with an owned particle is evaluated once per tile, the halo
+// work is spread over the halo particles' threads instead of loading the
+// tile's edge particles, and each thread runs one flat loop over its
+// candidates. Sums are fixed point in shared memory (fix_term): integer
+// atomics make them independent of the thread schedule, bit for bit. After a
+// barrier the owned particles run the pass's epilogue (integration, walls!,
+// binning, histogram).
+//
+// Tiles are handed to CTAs one per CTA (a grid of tiles) or through a device
+// work queue: a persistent grid of CTAs takes the next tile with an atomic
+// ticket until the tiles run out, and the last CTA to finish resets the queue
+// for the next launch. A tile whose window exceeds the shared-memory arrays
+// falls back to per-particle gathers for its owned particles.
+// ===========================================================================
+struct TileDesc {
+    int32_t rep, c0, r0, wh;   // replica, first column and row, w | (h << 8)
+};
+constexpr int kTileThreads = 256;
+constexpr int kTileMaxDim = 12;                       // tile side, chunks
+constexpr int kTileWin = kTileMaxDim + 2;             // window side, chunks
+constexpr int kTileWinChunks = kTileWin * kTileWin;   // 196 <= kTileThreads
+constexpr int kTileMaxWinParts = 1024;                // staged window particles
+constexpr int kTileMaxOwn = 640;                      // owned particles with shared sums
+#ifndef MAVI_TILE_BLOCKS
+#define MAVI_TILE_BLOCKS 4                            // resident tile CTAs per SM (64 registers)
+#endif
+
+// The passes that run tiled (Lennard-Jones: forces and both velocity-Verlet
+// halves; WCA: forces and the run-and-tumble update); other combinations use
+// the per-particle gathers.
+template <int DYN, int PASS>
+constexpr bool kTiledPass = (DYN == MAVI_DYN_LEN_JONES && (PASS == kPassForce || PASS == kPassVerlet1 ||
+                                                          PASS == kPassVerlet2)) ||
+                            (DYN == MAVI_DYN_RUN_TUMBLE && (PASS == kPassForce || PASS == kPassRTP));
+
+struct TileSmem {
+    int2 off[kTileMaxWinParts];             // fixed-point offsets of the window particles
+    unsigned long long acc[2][kTileMaxOwn]; // fixed-point force sums of the owned particles
+    int32_t cb[kTileWinChunks];             // window chunk -> first window index
+    int32_t ce[kTileWinChunks];             // one past its last
+    int32_t gs[kTileWinChunks];             // first global slot of the window chunk
+    uint8_t wq[kTileMaxWinParts];           // window chunk of each window particle
+    int32_t own0[kTileMaxDim + 1];          // first owned index of each tile column
+    int32_t nwin, nown, tile;
+    int scan[32];
+};
+
+// The fixed-point force on the particle with offset a from the one with
+// offset b; (shx, shy): the centre of b's chunk relative to a's, exact units.
+// Returns false when the pair lies outside the WCA cutoff.
+template <int DYN>
+__device__ __forceinline__ bool tile_term(const DevRep& R, const FixPair& fp0, int2 a, int2 b, int32_t shx,
+                                          int32_t shy, bool mi, long long& tx, long long& ty, bool& bad) {
+    int32_t dxi = (int32_t)((uint32_t)a.x - (uint32_t)b.x + (uint32_t)shx);
+    int32_t dyi = (int32_t)((uint32_t)a.y - (uint32_t)b.y + (uint32_t)shy);
+    if (mi) {
+        if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
+        if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
+    }
+    if constexpr (DYN == MAVI_DYN_RUN_TUMBLE) {
+        if (!inside_cutoff(fp0, dxi, dyi)) return false;
+    }
+    float fxh, fxl, fyh, fyl;
+    lj_pair_df(R, dxi, dyi, fxh, fxl, fyh, fyl);
+    tx = fix_term(fxh, fxl, bad);
+    ty = fix_term(fyh, fyl, bad);
+    return true;
+}
+
+template <int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
+__global__ void __launch_bounds__(kTileThreads, MAVI_TILE_BLOCKS)
+k_tpass(Ctx C, int32_t with_wall_forces, const TileDesc* __restrict__ tiles, int32_t ntiles,
+        int32_t* __restrict__ queue, int32_t persistent) {
+    __shared__ TileSmem sm;
+    const int2* Po = (PASS == kPassVerlet2) ? C.off_mid : C.off_cur;
+    const double2* Pd = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    const int tid = threadIdx.x;
+    int32_t t = blockIdx.x;
+    for (;;) {
+        if (persistent) {
+            __syncthreads();   // the previous tile is done with the shared arrays
+            if (tid == 0) sm.tile = atomicAdd(&queue[0], 1);
+            __syncthreads();
+            t = sm.tile;
+        }
+        if (t >= ntiles) break;
+        const TileDesc td = tiles[t];
+        const int32_t rep = td.rep;
+        const DevRep& R = C.reps[rep];
+        const int w = td.wh & 0xff, h = td.wh >> 8;
+        const int H = h + 2, nq = (w + 2) * H;
+        // 1. window chunks, column-major: q = k * H + qq is column c0 - 1 + k, row r0 - 1 + qq
+        int32_t cnt = 0;
+        if (tid < nq) {
+            const int k = tid / H, qq = tid - k * H;
+            int gc = td.c0 - 1 + k, gr = td.r0 - 1 + qq;
+            bool inside = true;
+            if (R.periodic) {
+                gc = gc < 0 ? gc + R.cols : (gc >= R.cols ? gc - R.cols : gc);
+                gr = gr < 0 ? gr + R.rows : (gr >= R.rows ? gr - R.rows : gr);
+            } else {
+                inside = gc >= 0 && gc < R.cols && gr >= 0 && gr < R.rows;
+            }
+            int32_t b = 0;
+            if (inside) {
+                const int64_t ch = R.c0 + (int64_t)gc * R.rows + gr;
+                b = C.start[ch];
+                cnt = C.start[ch + 1] - b;
+            }
+            sm.gs[tid] = b;
+        }
+        int total;
+        const int ex = block_exclusive_scan(cnt, sm.scan, total);   // nq <= 196 <= blockDim
+        if (tid < nq) { sm.cb[tid] = ex; sm.ce[tid] = ex + cnt; }
+        if (tid == 0) sm.nwin = total;
+        __syncthreads();
+        if (tid <= w) {
+            // owned particles: window columns 1..w, rows 1..h, contiguous per column
+            int32_t o = 0;
+            for (int k = 1; k <= tid; k++) o += sm.ce[k * H + h] - sm.cb[k * H + 1];
+            sm.own0[tid] = o;
+            if (tid == w) sm.nown = o;
+        }
+        __syncthreads();
+        const int32_t nwin = sm.nwin, nown = sm.nown;
+        const bool staged = nwin <= kTileMaxWinParts && nown <= kTileMaxOwn;
+        if (staged) {
+            if (tid < nq) {   // a thread per window chunk: its particles are consecutive slots
+                const int32_t b = sm.cb[tid], e = sm.ce[tid], g0 = sm.gs[tid] - b;
+                for (int32_t i = b; i < e; i++) {
+                    sm.off[i] = Po[g0 + i];
+                    sm.wq[i] = (uint8_t)tid;
+                }
+            }
+            for (int32_t i = tid; i < nown; i += kTileThreads) { sm.acc[0][i] = 0ull; sm.acc[1][i] = 0ull; }
+        }
+        __syncthreads();
+        // 2. pair terms, a thread per window particle, one flat loop over its candidates
+        if (staged) {
+            const FixPair& fp0 = C.fix[(int64_t)rep * MAVI_MAX_TYPES * MAVI_MAX_TYPES];
+            for (int32_t x = tid; x < nwin; x += kTileThreads) {
+                const int q = sm.wq[x], k = q / H, qq = q - k * H;
+                const bool own_x = k >= 1 && k <= w && qq >= 1 && qq <= h;
+                // true grid position of x (a halo position may wrap)
+                int gcol = td.c0 - 1 + k, grow = td.r0 - 1 + qq;
+                bool xw = false;
+                if (R.periodic) {
+                    if (gcol < 0) { gcol += R.cols; xw = true; } else if (gcol >= R.cols) { gcol -= R.cols; xw = true; }
+                    if (grow < 0) { grow += R.rows; xw = true; } else if (grow >= R.rows) { grow -= R.rows; xw = true; }
+                }
+                const bool raw = xw && !R.min_image;                 // periodic walls without minimum image
+                const bool mi = R.min_image && (xw || R.mi_small);
+                const int2 mx = sm.off[x];
+                long long X = 0, Y = 0;
+                bool bad = false;
+                int r = 0, dk = 0, dq = 0;
+                int32_t j = 0, e = 0, jown0 = 0;
+                for (;;) {
+                    while (j >= e && r < 9) {   // next owned neighbour chunk with candidates
+                        dk = r / 3 - 1;
+                        dq = r - 3 * (r / 3) - 1;
+                        r++;
+                        const int nk = k + dk, nqq = qq + dq;
+                        if (nk < 1 || nk > w || nqq < 1 || nqq > h) continue;
+                        const int wqn = nk * H + nqq;
+                        j = own_x ? max(sm.cb[wqn], x + 1) : sm.cb[wqn];
+                        e = sm.ce[wqn];
+                        jown0 = sm.own0[nk - 1] - sm.cb[nk * H + 1];
+                    }
+                    if (j >= e) break;
+                    const int2 mj = sm.off[j];
+                    long long tx, ty;
+                    if (own_x) {
+                        // both owned (never through a wrap): x's term, and its negation for j
+                        if (tile_term<DYN>(R, fp0, mx, mj, -dk * R.sx_i, dq * R.sy_i, R.min_image && R.mi_small, tx,
+                                           ty, bad)) {
+                            X += tx;
+                            Y += ty;
+                            atomicAdd(&sm.acc[0][jown0 + j], (unsigned long long)(-tx));
+                            atomicAdd(&sm.acc[1][jown0 + j], (unsigned long long)(-ty));
+                        }
+                    } else {
+                        // the owned j's term from the halo particle x
+                        bool ok = true;
+                        if (raw) {
+                            const int jcol = td.c0 + k + dk - 1, jrow = td.r0 + qq + dq - 1;
+                            const double dx = (double)((long long)mj.x - mx.x - (long long)(gcol - jcol) * R.sx_u) / R.inv_u;
+                            const double dy = (double)((long long)mj.y - mx.y + (long long)(grow - jrow) * R.sy_u) / R.inv_u;
+                            const double sc = pair_scalar<DYN, double>(R.pd, dx * dx + dy * dy);
+                            tx = fix_term((float)(sc * dx), 0.f, bad);
+                            ty = fix_term((float)(sc * dy), 0.f, bad);
+                        } else {
+                            ok = tile_term<DYN>(R, fp0, mj, mx, dk * R.sx_i, -dq * R.sy_i, mi, tx, ty, bad);
+                        }
+                        if (ok) {
+                            atomicAdd(&sm.acc[0][jown0 + j], (unsigned long long)tx);
+                            atomicAdd(&sm.acc[1][jown0 + j], (unsigned long long)ty);
+                        }
+                    }
+                    j++;
+                }
+                if (own_x) {
+                    const int32_t o = sm.own0[k - 1] + (x - sm.cb[k * H + 1]);
+                    atomicAdd(&sm.acc[0][o], (unsigned long long)X);
+                    atomicAdd(&sm.acc[1][o], (unsigned long long)Y);
+                }
+                if (bad) raise_error(C.err, MAVI_ERR_FORCE_RANGE, sm.gs[q] + (x - sm.cb[q]), 0);
+            }
+        }
+        __syncthreads();
+        // 3. epilogue per owned particle (a tile that was not staged gathers its pair sums here);
+        // warp-uniform trip counts: the histogram needs whole warps
+        for (int32_t base = 0; base < nown; base += kTileThreads) {
+            const int32_t o = base + tid;
+            const bool valid = o < nown;
+            int64_t s = 0, new_cell = 0;
+            int32_t cap = 1 << 30;
+            if (valid) {
+                int kc = 0;
+                while (kc + 1 < w && sm.own0[kc + 1] <= o) kc++;
+                s = sm.gs[(kc + 1) * H + 1] + (o - sm.own0[kc]);   // owned chunks of a column: consecutive slots
+                const int32_t cell = C.cell_cur[s];
+                float gx, gy;
+                if (staged) {
+                    gx = fix_value((long long)sm.acc[0][o]);
+                    gy = fix_value((long long)sm.acc[1][o]);
+                } else {
+                    Acc<kPrecMixed, DYN> acc;
+                    const Me<kPrecMixed, DYN> me = make_me<kPrecMixed, DYN>(C, R, rep, s, Po);
+                    gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, Po, me, acc);
+                    gx = acc.gx();
+                    gy = acc.gy();
+                }
+                new_cell = pass_epilogue<kPrecMixed, DYN, PASS, HAS_VEL, HAS_POL>(
+                    C, s, rep, R, cell, Pd[s], f32_to_f64_bits(gx), f32_to_f64_bits(gy), gx, gy, 0, with_wall_forces,
+                    cap);
+            }
+            if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
+                count_into_chunk(C, valid, s, new_cell, cap);
+        }
+        if (!persistent) break;
+    }
+    if (persistent && tid == 0) {
+        // every CTA has drawn its last ticket before it counts itself done, so
+        // the last one may reset the queue for the next launch
+        __threadfence();
+        if (atomicAdd(&queue[1], 1) == (int32_t)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+        }
+    }
 }
 
 // ===========================================================================

@@ -21,8 +21,31 @@ void count(MaviSystem* s, int use_guess, const double2* src) {
     k_count<PREC><<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, use_guess, src);
 }
 
+// Tiled Newton's-third-law pass (mixed Lennard-Jones / WCA): a CTA per tile,
+// or a persistent grid pulling tiles from the device work queue.
+template <int DYN, int PASS>
+void tpass(MaviSystem* s, int with_walls) {
+    const int32_t q = s->C.gather_mode == kGatherTilesQueue ? 1 : 0;
+    const unsigned g = q ? s->tile_grid : (unsigned)s->ntiles_t;
+    if (s->has_vel)
+        k_tpass<DYN, PASS, true, false><<<g, kTileThreads, 0, s->stream>>>(s->C, with_walls, s->tiles, s->ntiles_t,
+                                                                           s->tile_queue, q);
+    else if (s->has_pol)
+        k_tpass<DYN, PASS, false, true><<<g, kTileThreads, 0, s->stream>>>(s->C, with_walls, s->tiles, s->ntiles_t,
+                                                                           s->tile_queue, q);
+    else
+        k_tpass<DYN, PASS, false, false><<<g, kTileThreads, 0, s->stream>>>(s->C, with_walls, s->tiles, s->ntiles_t,
+                                                                            s->tile_queue, q);
+}
+
 template <int PREC, int DYN, int PASS>
 void pass(MaviSystem* s, int with_walls) {
+    if constexpr (PREC == kPrecMixed && kTiledPass<DYN, PASS>) {
+        if (s->tiles && s->C.gather_mode >= kGatherTiles) {
+            tpass<DYN, PASS>(s, with_walls);
+            return;
+        }
+    }
     unsigned g = nblocks(s->M, kPassThreads);
     if (s->has_vel) k_pass<PREC, DYN, PASS, true, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
     else if (s->has_pol) k_pass<PREC, DYN, PASS, false, true><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);

@@ -48,6 +48,12 @@ struct MaviSystem {
     double* series = nullptr;          // energy series (mavi_energy_series), grown on demand
     int64_t series_cap = 0;            // doubles
     unsigned long long* hist = nullptr;    // pair-distance histogram bins (mavi_pair_distribution)
+    // Newton's-third-law tiles of the mixed Lennard-Jones / WCA passes (static:
+    // chunk grids do not change), the work-queue tickets and the persistent grid
+    mavi::TileDesc* tiles = nullptr;
+    int32_t ntiles_t = 0;
+    int32_t* tile_queue = nullptr;
+    unsigned tile_grid = 0;
     double* noise_cur = nullptr;
     double* noise_queue = nullptr;
     int64_t noise_queue_cap = 0, noise_queue_len = 0, noise_queue_pos = 0;

@@ -221,6 +221,13 @@ class _Handle:
         self.check(self.lib.mavi_energies(self.handle, pe_mode, abi.as_dptr(ke), abi.as_dptr(pe)), "mavi_energies")
         return ke, pe
 
+    @property
+    def tiles_possible(self) -> bool:
+        """Whether the tiled Newton's-third-law modes serve this handle (mixed
+        Lennard-Jones / WCA with chunks in every replica)."""
+        return (self.device.precision == "mixed" and self.systems[0].dynamic_cfg.__class__.__name__ in
+                ("LenJonesCfg", "RunTumbleCfg") and all(s.int_cfg.chunks_cfg is not None for s in self.systems))
+
     def stats(self) -> abi.MaviStats:
         st = abi.MaviStats()
         self.check(self.lib.mavi_get_stats(self.handle, C.byref(st)), "mavi_get_stats")
