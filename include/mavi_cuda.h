@@ -213,6 +213,10 @@ typedef struct MaviOptions {
                                 4 = the same tiles from a device work queue
                                     (persistent CTAs); 3 and 4 give the same
                                     bits (fixed-point sums);
+                                mixed harmonic-truncated / Szabo only:
+                                5 = the column gather with 2 lanes per particle,
+                                6 = the same with 4 lanes (partial sums combined
+                                    in a fixed order);
                                 -1 = autotuned at creation (fastest force pass) */
 } MaviOptions;
 
@@ -222,7 +226,7 @@ typedef struct MaviStats {
     int64_t total_particles;
     int64_t total_chunks;
     int32_t max_chunk_count;  /* largest chunk occupancy at the last rebuild        */
-    int32_t gather_mode;      /* pair gather in use (MaviOptions.gather_mode)        */
+    int32_t gather_mode;      /* pass mode in use (MaviOptions.gather_mode 0..6)     */
 } MaviStats;
 
 /* Per-kernel device time accumulated while profiling is on (milliseconds). */

@@ -1,7 +1,8 @@
 """In-tree build of libmavi_cuda.so for sm_103a (GB300).
 
 The translation units (host runtime + C ABI, FP64 passes, mixed passes, the
-FMA peak probe, the allocation-free chunk lists, invasion detection) compile
+mixed multi-lane passes, the FMA peak probe, the allocation-free chunk lists,
+invasion detection) compile
 in parallel, then link into ``lib/libmavi_cuda.so``. No cmake.
 """
 from __future__ import annotations
@@ -16,8 +17,8 @@ PKG = pathlib.Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB = PKG / "lib"
 OBJ = PKG / "_build"
-SOURCES = ["mavi_api.cu", "mavi_steps_fp64.cu", "mavi_steps_mixed.cu", "mavi_peak.cu", "mavi_noalloc.cu",
-           "mavi_invasions.cu"]
+SOURCES = ["mavi_api.cu", "mavi_steps_fp64.cu", "mavi_steps_mixed.cu", "mavi_steps_lanes.cu", "mavi_peak.cu",
+           "mavi_noalloc.cu", "mavi_invasions.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -281,8 +281,10 @@ class CUDADevice:
     identical results; for the mixed Lennard-Jones / WCA passes also "tiles"
     (Newton's third law inside tiles of chunks, a CTA per tile) and
     "tiles_queue" (the same tiles pulled from a device work queue by
-    persistent CTAs), identical to each other; or "auto" (the fastest force
-    pass at creation)."""
+    persistent CTAs), identical to each other; for the mixed
+    harmonic-truncated and Szabo passes also "lanes2" / "lanes4" (the column
+    gather with 2 or 4 lanes per particle, partial sums combined in a fixed
+    order); or "auto" (the fastest force pass at creation)."""
     precision: str = "fp64"
     device: int = 0
     use_graph: bool = True
@@ -297,7 +299,8 @@ class CUDADevice:
         o.seed = int(self.seed) & ((1 << 64) - 1)
         o.device = int(self.device)
         o.use_graph = 1 if self.use_graph else 0
-        o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2, "tiles": 3, "tiles_queue": 4}[self.gather]
+        o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2, "tiles": 3, "tiles_queue": 4,
+                         "lanes2": 5, "lanes4": 6}[self.gather]
         return o
 
 

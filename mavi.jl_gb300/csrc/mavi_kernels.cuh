@@ -956,10 +956,16 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
 // ranges, so the loads hit L1). Same terms in the same order as the other
 // gathers, so the sums agree bitwise; suits sparse grids (about one particle
 // per chunk), where staging a window costs more than it saves.
+//
+// lane / lanes: with several lanes per particle (k_pass with LANES > 1) lane l
+// takes the candidates t = l, l + lanes, ... of the flat loop; outside the
+// flat loop lane 0 takes them all. The lanes' partial sums are combined in a
+// fixed order by the caller.
 template <int PREC, int DYN>
 __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
                                                const typename PartOf<PREC>::T* __restrict__ P,
-                                               const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc) {
+                                               const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc, int lane = 0,
+                                               int lanes = 1) {
     const int32_t lc = (int32_t)(cell - R.c0);
     const int32_t col = lc / R.rows, row = lc - col * R.rows;
     const bool rows_inside = row >= 1 && row + 1 < R.rows;
@@ -999,7 +1005,7 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
             const bool mi1 = R.min_image && (cws[1] || R.mi_small);
             const bool mi2 = R.min_image && (cws[2] || R.mi_small);
 #pragma unroll 4
-            for (int32_t t = 0; t < tot; t++) {
+            for (int32_t t = lane; t < tot; t += lanes) {
                 const bool k0 = t < n0, k1 = !k0 && t < n01;
                 const int32_t j = k0 ? g[0][0] + t : (k1 ? g[1][0] + (t - n0) : g[2][0] + (t - n01));
                 if (j == (int32_t)s) continue;
@@ -1014,6 +1020,7 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
             }
             return;
         }
+        if (lane != 0) return;
 #pragma unroll 1
         for (int k = 0; k < 3; k++) {
             const int dc = k - 1;
@@ -1036,6 +1043,7 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
         }
         return;
     }
+    if (lane != 0) return;
 #pragma unroll 1
     for (int dc = -1; dc <= 1; dc++) {
         int ncol = col + dc;
@@ -1085,7 +1093,9 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
 constexpr int kNumGatherModes = 3; // staged window, per-chunk global, per-column global
 constexpr int kGatherTiles = 3;      // Lennard-Jones / WCA, mixed form: Newton's-third-law tiles, a CTA per tile
 constexpr int kGatherTilesQueue = 4; // the same tiles from a device work queue (persistent CTAs)
-constexpr int kNumPassModes = 5;
+constexpr int kGatherLanes2 = 5;      // mixed short-range laws: column gather, 2 lanes per particle
+constexpr int kGatherLanes4 = 6;      // the same, 4 lanes per particle
+constexpr int kNumPassModes = 7;
 constexpr int kStageParts = 256;   // staged particles per window
 constexpr int kPassThreads = 128;
 constexpr int kPassWarps = kPassThreads / 32;
@@ -1669,6 +1679,56 @@ k_pass(Ctx C, int32_t with_wall_forces) {
     }
     if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
         count_into_chunk(C, valid, s, new_cell, cap);
+}
+
+// ===========================================================================
+// Several lanes per particle (mixed form, short-range laws). On sparse grids
+// (about one particle per chunk) a particle has only ~8 candidates, and one
+// lane per particle leaves the pass waiting on three dependent loads (chunk,
+// chunk bounds, neighbour offsets) with few pair terms to hide them. Here
+// LANES consecutive lanes share a particle: lane l takes the candidates
+// l, l + LANES, ... of the column gather's flat loop, and the partial sums are
+// combined by an xor butterfly (every lane ends with the same sum, formed in
+// the same order each run: deterministic). Lane 0 runs the epilogue.
+// ===========================================================================
+template <int DYN, int PASS>
+constexpr bool kLanesPass = (DYN == MAVI_DYN_HARM_TRUNC && (PASS == kPassForce || PASS == kPassOverdamped)) ||
+                            (DYN == MAVI_DYN_SZABO && (PASS == kPassForce || PASS == kPassSzabo));
+
+template <int DYN, int PASS, bool HAS_VEL, bool HAS_POL, int LANES>
+__global__ void __launch_bounds__(kPassThreads, MAVI_PASS_BLOCKS_MIXED) k_pass_lanes(Ctx C, int32_t with_wall_forces) {
+    static_assert(LANES == 2 || LANES == 4, "2 or 4 lanes per particle");
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t s = gt / LANES;
+    const int l = (int)(gt & (LANES - 1));
+    const bool valid = s < C.M;
+    const int32_t rep = (valid && C.num_reps > 1) ? C.rep_cur[s] : 0;
+    const DevRep& R = C.reps[rep];
+    const int32_t cell = valid ? C.cell_cur[s] : 0;
+    const int2* P = (PASS == kPassVerlet2) ? C.off_mid : C.off_cur;
+    const double2* Pd = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    const double2 p = (valid && l == 0) ? Pd[s] : make_double2(0.0, 0.0);
+    Acc<kPrecMixed, DYN> acc;
+    if (valid) {
+        const Me<kPrecMixed, DYN> me = make_me<kPrecMixed, DYN>(C, R, rep, s, P);
+        if (R.has_chunks) gather_columns<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc, l, LANES);
+        else if (l == 0) gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
+    }
+#pragma unroll
+    for (int o = 1; o < LANES; o <<= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    const bool lead = valid && l == 0;
+    int64_t new_cell = 0;
+    int32_t cap = 1 << 30;
+    if (lead) {
+        const float gx = acc.gx(), gy = acc.gy();
+        new_cell = pass_epilogue<kPrecMixed, DYN, PASS, HAS_VEL, HAS_POL>(
+            C, s, rep, R, cell, p, f32_to_f64_bits(gx), f32_to_f64_bits(gy), gx, gy, 0, with_wall_forces, cap);
+    }
+    if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
+        count_into_chunk(C, lead, s, new_cell, cap);
 }
 
 // ===========================================================================

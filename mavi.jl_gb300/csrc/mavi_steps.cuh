@@ -46,6 +46,12 @@ void pass(MaviSystem* s, int with_walls) {
             return;
         }
     }
+    if constexpr (PREC == kPrecMixed && kLanesPass<DYN, PASS>) {
+        if (s->lanes > 1) {
+            lanes_pass_mixed(s, DYN, PASS, with_walls);
+            return;
+        }
+    }
     unsigned g = nblocks(s->M, kPassThreads);
     if (s->has_vel) k_pass<PREC, DYN, PASS, true, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
     else if (s->has_pol) k_pass<PREC, DYN, PASS, false, true><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);

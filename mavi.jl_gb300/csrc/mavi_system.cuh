@@ -54,6 +54,7 @@ struct MaviSystem {
     int32_t ntiles_t = 0;
     int32_t* tile_queue = nullptr;
     unsigned tile_grid = 0;
+    int32_t lanes = 1;             // lanes per particle of the mixed short-range passes (1, 2, 4)
     double* noise_cur = nullptr;
     double* noise_queue = nullptr;
     int64_t noise_queue_cap = 0, noise_queue_len = 0, noise_queue_pos = 0;
@@ -206,6 +207,8 @@ void sources_mixed(MaviSystem* s);
 // check_invasions! for the listed replicas (mavi_invasions.cu); waits for the
 // device. from_sources: the step's k_sources left RingsInfo.cms.
 int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sources);
+// The mixed short-range passes with s->lanes lanes per particle (mavi_steps_lanes.cu).
+void lanes_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
 // waits for the stream and turns a device error flag into a status (mavi_api.cu)
 int device_error_status(MaviSystem* s);
 

@@ -221,12 +221,20 @@ class _Handle:
         self.check(self.lib.mavi_energies(self.handle, pe_mode, abi.as_dptr(ke), abi.as_dptr(pe)), "mavi_energies")
         return ke, pe
 
-    @property
-    def tiles_possible(self) -> bool:
-        """Whether the tiled Newton's-third-law modes serve this handle (mixed
-        Lennard-Jones / WCA with chunks in every replica)."""
-        return (self.device.precision == "mixed" and self.systems[0].dynamic_cfg.__class__.__name__ in
-                ("LenJonesCfg", "RunTumbleCfg") and all(s.int_cfg.chunks_cfg is not None for s in self.systems))
+    def pass_modes(self) -> list:
+        """The pass modes the autotuner chooses among for this handle: the three
+        per-particle gathers; the Newton's-third-law tiles for mixed
+        Lennard-Jones / WCA with chunks in every replica; 2 or 4 lanes per
+        particle for the mixed harmonic-truncated and Szabo passes."""
+        modes = ["staged", "global", "columns"]
+        kind = self.systems[0].dynamic_cfg.__class__.__name__
+        if self.device.precision == "mixed":
+            if kind in ("LenJonesCfg", "RunTumbleCfg") and all(
+                    getattr(s.int_cfg, "chunks_cfg", None) is not None for s in self.systems):
+                modes += ["tiles", "tiles_queue"]
+            if kind in ("HarmTruncCfg", "SzaboCfg"):
+                modes += ["lanes2", "lanes4"]
+        return modes
 
     def stats(self) -> abi.MaviStats:
         st = abi.MaviStats()
