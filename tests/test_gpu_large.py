@@ -193,3 +193,22 @@ def test_lj_4194304_energy_and_pair_distribution_mixed_follow_fp64(mg, wl):
     assert np.max(np.abs(emx - e64)) / scale < 1e-6
     assert abs(dmx - d64) < 1e-6
     assert np.all(np.abs(gmx - g64) <= 5 * noise + 1e-12)
+
+
+def test_lj_1024_fp64_trajectory_all_2000_steps(mg, orc, wl):
+    """The CPU-runnable configuration over its full length: 1,024 LJ particles
+    in a rigid box, velocity Verlet dt = 1e-3, 2,000 steps. The FP64 form
+    follows the oracle's trajectory (same arithmetic up to the summation order
+    of the pair terms) to 1e-8, and its chunk lists at the end are the
+    oracle's."""
+    s, step = wl.lj_1024(precision="fp64")
+    ref = orc.from_system(s, step_kind=step.kind)
+    mg.run_system(s, num_steps=2000, step_func=step)
+    ref.step(2000)
+    p, v, _ = ref.state()
+    assert np.max(np.abs(s.state.pos - p)) < 1e-8
+    assert np.max(np.abs(s.state.vel - v)) < 1e-8
+    ref.update_chunks()
+    assert chunks_equal(s.chunks(), ref.chunks())
+    ref.close()
+    s.close()

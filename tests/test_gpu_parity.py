@@ -566,3 +566,33 @@ def test_lanes_reject_other_laws(mg):
     with pytest.raises(mg.MaviError) as e:
         s.calc_forces()
     assert e.value.status == mg.abi.MAVI_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ragged_batch_with_tiny_replicas(mg, orc, precision):
+    """Replicas of 1, 2, 3 and 6 particles beside a 400-particle one, rigid and
+    periodic: chunk lists, forces and 50-step trajectories of every replica
+    against the oracle (a lone particle has zero pair force)."""
+    shapes = [(1, 1, "rigid"), (2, 1, "periodic"), (3, 1, "rigid"), (3, 2, "periodic"), (20, 20, "periodic")]
+    systems = [lj_grid(mg, nx, ny, wall=w, precision=precision, seed=k) for k, (nx, ny, w) in enumerate(shapes)]
+    b = mg.SystemBatch(systems)
+    forces = b.calc_forces()
+    refs = [orc.from_system(s) for s in systems]
+    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    for k, (s, ref) in enumerate(zip(systems, refs)):
+        assert chunks_equal_handle(b.handle.chunks(k), ref.chunks()), k
+        fr = ref.forces()
+        if k == 0:
+            assert np.all(forces[k] == 0) and np.all(fr == 0)
+        else:
+            assert rel_force_err(forces[k], fr) < tol, k
+    b.run(50)
+    for k, (s, ref) in enumerate(zip(systems, refs)):
+        ref.step(50)
+        assert np.max(np.abs(s.state.pos - ref.state()[0])) < (1e-9 if precision == "fp64" else 1e-6), k
+        ref.close()
+    b.close()
+
+
+def chunks_equal_handle(a, b):
+    return np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
