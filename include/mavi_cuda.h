@@ -310,6 +310,21 @@ int mavi_upload_state(MaviSystem* sys, const double* pos, const double* vel,
                       const double* pol);
 int mavi_download_state(MaviSystem* sys, double* pos, double* vel, double* pol);
 
+/* mavi_download_state without the wait: the copies into pos / vel / pol are
+ * queued on the handle's stream behind the steps and the call returns; the
+ * arrays hold the state once mavi_synchronize (or any call that waits) has
+ * returned, and must stay valid until then. From page-locked host memory the
+ * copies run while the host queues work on other handles, so independent
+ * replica groups on their own handles overlap one group's transfers with
+ * another's steps (the reference runs independent systems of an experiment
+ * batch side by side, one per thread, src/experiments.jl:271-280). No
+ * reference counterpart: a transfer-scheduling call. */
+int mavi_download_state_async(MaviSystem* sys, double* pos, double* vel, double* pol);
+
+/* Waits for everything queued on the handle's stream and returns the first
+ * device error of that work (as the waiting calls do), or MAVI_OK. */
+int mavi_synchronize(MaviSystem* sys);
+
 /* Noise for the next step in MAVI_NOISE_INJECTED mode: per replica, Szabo uses
  * one standard normal per particle (src/integration.jl:460), RTP two uniforms
  * per particle (src/integration.jl:493-495), rings one standard normal per ring

@@ -206,6 +206,8 @@ SIGNATURES = {
     "mavi_calc_forces": (C.c_int, [_vp, C.c_int32, _dp]),
     "mavi_upload_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mavi_download_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "mavi_download_state_async": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "mavi_synchronize": (C.c_int, [_vp]),
     "mavi_noise_count": (C.c_int64, [_vp]),
     "mavi_set_noise": (C.c_int, [_vp, _dp, C.c_int64]),
     "mavi_set_seed": (C.c_int, [_vp, C.c_uint64]),

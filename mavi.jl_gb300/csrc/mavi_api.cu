@@ -982,6 +982,17 @@ int mavi_upload_state(MaviSystem* s, const double* pos, const double* vel, const
 }
 
 int mavi_download_state(MaviSystem* s, double* pos, double* vel, double* pol) {
+    const int rc = mavi_download_state_async(s, pos, vel, pol);
+    if (rc) return rc;
+    return check_device_error(s);   // waits for the copies
+}
+
+int mavi_synchronize(MaviSystem* s) {
+    if (!s) return MAVI_ERR_INVALID_ARG;
+    return check_device_error(s);
+}
+
+int mavi_download_state_async(MaviSystem* s, double* pos, double* vel, double* pol) {
     if (!s) return MAVI_ERR_INVALID_ARG;
     k_scatter_user<<<nblocks(s->M), kBlock, 0, s->stream>>>(s->C, s->pos_user, s->has_vel ? s->vel_user : nullptr,
                                                             s->has_pol ? s->pol_user : nullptr);
@@ -993,7 +1004,7 @@ int mavi_download_state(MaviSystem* s, double* pos, double* vel, double* pol) {
         CUDA_TRY(s, cudaMemcpyAsync(pol, s->pol_user, sizeof(double) * s->Nslots, cudaMemcpyDeviceToHost, s->stream));
     if (pol && s->is_rings)
         CUDA_TRY(s, cudaMemcpyAsync(pol, s->C.ring_pol, sizeof(double) * s->total_rings, cudaMemcpyDeviceToHost, s->stream));
-    return check_device_error(s);   // waits for the copies
+    return MAVI_OK;
 }
 
 int64_t mavi_noise_count(MaviSystem* s) { return s ? s->noise_count : -1; }

@@ -411,6 +411,26 @@ function sync!(system)
     return system
 end
 
+"""
+Queue the copy of the GPU state into `system.state` and return
+(`mavi_download_state_async`); the arrays are complete after `wait!(system)`.
+Independent systems on their own handles overlap one system's copy with the
+others' steps.
+"""
+function download_async!(system)
+    h = handle!(system)
+    st = system.state
+    vel, pol = _vel_ptr(st), _pol_ptr(st)
+    check(ccall((:mavi_download_state_async, libmavi), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                h, pointer(st.pos), vel, pol), "mavi_download_state_async", h)
+end
+
+"Wait for the system's queued GPU work and copies (`mavi_synchronize`); throws on a device error."
+function wait!(system)
+    h = handle!(system)
+    check(ccall((:mavi_synchronize, libmavi), Cint, (Ptr{Cvoid},), h), "mavi_synchronize", h)
+end
+
 "Push `system.state` to the GPU (after the caller edited it on the host)."
 function upload!(system)
     h = handle!(system)

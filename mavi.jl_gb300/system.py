@@ -173,6 +173,18 @@ class _Handle:
             if pol is not None:
                 s.state.pol_array()[...] = pol[self.pol_offsets[k]:self.pol_offsets[k + 1]]
 
+    def download_async(self, pos, vel=None, pol=None):
+        """Queue the copy of the device state into the given arrays (user
+        order, the layout of mavi_create; page-locked memory for a copy that
+        overlaps other work) and return; the arrays hold the state after
+        synchronize()."""
+        self.check(self.lib.mavi_download_state_async(self.handle, abi.as_dptr(pos), abi.as_dptr(vel),
+                                                      abi.as_dptr(pol)), "mavi_download_state_async")
+
+    def synchronize(self):
+        """Wait for the handle's queued work; raises on a device error of it."""
+        self.check(self.lib.mavi_synchronize(self.handle), "mavi_synchronize")
+
     def upload(self):
         pos = np.ascontiguousarray(np.concatenate([s.state.pos.reshape(-1) for s in self.systems]))
         vel = pol = None

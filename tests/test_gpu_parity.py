@@ -596,3 +596,29 @@ def test_ragged_batch_with_tiny_replicas(mg, orc, precision):
 
 def chunks_equal_handle(a, b):
     return np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_async_download_then_synchronize(mg):
+    """mavi_download_state_async + mavi_synchronize give the arrays the
+    blocking download gives; a device error of the queued work (a NaN position
+    uploaded before the steps) is reported by mavi_synchronize."""
+    import torch
+    s = lj_grid(mg, 20, 20, wall="periodic")
+    h = s._ensure()
+    h.step(25)
+    h.download()
+    want_pos, want_vel = s.state.pos.copy(), s.state.vel.copy()
+    pos = torch.zeros(want_pos.shape, dtype=torch.float64).pin_memory().numpy()
+    vel = torch.zeros(want_vel.shape, dtype=torch.float64).pin_memory().numpy()
+    h.download_async(pos, vel)
+    h.synchronize()
+    assert np.array_equal(pos, want_pos) and np.array_equal(vel, want_vel)
+    bad = want_pos.copy()
+    bad[7] = (np.nan, 1.0)
+    h.check(h.lib.mavi_upload_state(h.handle, mg.abi.as_dptr(np.ascontiguousarray(bad)), None, None), "upload")
+    h.step(1)
+    h.download_async(pos, vel)
+    with pytest.raises(mg.MaviError) as e:
+        h.synchronize()
+    assert e.value.status == mg.abi.MAVI_ERR_NONFINITE
+    s.close()
