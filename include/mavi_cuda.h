@@ -358,7 +358,7 @@ int mavi_energy_series(MaviSystem* sys, int64_t num_samples, int64_t steps_betwe
  * d < r_max, dr = r_max / num_bins; d is the length of calc_diff (minimum
  * image where the reference applies it, src/integration.jl:38-52) computed
  * in FP64 without fused operations, so the counts are exact. The reference
- * has no g(r) routine; this is the statistic its long runs are judged by.
+ * has no g(r) routine; long runs of the two forms are compared by it.
  * r_max must not exceed any selected replica's chunk sides (replicas without
  * chunks: any r_max); 1 <= num_bins <= 4096. counts: num_bins uint64. */
 int mavi_pair_distribution(MaviSystem* sys, int32_t replica, double r_max, int32_t num_bins,

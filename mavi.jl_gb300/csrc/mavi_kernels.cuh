@@ -28,9 +28,12 @@
 
 namespace mavi {
 
+#ifndef MAVI_SCAN_ITEMS
+#define MAVI_SCAN_ITEMS 4
+#endif
 constexpr int kFixBits = 28;                       // fixed-point offsets: chunk = 2^28 units
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 4;                          // one int4 per thread
+constexpr int kScanItems = MAVI_SCAN_ITEMS;            // consecutive chunks per thread (int4 loads)
 constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
 constexpr int64_t kScanDirectTiles = 512;  // above this, tile offsets come from k_tile_offsets
 constexpr int kTileScanThreads = 1024;     // tiles per group of k_tile_offsets
@@ -393,30 +396,42 @@ static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int3
         for (int64_t t = threadIdx.x; t < (int64_t)blockIdx.x; t += blockDim.x) pre += tile_sum[t];
         block_exclusive_scan(pre, smem, tile_off);
     }
+    static_assert(kScanItems % 4 == 0, "int4 loads");
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
-    const bool full4 = base + kScanItems <= n;   // count is 16-byte aligned and base a multiple of 4
-    if (full4) {
-        int4 q = *reinterpret_cast<const int4*>(count + base);
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    const bool full = base + kScanItems <= n;   // count is 16-byte aligned and base a multiple of 4
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; q++) {
+            const int4 c = *reinterpret_cast<const int4*>(count + base + 4 * q);
+            v[4 * q] = c.x; v[4 * q + 1] = c.y; v[4 * q + 2] = c.z; v[4 * q + 3] = c.w;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; k++) v[k] = (base + k < n) ? count[base + k] : 0;
     }
-    int sum = v[0] + v[1] + v[2] + v[3];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) sum += v[k];
     int total;
-    int ex = block_exclusive_scan(sum, smem, total) + tile_off;
-    int4 o;
-    o.x = ex; o.y = ex + v[0]; o.z = o.y + v[1]; o.w = o.z + v[2];
-    if (full4) {
+    int run = block_exclusive_scan(sum, smem, total) + tile_off;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {   // v becomes the exclusive prefix
+        const int c = v[k];
+        v[k] = run;
+        run += c;
+    }
+    if (full) {
         // start has n + 1 entries and the same alignment as count
-        *reinterpret_cast<int4*>(start + base) = o;
-        if (clear) *reinterpret_cast<int4*>(count + base) = make_int4(0, 0, 0, 0);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; q++) {
+            *reinterpret_cast<int4*>(start + base + 4 * q) = make_int4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            if (clear) *reinterpret_cast<int4*>(count + base + 4 * q) = make_int4(0, 0, 0, 0);
+        }
     } else {
-        const int ov[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
         for (int k = 0; k < kScanItems; k++)
-            if (base + k < n) { start[base + k] = ov[k]; if (clear) count[base + k] = 0; }
+            if (base + k < n) { start[base + k] = v[k]; if (clear) count[base + k] = 0; }
     }
     if (threadIdx.x == 0) {
         if (blockIdx.x == gridDim.x - 1) start[n] = tile_off + total;
