@@ -52,7 +52,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 import __graft_entry__ as graft  # noqa: E402
 
-GATHER_NAMES = {0: "staged", 1: "global", 2: "columns", 3: "tiles", 4: "tiles_queue", 5: "lanes2", 6: "lanes4"}
+GATHER_NAMES = {0: "staged", 1: "global", 2: "columns", 3: "tiles", 4: "tiles_queue", 5: "lanes2", 6: "lanes4", 7: "split"}
 METRIC = "particle-steps/s on 1 GB300, mixed+batched vs plain FP64, at ≤1e-5 rel force err"
 UNIT = "particle-steps/s"
 

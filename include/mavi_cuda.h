@@ -217,6 +217,10 @@ typedef struct MaviOptions {
                                 5 = the column gather with 2 lanes per particle,
                                 6 = the same with 4 lanes (partial sums combined
                                     in a fixed order);
+                                mixed Lennard-Jones only:
+                                7 = the per-chunk gather with pairs at r >= 2
+                                    sigma in plain FP32 and closer ones in
+                                    double-float (a fixed order);
                                 -1 = autotuned at creation (fastest force pass) */
 } MaviOptions;
 
@@ -226,7 +230,7 @@ typedef struct MaviStats {
     int64_t total_particles;
     int64_t total_chunks;
     int32_t max_chunk_count;  /* largest chunk occupancy at the last rebuild        */
-    int32_t gather_mode;      /* pass mode in use (MaviOptions.gather_mode 0..6)     */
+    int32_t gather_mode;      /* pass mode in use (MaviOptions.gather_mode 0..7)     */
 } MaviStats;
 
 /* Per-kernel device time accumulated while profiling is on (milliseconds). */

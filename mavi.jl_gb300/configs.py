@@ -284,7 +284,9 @@ class CUDADevice:
     persistent CTAs), identical to each other; for the mixed
     harmonic-truncated and Szabo passes also "lanes2" / "lanes4" (the column
     gather with 2 or 4 lanes per particle, partial sums combined in a fixed
-    order); or "auto" (the fastest force pass at creation)."""
+    order); for the mixed Lennard-Jones passes also "split" (pairs at
+    r >= 2 sigma in plain FP32, closer ones in double-float); or "auto"
+    (the fastest force pass at creation)."""
     precision: str = "fp64"
     device: int = 0
     use_graph: bool = True
@@ -300,7 +302,7 @@ class CUDADevice:
         o.device = int(self.device)
         o.use_graph = 1 if self.use_graph else 0
         o.gather_mode = {"auto": -1, "staged": 0, "global": 1, "columns": 2, "tiles": 3, "tiles_queue": 4,
-                         "lanes2": 5, "lanes4": 6}[self.gather]
+                         "lanes2": 5, "lanes4": 6, "split": 7}[self.gather]
         return o
 
 

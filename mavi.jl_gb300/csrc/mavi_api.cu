@@ -363,6 +363,8 @@ static void set_fixed_point(const MaviReplicaParams& p, DevRep& R) {
         R.lj_al = (float)(ad - (double)R.lj_ah);
         R.lj_bh = (float)bd;
         R.lj_bl = (float)(bd - (double)R.lj_bh);
+        const double rn = kLjSplitSigmas * p.dyn.sigma / u;
+        R.lj_near2 = (float)(rn * rn);
     }
 }
 
@@ -474,7 +476,7 @@ static int ensure_graph(MaviSystem* s) {
 // each gather and keeps the fastest for the handle's lifetime; graphs are
 // captured afterwards and use it. The gathers add the same terms in the same
 // order, so the choice never changes results, only speed.
-// Pass mode `mode` (MaviOptions.gather_mode 0..6) on the handle: the device
+// Pass mode `mode` (MaviOptions.gather_mode 0..7) on the handle: the device
 // gather, and the lanes per particle of the mixed short-range passes.
 static void set_pass_mode(MaviSystem* s, int mode) {
     s->lanes = mode == kGatherLanes2 ? 2 : (mode == kGatherLanes4 ? 4 : 1);
@@ -486,6 +488,9 @@ static int pass_mode_of(const MaviSystem* s) {
 static bool lanes_possible(const MaviSystem* s) {
     return s->prec == MAVI_PREC_MIXED && (s->dyn == MAVI_DYN_HARM_TRUNC || s->dyn == MAVI_DYN_SZABO);
 }
+static bool split_possible(const MaviSystem* s) {
+    return s->prec == MAVI_PREC_MIXED && s->dyn == MAVI_DYN_LEN_JONES;
+}
 
 static int autotune_gather(MaviSystem* s) {
     cudaEvent_t a = nullptr, b = nullptr;
@@ -494,9 +499,11 @@ static int autotune_gather(MaviSystem* s) {
     float best = INFINITY;
     int best_mode = 0;
     for (int mode = 0; mode < kNumPassModes; mode++) {
-        // tiles: mixed Lennard-Jones / WCA with chunks; lanes: mixed short-range laws
+        // tiles: mixed Lennard-Jones / WCA with chunks; lanes: mixed short-range
+        // laws; split: mixed Lennard-Jones
         if ((mode == kGatherTiles || mode == kGatherTilesQueue) && !s->tiles) continue;
         if ((mode == kGatherLanes2 || mode == kGatherLanes4) && !lanes_possible(s)) continue;
+        if (mode == kGatherSplit && !split_possible(s)) continue;
         set_pass_mode(s, mode);
         for (int w = 0; w < 2; w++) {
             if (s->prec == MAVI_PREC_FP64) forces_only_fp64(s, 0);
@@ -512,7 +519,7 @@ static int autotune_gather(MaviSystem* s) {
         float ms = INFINITY;
         if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
         // modes 0..2 give the same bits; a mode that changes them (tiles,
-        // lanes) must beat the fastest of those by 10 %, so that timing noise
+        // lanes, split) must beat the fastest of those by 10 %, so that timing noise
         // cannot make two runs of the same system differ
         const float need = mode < kNumGatherModes ? best : best * 0.9f;
         if (ms < need) {
@@ -839,6 +846,8 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
     if (s->lanes > 1 && !lanes_possible(s))
         return bail(fail(s, MAVI_ERR_UNSUPPORTED,
                          "gather modes 5 and 6 (lanes) serve the mixed harmonic-truncated and Szabo passes"));
+    if (opt->gather_mode == kGatherSplit && !split_possible(s))
+        return bail(fail(s, MAVI_ERR_UNSUPPORTED, "gather mode 7 (split) serves the mixed Lennard-Jones passes"));
     C.num_reps = s->R;
     C.seed = opt->seed;
 

@@ -102,7 +102,7 @@ struct DevRep {
     // lj_sk = 2^-k to O(1); (ah + al) = 48 eps sigma^12 u g^-7 and
     // (bh + bl) = 24 eps sigma^6 u g^-4 with g = 2^k u^2
     float lj_sk, lj_ah, lj_al, lj_bh, lj_bl;
-    int32_t _pad2;
+    float lj_near2;        // split gather: pairs closer than 2 sigma (units^2) take the double-float term
     // rings, per type: target area A0^2 = (n l / p0)^2 and float copies of the
     // ring-internal constants (mixed form)
     double ring_a0sq[MAVI_MAX_TYPES];

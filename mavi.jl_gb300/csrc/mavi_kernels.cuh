@@ -38,6 +38,12 @@ constexpr int kScanTile = kScanThreads * kScanItems;   // chunks per scan tile
 constexpr int64_t kScanDirectTiles = 512;  // above this, tile offsets come from k_tile_offsets
 constexpr int kTileScanThreads = 1024;     // tiles per group of k_tile_offsets
 constexpr int32_t kFixClamp = (1 << 30) - 1;       // |offset| clamp: 4 chunks
+constexpr int kPassThreads = 128;                   // threads per block of the pair passes
+constexpr int kPassWarps = kPassThreads / 32;
+#ifndef MAVI_LJ_SPLIT_SIGMAS
+#define MAVI_LJ_SPLIT_SIGMAS 2.0
+#endif
+constexpr double kLjSplitSigmas = MAVI_LJ_SPLIT_SIGMAS;   // split gather: double-float below this distance (sigmas)
 // |offset| allowed in a pair term: two offsets of at most 1.5 chunks and the
 // one-chunk stencil shift keep every difference within 4 chunks < 2^31 units
 constexpr int32_t kFixRange = 3 << (kFixBits - 1);
@@ -657,6 +663,14 @@ __device__ __forceinline__ bool inside_cutoff(const FixPair& fp, int32_t dxi, in
 //   f/d = (ah + al) (h+l)^-7 - (bh + bl) (h+l)^-4 = t^4 (A t^3 - B) (1 + O(e))
 // _rn intrinsics keep the compiler from fusing the products the error terms
 // are taken of.
+// Hardware reciprocal approximation (about 1 ulp); inputs here are normal
+// numbers (scaled squared distances of distinct particles).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ void lj_pair_df(const DevRep& R, int32_t dxi, int32_t dyi, float& fxh, float& fxl,
                                            float& fyh, float& fyl) {
     const float xh = (float)dxi, yh = (float)dyi;
@@ -668,7 +682,9 @@ __device__ __forceinline__ void lj_pair_df(const DevRep& R, int32_t dxi, int32_t
     const float E = __fadd_rn(__fsub_rn(p1, __fsub_rn(S, sv)), __fsub_rn(p2, sv)) + e1 + e2 +
                     2.0f * fmaf(xh, xl, yh * yl);
     const float h = __fmul_rn(S, R.lj_sk), l = E * R.lj_sk;   // power-of-two scaling: exact
-    const float t = __frcp_rn(h);
+    // t ~ 1/h to ~1 ulp; e = 1 - (h + l) t is formed exactly enough (the FMA
+    // residual) that the first-order correction below absorbs t's error
+    const float t = rcp_approx(h);
     const float e = fmaf(-h, t, 1.0f) - l * t;
     const float t2 = __fmul_rn(t, t), t2e = fmaf(t, t, -t2);
     const float t3 = __fmul_rn(t2, t), t3e = fmaf(t2, t, -t3) + t2e * t;
@@ -1105,15 +1121,134 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
 // table. Windows that do not fit fall back to the global gather (same terms
 // in the same order, bitwise-identical sums).
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Split gather of the mixed Lennard-Jones pass (pass mode 7), over the same
+// chunk loops as gather_global. A candidate at r >= 2 sigma (R.lj_near2,
+// units^2) is evaluated on the spot in plain FP32: its force is below
+// ~0.2 eps / sigma, so the ~10 ulp of that form stay far under the
+// double-float error of the close pairs (the first two neighbour shells). A closer candidate's exact integer
+// displacement is parked in the thread's slots of shared memory (`slots`,
+// stride kPassThreads, kSplitSlots of them) and evaluated in double-float afterwards, so the
+// costly term runs ~7-9 times per particle instead of ~33, with no divergence
+// between the two forms inside a warp, and the candidate loop carries no
+// double-float registers. Order: the close terms in candidate order into the
+// compensated sum, then the raw wrapped pairs of periodic spaces without
+// minimum image (their chunks are set aside in the first loop), then the FP32
+// sum of the far ones: fixed, so deterministic. Both particles of a pair see
+// the same displacement (negated), hence the same classification and opposite
+// forces. A particle with more close candidates than slots takes gather_global
+// instead (every term in double-float).
+// ---------------------------------------------------------------------------
+#ifndef MAVI_SPLIT_SLOTS
+#define MAVI_SPLIT_SLOTS 14
+#endif
+#ifndef MAVI_SPLIT_UNROLL
+#define MAVI_SPLIT_UNROLL 1
+#endif
+constexpr int kSplitSlots = MAVI_SPLIT_SLOTS;   // close candidates parked per particle (8 B each per thread)
+constexpr int kSplitUnroll = MAVI_SPLIT_UNROLL;
+
+template <int DYN>
+__device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
+                                             const int2* __restrict__ P, const Me<kPrecMixed, DYN>& me,
+                                             Acc<kPrecMixed, DYN>& acc, int2* __restrict__ slots) {
+    float fx = 0.f, fy = 0.f;
+    int n_near = 0;
+    const float near2 = R.lj_near2, sk = R.lj_sk, ah = R.lj_ah, bh = R.lj_bh;
+    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
+#pragma unroll kSplitUnroll
+        for (int32_t j = b; j < e; j++) {
+            if (j == (int32_t)s) continue;
+            const int2 oj = P[j];
+            int32_t dxi = (int32_t)((uint32_t)me.p.x - (uint32_t)oj.x + (uint32_t)shx);
+            int32_t dyi = (int32_t)((uint32_t)me.p.y - (uint32_t)oj.y + (uint32_t)shy);
+            if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
+                if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
+                if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
+            }
+            const float xf = (float)dxi, yf = (float)dyi;
+            const float S = fmaf(xf, xf, yf * yf);
+            if (S < near2) {
+                if (n_near < kSplitSlots) slots[n_near * kPassThreads] = make_int2(dxi, dyi);
+                n_near++;
+            } else {
+                // (48 eps sigma^12 / r^14 - 24 eps sigma^6 / r^8) d in the scaled units
+                const float ti = rcp_approx(S * sk);
+                const float t2 = ti * ti;
+                const float sh = fmaf(ah, t2 * ti, -bh) * (t2 * t2);
+                fx = fmaf(sh, xf, fx);
+                fy = fmaf(sh, yf, fy);
+            }
+        }
+    };
+    int32_t col = 0, row = 0;
+    uint32_t raw_chunks = 0;   // bit 3 (dc + 1) + (dr + 1): a wrapped chunk without minimum image
+    if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224): its one chunk
+        visit(C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
+    } else {
+        const int32_t lc = (int32_t)(cell - R.c0);
+        col = lc / R.rows;
+        row = lc - col * R.rows;
+#pragma unroll 1
+        for (int dc = -1; dc <= 1; dc++) {
+            int ncol = col + dc;
+            bool wrapped = false;
+            if (R.periodic) {
+                if (ncol < 0) { ncol += R.cols; wrapped = true; }
+                else if (ncol >= R.cols) { ncol -= R.cols; wrapped = true; }
+            } else if (ncol < 0 || ncol >= R.cols) continue;
+#pragma unroll 1
+            for (int dr = -1; dr <= 1; dr++) {
+                int nrow = row + dr;
+                bool wr = wrapped;
+                if (R.periodic) {
+                    if (nrow < 0) { nrow += R.rows; wr = true; }
+                    else if (nrow >= R.rows) { nrow -= R.rows; wr = true; }
+                } else if (nrow < 0 || nrow >= R.rows) continue;
+                if (wr && !R.min_image) {
+                    raw_chunks |= 1u << (3 * (dc + 1) + (dr + 1));
+                    continue;
+                }
+                const int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
+                visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small));
+            }
+        }
+    }
+    if (n_near > kSplitSlots) {   // rare: more close candidates than slots
+        gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
+        return;
+    }
+#pragma unroll 2
+    for (int k = 0; k < n_near; k++) {
+        const int2 d = slots[k * kPassThreads];
+        float fxh, fxl, fyh, fyl;
+        lj_pair_df(R, d.x, d.y, fxh, fxl, fyh, fyl);
+        acc.add2(fxh, fxl, fyh, fyl);
+    }
+#pragma unroll 1
+    while (raw_chunks) {   // periodic spaces without minimum image: the raw difference (src/integration.jl:38-52)
+        const int bit = __ffs(raw_chunks) - 1;
+        raw_chunks &= raw_chunks - 1;
+        const int dc = bit / 3 - 1, dr = bit % 3 - 1;
+        int ncol = col + dc, nrow = row + dr;
+        ncol += ncol < 0 ? R.cols : (ncol >= R.cols ? -R.cols : 0);
+        nrow += nrow < 0 ? R.rows : (nrow >= R.rows ? -R.rows : 0);
+        const int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
+        const long long rshx = -(long long)(ncol - col) * R.sx_u, rshy = (long long)(nrow - row) * R.sy_u;
+        for (int32_t j = C.start[nc]; j < C.start[nc + 1]; j++)
+            if (j != (int32_t)s) pair_term_raw<DYN>(C, R, rep, me, P[j], 0, rshx, rshy, acc);
+    }
+    acc.add(fx, fy);
+}
+
 constexpr int kNumGatherModes = 3; // staged window, per-chunk global, per-column global
 constexpr int kGatherTiles = 3;      // Lennard-Jones / WCA, mixed form: Newton's-third-law tiles, a CTA per tile
 constexpr int kGatherTilesQueue = 4; // the same tiles from a device work queue (persistent CTAs)
 constexpr int kGatherLanes2 = 5;      // mixed short-range laws: column gather, 2 lanes per particle
 constexpr int kGatherLanes4 = 6;      // the same, 4 lanes per particle
-constexpr int kNumPassModes = 7;
+constexpr int kGatherSplit = 7;       // mixed Lennard-Jones: far pairs in FP32, close ones in double-float
+constexpr int kNumPassModes = 8;
 constexpr int kStageParts = 256;   // staged particles per window
-constexpr int kPassThreads = 128;
-constexpr int kPassWarps = kPassThreads / 32;
 
 constexpr int kStageRows = 64;     // window rows per column
 
@@ -1694,6 +1829,37 @@ k_pass(Ctx C, int32_t with_wall_forces) {
     }
     if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
         count_into_chunk(C, valid, s, new_cell, cap);
+}
+
+// The mixed Lennard-Jones pass with the split gather (pass mode 7): k_pass
+// with gather_split in place of the warp gathers, in a kernel of its own so
+// that its registers serve this gather alone.
+#ifndef MAVI_PASS_BLOCKS_SPLIT
+#define MAVI_PASS_BLOCKS_SPLIT 10   // measured faster than 8 or 12 (start and melted states)
+#endif
+template <int PASS, bool HAS_VEL, bool HAS_POL>
+__global__ void __launch_bounds__(kPassThreads, MAVI_PASS_BLOCKS_SPLIT) k_pass_split(Ctx C, int32_t with_wall_forces) {
+    constexpr int DYN = MAVI_DYN_LEN_JONES;
+    __shared__ int2 slots[kSplitSlots * kPassThreads];
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = s < C.M;
+    const int32_t rep = (valid && C.num_reps > 1) ? C.rep_cur[s] : 0;
+    const DevRep& R = C.reps[rep];
+    const int32_t cell = valid ? C.cell_cur[s] : 0;
+    const int2* P = (PASS == kPassVerlet2) ? C.off_mid : C.off_cur;
+    const double2* Pd = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    const double2 p = valid ? Pd[s] : make_double2(0.0, 0.0);
+    int64_t new_cell = 0;
+    int32_t cap = 1 << 30;
+    if (valid) {
+        Acc<kPrecMixed, DYN> acc;
+        const Me<kPrecMixed, DYN> me = make_me<kPrecMixed, DYN>(C, R, rep, s, P);
+        gather_split<DYN>(C, R, rep, s, cell, P, me, acc, slots + threadIdx.x);
+        const float gx = acc.gx(), gy = acc.gy();
+        new_cell = pass_epilogue<kPrecMixed, DYN, PASS, HAS_VEL, HAS_POL>(
+            C, s, rep, R, cell, p, f32_to_f64_bits(gx), f32_to_f64_bits(gy), gx, gy, 0, with_wall_forces, cap);
+    }
+    if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped) count_into_chunk(C, valid, s, new_cell, cap);
 }
 
 // ===========================================================================

@@ -41,8 +41,14 @@ void tpass(MaviSystem* s, int with_walls) {
 template <int PREC, int DYN, int PASS>
 void pass(MaviSystem* s, int with_walls) {
     if constexpr (PREC == kPrecMixed && kTiledPass<DYN, PASS>) {
-        if (s->tiles && s->C.gather_mode >= kGatherTiles) {
+        if (s->tiles && (s->C.gather_mode == kGatherTiles || s->C.gather_mode == kGatherTilesQueue)) {
             tpass<DYN, PASS>(s, with_walls);
+            return;
+        }
+    }
+    if constexpr (PREC == kPrecMixed && DYN == MAVI_DYN_LEN_JONES) {
+        if (s->C.gather_mode == kGatherSplit) {
+            split_pass_mixed(s, PASS, with_walls);
             return;
         }
     }

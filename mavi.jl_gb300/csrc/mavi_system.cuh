@@ -209,6 +209,8 @@ void sources_mixed(MaviSystem* s);
 int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sources);
 // The mixed short-range passes with s->lanes lanes per particle (mavi_steps_lanes.cu).
 void lanes_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
+// The mixed Lennard-Jones passes with the split gather (mavi_steps_split.cu).
+void split_pass_mixed(MaviSystem* s, int pass, int with_walls);
 // waits for the stream and turns a device error flag into a status (mavi_api.cu)
 int device_error_status(MaviSystem* s);
 

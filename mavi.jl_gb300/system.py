@@ -237,7 +237,8 @@ class _Handle:
         """The pass modes the autotuner chooses among for this handle: the three
         per-particle gathers; the Newton's-third-law tiles for mixed
         Lennard-Jones / WCA with chunks in every replica; 2 or 4 lanes per
-        particle for the mixed harmonic-truncated and Szabo passes."""
+        particle for the mixed harmonic-truncated and Szabo passes; the split
+        gather (far pairs in FP32) for mixed Lennard-Jones."""
         modes = ["staged", "global", "columns"]
         kind = self.systems[0].dynamic_cfg.__class__.__name__
         if self.device.precision == "mixed":
@@ -246,6 +247,8 @@ class _Handle:
                 modes += ["tiles", "tiles_queue"]
             if kind in ("HarmTruncCfg", "SzaboCfg"):
                 modes += ["lanes2", "lanes4"]
+            if kind == "LenJonesCfg":
+                modes += ["split"]
         return modes
 
     def stats(self) -> abi.MaviStats:
