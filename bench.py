@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="lj_batch_512")
+    ap.add_argument("--gather", default="auto",
+                    help="pair gather of the mixed form (auto: the autotuner's choice; a fixed one for profiling "
+                         "runs, where serialised launches make the autotuner's timings meaningless)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--accuracy-steps", type=int, default=500,
@@ -508,6 +511,9 @@ def cpu_baseline(mg, orc, runner, seconds, nthreads):
 BATCHED = {"lj_batch_512": 512, "rings_64": 64}
 
 
+MIXED_GATHER = "auto"   # --gather: the mixed form's pair gather
+
+
 def workload_share(name, precision, rank=0, world=1):
     """The systems this rank advances (host side, no device handle yet).
     Batched workloads under torchrun: R x world replicas from the same seeded
@@ -518,8 +524,13 @@ def workload_share(name, precision, rank=0, world=1):
     if name in BATCHED and world > 1:
         obj, step = W[name](precision=precision, num_replicas=BATCHED[name] * world)
         mine = replicas.my_replicas([s.num_slots for s in obj], rank, world)
-        return [obj[i] for i in mine], step
-    return W[name](precision=precision)
+        obj = [obj[i] for i in mine]
+    else:
+        obj, step = W[name](precision=precision)
+    if precision == "mixed" and MIXED_GATHER != "auto":
+        for s in (obj if isinstance(obj, (list, tuple)) else [obj]):
+            s.int_cfg.device.gather = MIXED_GATHER
+    return obj, step
 
 
 def build_workload(mg, name, precision, rank=0, world=1):
@@ -607,7 +618,9 @@ def run_reference(args):
 
 
 def main():
+    global MIXED_GATHER
     args = parse()
+    MIXED_GATHER = args.gather
     if args.impl == "reference":
         return run_reference(args)
     rank, world, local = dist_info()
