@@ -1155,31 +1155,32 @@ __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int3
     float fx = 0.f, fy = 0.f;
     int n_near = 0;
     const float near2 = R.lj_near2, sk = R.lj_sk, ah = R.lj_ah, bh = R.lj_bh;
+    // one candidate: the FP32 term on the spot, or the displacement parked
+    auto term = [&](int32_t j, int2 oj, int32_t shx, int32_t shy, bool mi) {
+        if (j == (int32_t)s) return;
+        int32_t dxi = (int32_t)((uint32_t)me.p.x - (uint32_t)oj.x + (uint32_t)shx);
+        int32_t dyi = (int32_t)((uint32_t)me.p.y - (uint32_t)oj.y + (uint32_t)shy);
+        if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
+            if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
+            if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
+        }
+        const float xf = (float)dxi, yf = (float)dyi;
+        const float S = fmaf(xf, xf, yf * yf);
+        if (S < near2) {
+            if (n_near < kSplitSlots) slots[n_near * kPassThreads] = make_int2(dxi, dyi);
+            n_near++;
+        } else {
+            // (48 eps sigma^12 / r^14 - 24 eps sigma^6 / r^8) d in the scaled units
+            const float ti = rcp_approx(S * sk);
+            const float t2 = ti * ti;
+            const float sh = fmaf(ah, t2 * ti, -bh) * (t2 * t2);
+            fx = fmaf(sh, xf, fx);
+            fy = fmaf(sh, yf, fy);
+        }
+    };
     auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
 #pragma unroll kSplitUnroll
-        for (int32_t j = b; j < e; j++) {
-            if (j == (int32_t)s) continue;
-            const int2 oj = P[j];
-            int32_t dxi = (int32_t)((uint32_t)me.p.x - (uint32_t)oj.x + (uint32_t)shx);
-            int32_t dyi = (int32_t)((uint32_t)me.p.y - (uint32_t)oj.y + (uint32_t)shy);
-            if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
-                if (abs(dxi) > R.half_bx_i) dxi -= dxi > 0 ? R.bx_i : -R.bx_i;
-                if (abs(dyi) > R.half_by_i) dyi -= dyi > 0 ? R.by_i : -R.by_i;
-            }
-            const float xf = (float)dxi, yf = (float)dyi;
-            const float S = fmaf(xf, xf, yf * yf);
-            if (S < near2) {
-                if (n_near < kSplitSlots) slots[n_near * kPassThreads] = make_int2(dxi, dyi);
-                n_near++;
-            } else {
-                // (48 eps sigma^12 / r^14 - 24 eps sigma^6 / r^8) d in the scaled units
-                const float ti = rcp_approx(S * sk);
-                const float t2 = ti * ti;
-                const float sh = fmaf(ah, t2 * ti, -bh) * (t2 * t2);
-                fx = fmaf(sh, xf, fx);
-                fy = fmaf(sh, yf, fy);
-            }
-        }
+        for (int32_t j = b; j < e; j++) term(j, P[j], shx, shy, mi);
     };
     int32_t col = 0, row = 0;
     uint32_t raw_chunks = 0;   // bit 3 (dc + 1) + (dr + 1): a wrapped chunk without minimum image
