@@ -343,11 +343,14 @@ def e2e_pipelined(mg, name, rank, world, K, torch, groups=8):
     """End to end through the C ABI for a batched workload, the way a host runs
     independent replica groups side by side: the batch as `groups` handles of
     consecutive replicas (about equal particle counts), each on its own
-    stream; every step each group uploads its state from page-locked memory,
-    steps once and queues its download (mavi_download_state_async), then every
-    group is awaited (mavi_synchronize). One group's copies overlap another
-    group's steps, and uploads overlap downloads (the host link moves both
-    directions at once)."""
+    stream. Every step, group by group: wait for the group's previous
+    download (mavi_synchronize: the host then holds that step's result),
+    upload its state from page-locked memory, step once and queue its
+    download (mavi_download_state_async). A group waits only for its own
+    previous step, so one group's copies overlap the other groups' steps
+    across step boundaries too, and uploads overlap downloads (the host link
+    moves both directions at once); after the last step every group is
+    awaited inside the timed region."""
     systems, step = workload_share(name, "mixed", rank, world)
     cum = np.cumsum([s.num_slots for s in systems])
     cuts = [0] + [int(np.searchsorted(cum, cum[-1] * g / groups)) + 1 for g in range(1, groups)] + [len(systems)]
@@ -370,17 +373,22 @@ def e2e_pipelined(mg, name, rank, world, K, torch, groups=8):
     def one_step():
         for r, ((_, pp), (_, vp), (_, qp)) in zip(runs, sets):
             h = r.handle
+            h.synchronize()   # this group's previous step is back on the host
             h.check(h.lib.mavi_upload_state(h.handle, pp, vp, qp), "upload")
             h.check(h.lib.mavi_step(h.handle, 1), "step")
             h.check(h.lib.mavi_download_state_async(h.handle, pp, vp, qp), "download")
+
+    def wait_all():
         for r in runs:
             r.handle.synchronize()
 
     for _ in range(3):
         one_step()
+    wait_all()
     t0 = time.perf_counter()
     for _ in range(K):
         one_step()
+    wait_all()
     dt = time.perf_counter() - t0
     n = sum(r.num_slots for r in runs)
     for r in runs:
@@ -728,9 +736,9 @@ def main():
                 {"value": world * e2e_pipe["value"], "unit": UNIT,
                  "h2d_bytes_per_step": e2e_pipe["h2d"], "d2h_bytes_per_step": e2e_pipe["d2h"],
                  "path": f"the batch as {e2e_pipe['groups']} handles of consecutive replicas on their own streams; "
-                         "every step each uploads its state (mavi_upload_state), steps once (mavi_step) and queues "
-                         "its download (mavi_download_state_async), then each is awaited (mavi_synchronize); "
-                         "pinned host buffers",
+                         "every step, group by group: wait for the group's previous download (mavi_synchronize), "
+                         "upload its state (mavi_upload_state), step once (mavi_step), queue its download "
+                         "(mavi_download_state_async); every group awaited after the last step; pinned host buffers",
                  "single_handle": {"value": world * n * min(K, 300) / e2e["seconds"],
                                    "path": "one handle: mavi_upload_state -> mavi_step(1) -> mavi_download_state"}}
                 if e2e_pipe else
