@@ -17,7 +17,7 @@ PKG = pathlib.Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB = PKG / "lib"
 OBJ = PKG / "_build"
-SOURCES = ["mavi_api.cu", "mavi_steps_fp64.cu", "mavi_steps_mixed.cu", "mavi_steps_lanes.cu", "mavi_steps_split.cu", "mavi_peak.cu",
+SOURCES = ["mavi_api.cu", "mavi_steps_fp64.cu", "mavi_steps_mixed.cu", "mavi_steps_lanes.cu", "mavi_steps_split.cu", "mavi_steps_cols.cu", "mavi_peak.cu",
            "mavi_noalloc.cu", "mavi_invasions.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

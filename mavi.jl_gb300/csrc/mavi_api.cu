@@ -891,6 +891,12 @@ int mavi_create(const MaviOptions* opt, int32_t num_replicas, const MaviReplicaP
         for (int k = 0; k < MAVI_MAX_SPACES; k++) spaces_h[(size_t)r * MAVI_MAX_SPACES + k] = replicas[r].spaces[k];
         rcfg_h[r] = replicas[r].rings;
     }
+    // the ring kernel specialised to the exact integer path of the mixed form
+    s->rings_small = s->is_rings && s->prec == MAVI_PREC_MIXED;
+    for (int r = 0; r < s->R && s->rings_small; r++) {
+        s->rings_small = !s->reps_h[r].min_image;
+        for (int t = 0; t < rcfg_h[r].num_types; t++) s->rings_small = s->rings_small && rcfg_h[r].num_particles[t] <= 32;
+    }
     // identity user order over active slots
     std::vector<int32_t> uid_h(M), rep_h(M);
     std::vector<int32_t> types_all, ring_rep_h;

@@ -1832,6 +1832,53 @@ k_pass(Ctx C, int32_t with_wall_forces) {
         count_into_chunk(C, valid, s, new_cell, cap);
 }
 
+// The mixed short-range passes with the column gather (pass mode 2): k_pass
+// with gather_columns called directly in place of the warp gathers (the same
+// terms in the same order, so the same bits), in a kernel of its own so that
+// its registers serve this gather alone (the warp-staged gather's registers
+// made k_pass spill in the column gather's loop).
+template <int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
+__global__ void __launch_bounds__(kPassThreads, DYN == MAVI_DYN_RINGS ? MAVI_PASS_BLOCKS_RINGS : MAVI_PASS_BLOCKS_MIXED)
+k_pass_cols(Ctx C, int32_t with_wall_forces) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = s < C.M;
+    const int32_t rep = (valid && C.num_reps > 1) ? C.rep_cur[s] : 0;
+    const DevRep& R = C.reps[rep];
+    const int32_t cell = valid ? C.cell_cur[s] : 0;
+    if constexpr (DYN == MAVI_DYN_RINGS) {
+        // particles of inactive rings (parked after every real chunk): zero
+        // force (clean_forces!), no neighbours, no pair terms
+        if (valid && C.var_rings && cell == C.park) {
+            const int32_t u = C.uid_cur[s];
+            C.ff_u[u] = make_float2(0.f, 0.f);
+            if (C.nb_mode) C.nb_count[u] = 0;
+            valid = false;
+        }
+    }
+    const int2* P = (PASS == kPassVerlet2) ? C.off_mid : C.off_cur;
+    const double2* Pd = (PASS == kPassVerlet2) ? C.pos_mid : C.pos_cur;
+    const double2 p = valid ? Pd[s] : make_double2(0.0, 0.0);
+    int64_t new_cell = 0;
+    int32_t cap = 1 << 30;
+    if (valid) {
+        Acc<kPrecMixed, DYN> acc;
+        const Me<kPrecMixed, DYN> me = make_me<kPrecMixed, DYN>(C, R, rep, s, P);
+        if (R.has_chunks) gather_columns<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
+        else gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
+        const float gx = acc.gx(), gy = acc.gy();
+        new_cell = pass_epilogue<kPrecMixed, DYN, PASS, HAS_VEL, HAS_POL>(
+            C, s, rep, R, cell, p, f32_to_f64_bits(gx), f32_to_f64_bits(gy), gx, gy, acc.nb, with_wall_forces, cap);
+    }
+    if constexpr (PASS == kPassVerlet2 || PASS == kPassOverdamped || PASS == kPassSzabo || PASS == kPassRTP)
+        count_into_chunk(C, valid, s, new_cell, cap);
+}
+
+template <int DYN, int PASS>
+constexpr bool kColsPass = (DYN == MAVI_DYN_HARM_TRUNC && (PASS == kPassForce || PASS == kPassOverdamped ||
+                                                          PASS == kPassVerlet1 || PASS == kPassVerlet2)) ||
+                           (DYN == MAVI_DYN_SZABO && (PASS == kPassForce || PASS == kPassSzabo)) ||
+                           (DYN == MAVI_DYN_RINGS && PASS == kPassForce);
+
 // The mixed Lennard-Jones pass with the split gather (pass mode 7): k_pass
 // with gather_split in place of the warp gathers, in a kernel of its own so
 // that its registers serve this gather alone.
@@ -2209,12 +2256,19 @@ __device__ __forceinline__ void ring_vc_store(const Ctx& C, int64_t g, int lane,
 #ifndef MAVI_RINGS_MIN_BLOCKS
 #define MAVI_RINGS_MIN_BLOCKS 8    // ring-kernel blocks per SM (64 registers; measured faster than 4, 5 or 6)
 #endif
-template <int PREC>
-__global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_rings(Ctx C, int64_t total_rings,
-                                                                                 int32_t do_update,
-                                                                                 int32_t with_walls) {
-    __shared__ double2 sp_[kRingWarps][kRingMax];
-    __shared__ int32_t ss_[kRingWarps][kRingMax];
+#ifndef MAVI_RINGS_SMALL_BLOCKS
+#define MAVI_RINGS_SMALL_BLOCKS 10 // the same for k_rings<mixed, SMALL> (48 registers; faster than 8, level with 12)
+#endif
+// SMALL (mixed form): every ring of the handle has at most 32 particles and
+// no replica takes the minimum image, so every ring takes the exact integer
+// path below; the general path is compiled out and its registers with it.
+template <int PREC, bool SMALL = false>
+__global__ void __launch_bounds__(32 * kRingWarps, SMALL ? MAVI_RINGS_SMALL_BLOCKS : MAVI_RINGS_MIN_BLOCKS)
+k_rings(Ctx C, int64_t total_rings, int32_t do_update, int32_t with_walls) {
+    static_assert(!SMALL || PREC == kPrecMixed, "the exact integer ring path is the mixed form's");
+    constexpr int kRingSlots = SMALL ? 32 : kRingMax;
+    __shared__ double2 sp_[kRingWarps][kRingSlots];
+    __shared__ int32_t ss_[kRingWarps][kRingSlots];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t g = (int64_t)blockIdx.x * kRingWarps + w;
     if (g >= total_rings) return;   // whole warp exits together
@@ -2314,7 +2368,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, MAVI_RINGS_MIN_BLOCKS) k_ring
         return nc;
     };
     if constexpr (PREC == kPrecMixed) {
-        if (n <= 32 && !R.min_image) {
+        if (SMALL || (n <= 32 && !R.min_image)) {
             // Mixed form, rings of <= 32 particles without minimum image: the
             // ring geometry comes from the exact integer chunk offsets. Each
             // lane's absolute position in units from the centre of chunk

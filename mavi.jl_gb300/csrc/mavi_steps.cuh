@@ -52,6 +52,12 @@ void pass(MaviSystem* s, int with_walls) {
             return;
         }
     }
+    if constexpr (PREC == kPrecMixed && kColsPass<DYN, PASS>) {
+        if (s->C.gather_mode == 2 && s->lanes == 1) {
+            cols_pass_mixed(s, DYN, PASS, with_walls);
+            return;
+        }
+    }
     if constexpr (PREC == kPrecMixed && kLanesPass<DYN, PASS>) {
         if (s->lanes > 1) {
             lanes_pass_mixed(s, DYN, PASS, with_walls);
@@ -70,7 +76,12 @@ void rings_terms(MaviSystem* s, int do_update, int with_walls) {
     unsigned g = (unsigned)((s->total_rings + kRingWarps - 1) / kRingWarps);
     // FP64 form: ring areas in the reference's operation order first
     if constexpr (PREC == kPrecFP64) k_ring_area_ref<<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings);
-    k_rings<PREC><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
+    if constexpr (PREC == kPrecMixed) {
+        if (s->rings_small) k_rings<PREC, true><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
+        else k_rings<PREC, false><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
+    } else {
+        k_rings<PREC, false><<<g, 32 * kRingWarps, 0, s->stream>>>(s->C, s->total_rings, do_update, with_walls);
+    }
     if (do_update) k_ring_pol<PREC><<<nblocks(s->total_rings), kBlock, 0, s->stream>>>(s->C, s->total_rings, 1);
 }
 

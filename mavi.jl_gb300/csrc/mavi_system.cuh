@@ -35,6 +35,7 @@ struct MaviSystem {
     std::vector<int64_t> rep_active;   // active particles per replica
     int32_t dyn = 0, step_kind = 0, state_kind = 0, prec = 0;
     bool has_vel = false, has_pol = false, is_rings = false;
+    bool rings_small = false;   // mixed rings, every ring <= 32 particles, no minimum image: k_rings<mixed, true>
     int64_t M = 0, Nslots = 0, Ctot = 0, total_rings = 0, noise_count = 0, ntiles = 0;
     std::vector<int64_t> num_steps;
     std::vector<double> time;
@@ -211,6 +212,8 @@ int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sour
 void lanes_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
 // The mixed Lennard-Jones passes with the split gather (mavi_steps_split.cu).
 void split_pass_mixed(MaviSystem* s, int pass, int with_walls);
+// The mixed short-range passes with the column gather (mavi_steps_cols.cu).
+void cols_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
 // waits for the stream and turns a device error flag into a status (mavi_api.cu)
 int device_error_status(MaviSystem* s);
 
