@@ -822,6 +822,24 @@ __device__ __forceinline__ void nb_record(const Ctx& C, int32_t me_uid, int32_t 
 // offset (mixed), uq its user id (rings), (shx, shy) the stencil shift in
 // fixed-point units, mi whether the minimum image applies. The global and the
 // staged gathers both call this, in the same order, so they agree bitwise.
+// Rings pair law on an exact integer displacement (mixed form): bonded
+// neighbours of the same ring excluded, no attraction inside a ring
+// (src/rings/integration.jl:32-70).
+template <int DYN>
+__device__ __forceinline__ void rings_pair_dxy(const DevRep& R, const Me<kPrecMixed, DYN>& me, const RingInfo& o,
+                                               int32_t dxi, int32_t dyi, Acc<kPrecMixed, DYN>& acc) {
+    const bool same = o.ring == me.ri.ring;
+    if (same) {
+        int32_t diff = me.ri.p > o.p ? me.ri.p - o.p : o.p - me.ri.p;
+        if (diff == 1 || diff == me.n_ring - 1) return;
+    }
+    FixPair fp = me.fixr[me.ri.type * MAVI_MAX_TYPES + o.type];
+    if (same) fp.k_atr = 0.f;
+    float fx, fy;
+    pair_fixed<DYN>(R, fp, dxi, dyi, fx, fy);
+    acc.add(fx, fy);
+}
+
 template <int DYN>
 __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t rep, const Me<kPrecFP64, DYN>& me,
                                           double2 q, int32_t uq, int32_t, int32_t, bool mi,
@@ -883,13 +901,8 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
             }
             if (in) nb_record(C, me.uid, user_of_key(C, R, uq, o), acc);
         }
-        if (same) {
-            int32_t diff = me.ri.p > o.p ? me.ri.p - o.p : o.p - me.ri.p;
-            if (diff == 1 || diff == me.n_ring - 1) return;
-        }
-        FixPair fp = me.fixr[me.ri.type * MAVI_MAX_TYPES + o.type];
-        if (same) fp.k_atr = 0.f;
-        pair_fixed<DYN>(R, fp, dxi, dyi, fx, fy);
+        rings_pair_dxy<DYN>(R, me, o, dxi, dyi, acc);
+        return;
     } else {
         pair_fixed<DYN>(R, me.fixr[0], dxi, dyi, fx, fy);
     }

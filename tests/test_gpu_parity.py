@@ -128,6 +128,23 @@ def test_rings(mg, orc, factory, precision):
     s.close()
 
 
+@pytest.mark.parametrize("factory", ["normal", "types"])
+def test_rings_column_gather_equals_global_gather_bitwise(mg, factory):
+    """Mixed rings: the column-gather kernel and the per-chunk gather give the
+    same forces and 50-step trajectories bit for bit."""
+    out = []
+    for gather in ("columns", "global"):
+        s = rings_normal(mg, precision="mixed") if factory == "normal" else rings_types(mg, precision="mixed")
+        s.int_cfg.device.gather = gather
+        f = s.calc_forces()
+        assert s.stats().gather_mode == {"columns": 2, "global": 1}[gather]
+        n = s.handle.noise_count()
+        s.run(50, noise=np.random.default_rng(7).normal(size=n * 50))
+        out.append((f, s.state.pos.copy()))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def test_rings_bending_forces(mg, orc):
     s = rings_normal(mg, k_bend=2.0)
     ref = orc.from_system(s)
