@@ -526,8 +526,8 @@ int mavi_fma_peak(int32_t precision, int32_t device, double* flops_per_s);
  * chunks and a chunk capacity of at most 1024; larger requests return
  * MAVI_ERR_INVALID_ARG with the limit in msg. The first call on a device
  * loads this part of the library on that device (CUDA's lazy module loading),
- * which reserves the 4 MiB array there, and locates the array (set-up): make
- * that first call before any stream capture. Later calls allocate nothing.
+ * which reserves the 4 MiB array there, and locates the array: make that
+ * first call during the host's set-up. Later calls allocate nothing.
  * Every call waits for `stream` before it returns (it reads the status back).
  * A CUDA error already pending in the calling thread is returned as
  * MAVI_ERR_CUDA, named as not this call's, before anything is launched.
