@@ -1845,12 +1845,12 @@ k_pass(Ctx C, int32_t with_wall_forces) {
         count_into_chunk(C, valid, s, new_cell, cap);
 }
 
-// The mixed short-range passes with the column gather (pass mode 2): k_pass
-// with gather_columns called directly in place of the warp gathers (the same
-// terms in the same order, so the same bits), in a kernel of its own so that
-// its registers serve this gather alone (the warp-staged gather's registers
-// made k_pass spill in the column gather's loop).
-template <int DYN, int PASS, bool HAS_VEL, bool HAS_POL>
+// The mixed short-range passes with the column gather (pass mode 2, COLS) or
+// the per-chunk gather (pass mode 1): k_pass with that gather called directly
+// in place of the warp gathers (the same terms in the same order, so the same
+// bits), in a kernel of its own so that its registers serve this gather alone
+// (the warp-staged gather's registers made k_pass spill in these loops).
+template <int DYN, int PASS, bool HAS_VEL, bool HAS_POL, bool COLS>
 __global__ void __launch_bounds__(kPassThreads, DYN == MAVI_DYN_RINGS ? MAVI_PASS_BLOCKS_RINGS : MAVI_PASS_BLOCKS_MIXED)
 k_pass_cols(Ctx C, int32_t with_wall_forces) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1876,7 +1876,7 @@ k_pass_cols(Ctx C, int32_t with_wall_forces) {
     if (valid) {
         Acc<kPrecMixed, DYN> acc;
         const Me<kPrecMixed, DYN> me = make_me<kPrecMixed, DYN>(C, R, rep, s, P);
-        if (R.has_chunks) gather_columns<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
+        if (COLS && R.has_chunks) gather_columns<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
         else gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
         const float gx = acc.gx(), gy = acc.gy();
         new_cell = pass_epilogue<kPrecMixed, DYN, PASS, HAS_VEL, HAS_POL>(

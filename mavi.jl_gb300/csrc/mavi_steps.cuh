@@ -53,7 +53,7 @@ void pass(MaviSystem* s, int with_walls) {
         }
     }
     if constexpr (PREC == kPrecMixed && kColsPass<DYN, PASS>) {
-        if (s->C.gather_mode == 2 && s->lanes == 1) {
+        if ((s->C.gather_mode == 1 || s->C.gather_mode == 2) && s->lanes == 1) {
             cols_pass_mixed(s, DYN, PASS, with_walls);
             return;
         }

@@ -1,17 +1,23 @@
-// mavi_steps_cols.cu — the mixed-form short-range pair passes with the column
-// gather (k_pass_cols), in a translation unit of their own so that they
-// compile in parallel with the other pass instantiations.
+// mavi_steps_cols.cu — the mixed-form short-range pair passes with the
+// per-chunk or the column gather (k_pass_cols), in a translation unit of their
+// own so that they compile in parallel with the other pass instantiations.
 #include "mavi_system.cuh"
 
 namespace mavi {
 namespace {
 
+template <int DYN, int PASS, bool COLS>
+void launch(MaviSystem* s, int with_walls) {
+    const unsigned g = nblocks(s->M, kPassThreads);
+    if (s->has_vel) k_pass_cols<DYN, PASS, true, false, COLS><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+    else if (s->has_pol) k_pass_cols<DYN, PASS, false, true, COLS><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+    else k_pass_cols<DYN, PASS, false, false, COLS><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+}
+
 template <int DYN, int PASS>
 void launch_cols(MaviSystem* s, int with_walls) {
-    const unsigned g = nblocks(s->M, kPassThreads);
-    if (s->has_vel) k_pass_cols<DYN, PASS, true, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
-    else if (s->has_pol) k_pass_cols<DYN, PASS, false, true><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
-    else k_pass_cols<DYN, PASS, false, false><<<g, kPassThreads, 0, s->stream>>>(s->C, with_walls);
+    if (s->C.gather_mode == 2) launch<DYN, PASS, true>(s, with_walls);
+    else launch<DYN, PASS, false>(s, with_walls);
 }
 
 }  // namespace

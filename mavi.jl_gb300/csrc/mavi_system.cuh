@@ -212,7 +212,7 @@ int run_invasions(MaviSystem* s, const std::vector<int32_t>& due, bool from_sour
 void lanes_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
 // The mixed Lennard-Jones passes with the split gather (mavi_steps_split.cu).
 void split_pass_mixed(MaviSystem* s, int pass, int with_walls);
-// The mixed short-range passes with the column gather (mavi_steps_cols.cu).
+// The mixed short-range passes with the per-chunk or the column gather (mavi_steps_cols.cu).
 void cols_pass_mixed(MaviSystem* s, int dyn, int pass, int with_walls);
 // waits for the stream and turns a device error flag into a status (mavi_api.cu)
 int device_error_status(MaviSystem* s);
