@@ -109,3 +109,20 @@ def test_split_rejects_other_forms(mg):
         with pytest.raises(mg.MaviError) as e:
             s.calc_forces()
         assert e.value.status == mg.abi.MAVI_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("wall", ["rigid", "periodic"])
+def test_split_all_pairs_without_chunks(mg, orc, wall):
+    """No chunk grid (every pair of the replica is a candidate, ~400 per
+    particle, so most are evaluated in FP32): forces and a 50-step trajectory
+    against the oracle's all-pairs form."""
+    s = lj_grid(mg, 20, 20, wall=wall, chunks=False, precision="mixed")
+    s.int_cfg.device.gather = "split"
+    ref = orc.from_system(s)
+    assert rel_force_err(s.calc_forces(), ref.forces(orc.ALL_PAIRS)) < TOL
+    assert s.stats().gather_mode == 7
+    mg.run_system(s, num_steps=50)
+    ref.step(50)
+    assert np.max(np.abs(s.state.pos - ref.state()[0])) < 1e-6
+    ref.close()
+    s.close()
