@@ -882,7 +882,6 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
         acc.add2(fxh, fxl, fyh, fyl);
         return;
     }
-    float fx, fy;
     if constexpr (DYN == MAVI_DYN_RINGS) {
         RingInfo o = ring_of_key(C, R, uq);
         bool same = o.ring == me.ri.ring;
@@ -902,11 +901,11 @@ __device__ __forceinline__ void pair_term(const Ctx& C, const DevRep& R, int32_t
             if (in) nb_record(C, me.uid, user_of_key(C, R, uq, o), acc);
         }
         rings_pair_dxy<DYN>(R, me, o, dxi, dyi, acc);
-        return;
     } else {
+        float fx, fy;
         pair_fixed<DYN>(R, me.fixr[0], dxi, dyi, fx, fy);
+        acc.add(fx, fy);
     }
-    acc.add(fx, fy);
 }
 
 // Pair term of a neighbour reached through a wrapped periodic stencil on a
