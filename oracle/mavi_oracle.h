@@ -6,8 +6,9 @@
  * It is never linked into libmavi_cuda.so and nothing on the product path calls
  * it. Each function in mavi_oracle.c cites the reference file:line it follows.
  *
- * Parity status: the reference (Julia) cannot run on these machines and ships
- * no numeric golden vectors for this path. The restatement is pinned by the
+ * Parity status: parity unpinned at the golden-vector level — the reference
+ * (Julia) cannot run on these machines and ships no numeric golden vectors for
+ * this path. The restatement is pinned by the
  * reference's own self-consistency tests (chunked == all-pairs,
  * threaded == sequential; test/tests_rings/tests_general.jl:16-45) and by
  * closed-form known answers; see tests/test_oracle.py. Parity at the ULP level
