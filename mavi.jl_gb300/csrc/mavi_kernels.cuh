@@ -1159,6 +1159,10 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
 #endif
 constexpr int kSplitSlots = MAVI_SPLIT_SLOTS;   // close candidates parked per particle (8 B each per thread)
 constexpr int kSplitUnroll = MAVI_SPLIT_UNROLL;
+#ifndef MAVI_SPLIT_NEAR_UNROLL
+#define MAVI_SPLIT_NEAR_UNROLL 1
+#endif
+constexpr int kSplitNearUnroll = MAVI_SPLIT_NEAR_UNROLL;
 
 template <int DYN>
 __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
@@ -1168,8 +1172,10 @@ __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int3
     int n_near = 0;
     const float near2 = R.lj_near2, sk = R.lj_sk, ah = R.lj_ah, bh = R.lj_bh;
     // one candidate: the FP32 term on the spot, or the displacement parked
-    auto term = [&](int32_t j, int2 oj, int32_t shx, int32_t shy, bool mi) {
-        if (j == (int32_t)s) return;
+    auto term = [&](auto own, int32_t j, int2 oj, int32_t shx, int32_t shy, bool mi) {
+        if constexpr (decltype(own)::value) {   // the particle's own chunk holds the particle itself
+            if (j == (int32_t)s) return;
+        }
         int32_t dxi = (int32_t)((uint32_t)me.p.x - (uint32_t)oj.x + (uint32_t)shx);
         int32_t dyi = (int32_t)((uint32_t)me.p.y - (uint32_t)oj.y + (uint32_t)shy);
         if (mi) {   // minimum image (src/integration.jl:43-48) in exact units
@@ -1190,14 +1196,14 @@ __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int3
             fy = fmaf(sh, yf, fy);
         }
     };
-    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
+    auto visit = [&](auto own, int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi) {
 #pragma unroll kSplitUnroll
-        for (int32_t j = b; j < e; j++) term(j, P[j], shx, shy, mi);
+        for (int32_t j = b; j < e; j++) term(own, j, P[j], shx, shy, mi);
     };
     int32_t col = 0, row = 0;
     uint32_t raw_chunks = 0;   // bit 3 (dc + 1) + (dr + 1): a wrapped chunk without minimum image
     if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224): its one chunk
-        visit(C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
+        visit(std::true_type{}, C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
     } else {
         const int32_t lc = (int32_t)(cell - R.c0);
         col = lc / R.rows;
@@ -1223,7 +1229,10 @@ __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int3
                     continue;
                 }
                 const int64_t nc = R.c0 + (int64_t)ncol * R.rows + nrow;
-                visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small));
+                const int32_t b = C.start[nc], e = C.start[nc + 1];
+                const bool mi = R.min_image && (wr || R.mi_small);
+                if (dc == 0 && dr == 0) visit(std::true_type{}, b, e, 0, 0, mi);
+                else visit(std::false_type{}, b, e, -dc * R.sx_i, dr * R.sy_i, mi);
             }
         }
     }
@@ -1231,7 +1240,7 @@ __device__ __forceinline__ void gather_split(const Ctx& C, const DevRep& R, int3
         gather_global<kPrecMixed, DYN>(C, R, rep, s, cell, P, me, acc);
         return;
     }
-#pragma unroll 2
+#pragma unroll kSplitNearUnroll
     for (int k = 0; k < n_near; k++) {
         const int2 d = slots[k * kPassThreads];
         float fxh, fxl, fyh, fyl;
