@@ -950,10 +950,13 @@ template <int PREC, int DYN>
 __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int32_t rep, int64_t s, int32_t cell,
                                               const typename PartOf<PREC>::T* __restrict__ P,
                                               const Me<PREC, DYN>& me, Acc<PREC, DYN>& acc) {
-    auto visit = [&](int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi, bool raw = false,
+    // own: the particle's own chunk (the only one that holds the particle itself)
+    auto visit = [&](auto own, int32_t b, int32_t e, int32_t shx, int32_t shy, bool mi, bool raw = false,
                      long long rshx = 0, long long rshy = 0) {
         for (int32_t j = b; j < e; j++) {
-            if (j == (int32_t)s) continue;
+            if constexpr (decltype(own)::value) {
+                if (j == (int32_t)s) continue;
+            }
             int32_t uq = 0;
             if constexpr (DYN == MAVI_DYN_RINGS) uq = ring_key(C, j);
             if (raw) pair_term_raw<DYN>(C, R, rep, me, P[j], uq, rshx, rshy, acc);
@@ -961,7 +964,7 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
         }
     };
     if (!R.has_chunks) {  // all pairs inside the replica (src/integration.jl:197-224): its one chunk
-        visit(C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
+        visit(std::true_type{}, C.start[R.c0], C.start[R.c0 + 1], 0, 0, R.min_image);
         return;
     }
     int32_t lc = (int32_t)(cell - R.c0);
@@ -986,8 +989,11 @@ __device__ __forceinline__ void gather_global(const Ctx& C, const DevRep& R, int
             // centre of the neighbour chunk relative to ours, in units:
             // x grows with the column, y decreases with the row
             const bool raw = wr && !R.min_image;
-            visit(C.start[nc], C.start[nc + 1], -dc * R.sx_i, dr * R.sy_i, R.min_image && (wr || R.mi_small), raw,
-                  -(long long)(ncol - col) * R.sx_u, (long long)(nrow - row) * R.sy_u);
+            const int32_t b = C.start[nc], e = C.start[nc + 1];
+            const bool mi = R.min_image && (wr || R.mi_small);
+            if (dc == 0 && dr == 0) visit(std::true_type{}, b, e, 0, 0, mi);
+            else visit(std::false_type{}, b, e, -dc * R.sx_i, dr * R.sy_i, mi, raw,
+                       -(long long)(ncol - col) * R.sx_u, (long long)(nrow - row) * R.sy_u);
         }
     }
 }
