@@ -1144,12 +1144,12 @@ __device__ __forceinline__ void gather_columns(const Ctx& C, const DevRep& R, in
 // chunk loops as gather_global. A candidate at r >= 2 sigma (R.lj_near2,
 // units^2) is evaluated on the spot in plain FP32: its force is below
 // ~0.2 eps / sigma, so the ~10 ulp of that form stay far under the
-// double-float error of the close pairs (the first two neighbour shells). A closer candidate's exact integer
-// displacement is parked in the thread's slots of shared memory (`slots`,
-// stride kPassThreads, kSplitSlots of them) and evaluated in double-float afterwards, so the
-// costly term runs ~7-9 times per particle instead of ~33, with no divergence
-// between the two forms inside a warp, and the candidate loop carries no
-// double-float registers. Order: the close terms in candidate order into the
+// double-float error of the close pairs (the first two neighbour shells). A
+// closer candidate's exact integer displacement is parked in the thread's
+// slots of shared memory (`slots`, stride kPassThreads, kSplitSlots of them)
+// and evaluated in double-float afterwards, so the costly term runs ~7-9
+// times per particle instead of ~33, with no divergence between the two forms
+// inside a warp, and the candidate loop carries no double-float registers. Order: the close terms in candidate order into the
 // compensated sum, then the raw wrapped pairs of periodic spaces without
 // minimum image (their chunks are set aside in the first loop), then the FP32
 // sum of the far ones: fixed, so deterministic. Both particles of a pair see
