@@ -42,3 +42,17 @@ def test_cpu_baseline_at_one_core_and_all_cores(mg, orc):
         out = bench.cpu_baseline(mg, orc, r, 0.2, nthreads)
         assert out["value"] > 0 and out["cores"] == nthreads and out["kind"] == "port"
         assert ("Threaded" in out["sample"]) == (nthreads > 1)
+
+
+def test_gather_option_pins_the_mixed_form_only(mg):
+    """--gather pins the mixed form's pair gather (profiling runs); the FP64
+    form keeps the autotuner."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod2", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    bench.MIXED_GATHER = "split"
+    mixed, _ = bench.workload_share("lj_1024", "mixed")
+    fp64, _ = bench.workload_share("lj_1024", "fp64")
+    assert mixed.int_cfg.device.gather == "split" and fp64.int_cfg.device.gather == "auto"
+    assert mixed.int_cfg.device.options().gather_mode == 7
