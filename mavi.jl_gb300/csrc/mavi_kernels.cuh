@@ -406,7 +406,13 @@ static __global__ void k_scan(int32_t* __restrict__ count, int64_t n, const int3
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
     const bool full = base + kScanItems <= n;   // count is 16-byte aligned and base a multiple of 4
-    if (full) {
+    // a tile whose total is zero holds only zero counts (sparse grids: a third
+    // of the rings workload's tiles): its counts are not read
+    const bool empty = tile_sum[blockIdx.x] == 0;
+    if (empty) {
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) v[k] = 0;
+    } else if (full) {
 #pragma unroll
         for (int q = 0; q < kScanItems / 4; q++) {
             const int4 c = *reinterpret_cast<const int4*>(count + base + 4 * q);
