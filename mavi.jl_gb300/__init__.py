@@ -20,6 +20,7 @@ from .system import (
 from .init_states import fixed_speed_vel, maxwell_vel, random_vel, rectangular_grid
 from . import rings
 from . import replicas
+from . import tuning
 from . import experiments
 from .experiments import (
     CheckpointCfg, DelayedCfg, Experiment, ExperimentCfg, ManyColsCfg, load_experiment, run_experiment,

@@ -286,13 +286,17 @@ class CUDADevice:
     gather with 2 or 4 lanes per particle, partial sums combined in a fixed
     order); for the mixed Lennard-Jones passes also "split" (pairs at
     r >= 2 sigma in plain FP32, closer ones in double-float); or "auto"
-    (the fastest force pass at creation)."""
+    (the fastest force pass at creation).
+    tune_cache: a JSON file (or the MAVI_TUNE_CACHE environment variable) in
+    which "auto" records its choice per workload shape; later handles of
+    the same shape take the recorded mode without timing (tuning.py)."""
     precision: str = "fp64"
     device: int = 0
     use_graph: bool = True
     noise: str = "device"
     seed: int = 0
     gather: str = "auto"
+    tune_cache: str | None = None
 
     def options(self) -> abi.MaviOptions:
         o = abi.MaviOptions()

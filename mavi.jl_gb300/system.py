@@ -17,7 +17,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import abi
+from . import abi, tuning
 from .configs import CUDADevice, IntCfg, SpaceCfg, particle_radius, chunk_capacity
 from .states import SecondLawState, SelfPropelledState
 
@@ -129,10 +129,11 @@ class _Handle:
         if getattr(self.systems[0], "is_rings", False):
             types = np.ascontiguousarray(np.concatenate([s.state.types_array() for s in self.systems]).astype(np.int32))
         self.handle = C.c_void_p()
-        opt = device.options()
+        opt, cache, key = tuning.tuned_options(self.systems, step_kind, device)
         st = self.lib.mavi_create(C.byref(opt), n, self.params, abi.as_dptr(pos), abi.as_dptr(vel),
                                   abi.as_dptr(pol), abi.as_iptr(types), C.byref(self.handle))
         _check(self.lib, None, st, "mavi_create")
+        tuning.record(cache, key, self.stats())
         self.slot_offsets = np.cumsum([0] + [s.num_slots for s in self.systems])
         self.pol_offsets = np.cumsum([0] + [s.num_pol for s in self.systems])
         for k, s in enumerate(self.systems):   # per-replica clocks, then configuration (rings)
