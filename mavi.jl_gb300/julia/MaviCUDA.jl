@@ -117,10 +117,14 @@ Device mode for `IntCfg(device=CUDADevice())`. `precision = :fp64` runs every
 operation in double (the drop-in); `:mixed` runs the pair loop in FP32 on
 chunk-relative offsets with FP64 update, wrap and binning.
 """
+# gather: the pair pass (MaviOptions.gather_mode): -1 autotuned at creation;
+# 0-2 warp-staged / per-chunk / per-column (the same bits); 3-7 mixed-form
+# variants (tiles, tiles from a work queue, 2 or 4 lanes, split gather)
 Base.@kwdef struct CUDADevice <: DeviceMode
     precision::Symbol = :fp64
     device::Int = 0
     seed::UInt64 = 0
+    gather::Int = -1
 end
 
 # ---- packing -----------------------------------------------------------------
@@ -264,7 +268,7 @@ function handle!(system)
     haskey(HANDLES, system) && return HANDLES[system].ptr
     dev = system.int_cfg.device
     opt = COptions(dev.precision == :mixed ? PREC_MIXED : PREC_FP64, NOISE_DEVICE, dev.seed,
-                   dev.device, 1, 0, -1)   # gather: autotuned
+                   dev.device, 1, 0, dev.gather)
     params = Ref(replica_params(system))
     st = system.state
     vel, pol = _vel_ptr(st), _pol_ptr(st)
