@@ -126,3 +126,23 @@ def test_split_all_pairs_without_chunks(mg, orc, wall):
     assert np.max(np.abs(s.state.pos - ref.state()[0])) < 1e-6
     ref.close()
     s.close()
+
+
+def test_split_forces_on_a_melted_batch(mg, orc):
+    """After 3,000 steps (the jittered lattices have melted into liquids at
+    T = 0.3-1.0: more close pairs, disordered shells) the split gather's
+    forces still agree with the oracle's FP64 forces on the same positions.
+    (Periodic circles are left out: with no wall and no wrap, particles leave
+    their grid within ~2,700 steps, the reference's BoundsError.)"""
+    systems, step = _batch("split", num_replicas=9, n_min=2000, n_max=12000,
+                           quadrants=("rigid_rect", "periodic_rect", "rigid_circle"))
+    b = mg.SystemBatch(systems, step)
+    b.run(3000)
+    forces = b.calc_forces()
+    assert b.handle.stats().gather_mode == 7
+    for k, s in enumerate(systems):
+        ref = orc.from_system(s, nthreads=NT, step_kind=step.kind)
+        err = rel_force_err(forces[k], ref.forces(orc.THREADED))
+        assert err < TOL, (k, err)
+        ref.close()
+    b.close()
